@@ -1,0 +1,277 @@
+"""DRMLT hot-path benchmark: mutations/s of the GPU chain loop on one GB300.
+
+Workload (default): the H2MC second-stage configuration -- the Phong Cornell
+box (34 + 2 triangles) at 1024x1024, max depth 8, 16384 chains, type=mira,
+stage-2 anisotropic probability 0.5, sigma 1/64 -- written by
+drmlt/scenegen.py:config2 from a fixed seed (synthetic scene; the reference
+publishes no benchmark scene). One step = one DR iteration of every chain
+(16384 mutations). `value` is device-timed mutations/s over K steps with the
+chain state resident in HBM; `e2e` is the same metric through the public C ABI
+from host buffers (scene upload, prepass, direct pass, K steps, film readback).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank renders its own shard of chains (different
+random streams) and the films are summed; chains are independent, so there is
+no collective in the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "drmlt-dpt_gb300"))
+
+import numpy as np  # noqa: E402
+
+PEAKS_PATH = os.path.join(REPO, "MEASURED_PEAKS.json")
+WORKLOAD = "drmlt-h2mc-phong-cornell-1024x1024-depth8-16384chains-mira"
+METRIC = "mutations_per_second"
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def write_workload(tmp: str, spp: int = 64) -> str:
+    from drmlt import scenegen
+    return scenegen.write_cornell(os.path.join(tmp, "cfg2"), seed=2, width=1024, height=1024, phong=True,
+                                  options=scenegen.SceneOptions(maxdepth=8, numchains=16384, spp=spp, type="mira"))
+
+
+# Algorithmic bytes each stage moves per chain (read + write of chain state in
+# HBM). A Slot is 340 B, the scratch 112 B, a
+# stored FP64 Gaussian 4.9 KB.
+SLOT_B = 340
+SCRATCH_B = 112
+GAUSS_B = 8 * (24 * 24 + 2 * 24 + 2)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    tmp = tempfile.mkdtemp()
+    xml = write_workload(tmp)
+    sd = dscene.load_scene(xml)
+    seed = 0x1234ABCD + 7919 * rank
+
+    # ---- device-timed throughput (chain state resident in HBM)
+    r = Renderer(sd, device=local, seed=seed)
+    r.direct()
+    r.prepass()
+    r.run(args.warmup)
+    prof, prof_mut = r.profile(max(1, min(8, args.steps)))  # per-stage CUDA-event times (serialised)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        done = r.run(args.steps)
+        wall = time.perf_counter() - t0
+    dev_ms = r.last_run_ms()
+    torch.cuda.synchronize()
+    stats = r.stats()
+    r.close()
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        n = torch.tensor([done], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(n)
+        done_all = int(n.item())
+    else:
+        done_all = done
+    value = done_all / (dev_ms * 1e-3)
+
+    # ---- end to end through the C ABI: host scene -> film on the host
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    r2 = Renderer(sd, device=local, seed=seed + 1)
+    r2.direct()
+    r2.prepass()
+    e_done = r2.run(args.steps)
+    film = r2.film()
+    e2e_s = time.perf_counter() - t0
+    r2.close()
+    scene_bytes = sd.positions.nbytes + sd.normals.nbytes + 64 * 4
+    e2e = {"value": done / e2e_s * world, "unit": "mutations/s", "h2d_bytes_per_step": scene_bytes // args.steps,
+           "d2h_bytes_per_step": film.nbytes // args.steps}
+
+    # ---- roofline of the dominant stage kernel
+    hbm, peak_kind = _peaks()
+    stage_bytes = {
+        "stage1": 16384 * (2 * SLOT_B + SCRATCH_B),
+        "stage2": 16384 * (2 * SLOT_B + SCRATCH_B),
+        "finish": 16384 * (3 * SLOT_B + SCRATCH_B),
+        "derivs_x": 0, "derivs_z": 0, "gauss_x": 0, "gauss_z": 0,
+    }
+    iters = max(1, prof_mut // 16384)
+    dom = max(prof, key=prof.get)
+    per_launch_ms = prof[dom] / iters
+    # derivative / Gaussian stages: bytes = path records read + grad/Hessian or Gaussian written per listed chain
+    if dom.startswith("derivs"):
+        listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // 16384)) if stats["mutations"] else 1
+        stage_bytes[dom] = listed * (SLOT_B + 4 * (24 + 576))
+    if dom.startswith("gauss"):
+        listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // 16384)) if stats["mutations"] else 1
+        stage_bytes[dom] = listed * (4 * (24 + 576) + GAUSS_B)
+    achieved = stage_bytes[dom] / (per_launch_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+            "stage_ms_per_iteration": {k: v / iters for k, v in prof.items()}}
+
+    out = None
+    if rank == 0:
+        cpu = cpu_baseline_sample(xml) if not args.no_cpu else None
+        out = {
+            "metric": METRIC, "value": value, "unit": "mutations/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "chains": 16384, "width": 1024, "height": 1024, "max_depth": 8,
+                       "dr_type": "mira", "mutations_per_step": 16384 * world,
+                       "l2": "chain state (3 slots + 3 FP64 Gaussians per chain, 0.27 GB) exceeds L2"},
+            "e2e": e2e,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": 8 * args.steps,
+            "wall_s_timed_region": wall,
+            "acceptance": {k: stats[k + "_accepted"] / max(1, stats[k])
+                           for k in ("large_step", "stage1", "stage2_iso", "stage2_h2mc")},
+        }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def cpu_baseline_sample(xml: str, seconds: float = 15.0):
+    """The oracle's CPU restatement of the chain loop on this host's cores, on a
+    bounded sample of the same workload."""
+    try:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle_dr  # noqa: WPS433
+    except Exception as e:  # oracle not built on this machine
+        return {"value": None, "unit": "mutations/s", "cores": 0, "kind": "port", "sample": "unavailable: %s" % e}
+    return oracle_dr.cpu_throughput(xml, seconds=seconds)
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the reference's CPU algorithm (oracle restatement, all host
+    cores) on the same workload, metric and unit."""
+    if rank != 0:
+        return None
+    tmp = tempfile.mkdtemp()
+    xml = write_workload(tmp)
+    try:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle_dr
+    except Exception as e:
+        return {"impl": "reference", "unavailable": "oracle CPU port not built: %s" % e}
+    per = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        oracle_dr.cpu_throughput(xml, seconds=per)
+    vals = [oracle_dr.cpu_throughput(xml, seconds=per) for _ in range(args.steps)]
+    v = statistics.median([x["value"] for x in vals])
+    cpu = dict(vals[0])
+    cpu["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "mutations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD}, "cpu_baseline": cpu,
+            "e2e": {"value": v, "unit": "mutations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+    else:
+        out = run_ours(args, world, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,312 @@
+// Single-precision BSDF, light and camera evaluation used by the path tracer.
+// Each function states the reference routine whose arithmetic it reproduces.
+#pragma once
+#include "trace.cuh"
+
+namespace drmlt {
+
+struct BsdfOut {
+    V3 contrib;
+    float cosWo, pdf, revPdf;
+};
+
+DEV V3 kd_of(const Bsdf &b) { return V3(b.kd[0], b.kd[1], b.kd[2]); }
+DEV V3 ks_of(const Bsdf &b) { return V3(b.ks[0], b.ks[1], b.ks[2]); }
+
+// Lambertian::Evaluate (src/lambertian.cpp:15-38), Phong::Evaluate (src/phong.cpp:21-62).
+DEV void bsdf_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &wo, BsdfOut &o) {
+    o.contrib = V3(0.0f, 0.0f, 0.0f);
+    o.pdf = 0.0f;
+    o.revPdf = 0.0f;
+    float cosWi = dot(normal, wi);
+    V3 n = normal;
+    if (b.twoSided && cosWi < 0.0f) {
+        cosWi = -cosWi;
+        n = -n;
+    }
+    o.cosWo = dot(n, wo);
+    if (b.type == kBsdfLambertian) {
+        if (cosWi < kCosEps || o.cosWo < kCosEps) return;
+        const float fwd = o.cosWo * kInvPi;
+        o.contrib = fwd * kd_of(b);
+        o.pdf = fwd;
+        o.revPdf = cosWi * kInvPi;
+        return;
+    }
+    // Phong
+    if (cosWi <= kCosEps || o.cosWo <= kCosEps) return;
+    if (b.ksWeight > 0.0f) {
+        const float alpha = fmaxf(dot(reflect(wi, n), wo), 0.0f);
+        const float weight = powf(alpha, b.exponent) * kInvTwoPi;
+        if (weight > 1e-10f) {
+            o.contrib = ks_of(b) * ((b.exponent + 2.0f) * weight);
+            o.pdf = b.ksWeight * (b.exponent + 1.0f) * weight;
+            o.revPdf = o.pdf;
+        }
+    }
+    if (b.ksWeight < 1.0f) {
+        o.pdf += (1.0f - b.ksWeight) * o.cosWo * kInvPi;
+        o.revPdf += (1.0f - b.ksWeight) * cosWi * kInvPi;
+        o.contrib = o.contrib + kd_of(b) * kInvPi;
+    }
+    o.contrib = o.contrib * o.cosWo;
+    if (max_coeff(o.contrib) < 1e-10f) o.contrib = V3(0.0f, 0.0f, 0.0f);
+}
+
+// Lambertian::Sample (src/lambertian.cpp:56-90), Phong::Sample (src/phong.cpp:64-147).
+DEV bool bsdf_sample(const Bsdf &b, const V3 &wi, const V3 &normal, float r0, float r1, float uDiscrete,
+                     V3 &wo, BsdfOut &o) {
+    float cosWi = dot(wi, normal);
+    if (fabsf(cosWi) < kCosEps) return false;
+    V3 n = normal;
+    if (cosWi < 0.0f) {
+        if (b.twoSided) {
+            cosWi = -cosWi;
+            n = -n;
+        } else {
+            return false;
+        }
+    }
+    if (b.type == kBsdfLambertian) {
+        V3 b0, b1;
+        coordinate_system(n, b0, b1);
+        const V3 l = sample_cos_hemisphere(r0, r1);
+        wo = l.x * b0 + l.y * b1 + l.z * n;
+        o.cosWo = l.z;
+        o.pdf = l.z * kInvPi;
+        if (o.cosWo < kCosEps) return false;
+        o.revPdf = cosWi * kInvPi;
+        o.contrib = kd_of(b);
+        return true;
+    }
+    const V3 R = reflect(wi, n);
+    float g;
+    V3 axis;
+    if (uDiscrete > b.ksWeight) {
+        g = 1.0f;
+        axis = n;
+    } else {
+        g = b.exponent;
+        axis = R;
+    }
+    const float power = 1.0f / (g + 1.0f);
+    const float cosAlpha = powf(r1, power);
+    const float sinAlpha = sqrtf(1.0f - sq(cosAlpha));
+    const float phi = kTwoPi * r0;
+    const V3 local(sinAlpha * cosf(phi), sinAlpha * sinf(phi), cosAlpha);
+    V3 b0, b1;
+    coordinate_system(axis, b0, b1);
+    wo = local.x * b0 + local.y * b1 + local.z * axis;
+    o.cosWo = dot(n, wo);
+    if (o.cosWo < kCosEps) return false;
+    o.contrib = V3(0.0f, 0.0f, 0.0f);
+    o.pdf = 0.0f;
+    o.revPdf = 0.0f;
+    if (b.ksWeight > 0.0f) {
+        const float alpha = fmaxf(dot(R, wo), 0.0f);
+        const float weight = powf(alpha, b.exponent) * kInvTwoPi;
+        if (weight > 1e-10f) {
+            o.contrib = ks_of(b) * ((b.exponent + 2.0f) * weight);
+            o.pdf = b.ksWeight * (b.exponent + 1.0f) * weight;
+        }
+        o.revPdf = o.pdf;
+    }
+    if (b.ksWeight < 1.0f) {
+        o.contrib = o.contrib + kd_of(b) * kInvPi;
+        o.pdf += (1.0f - b.ksWeight) * o.cosWo * kInvPi;
+        o.revPdf += (1.0f - b.ksWeight) * cosWi * kInvPi;
+    }
+    o.contrib = o.contrib * o.cosWo;
+    if (o.pdf < 1e-10f) return false;
+    o.contrib = o.contrib * (1.0f / o.pdf);
+    return true;
+}
+
+// BSDF::Roughness: Lambertian 1 (src/lambertian.h:38-40), Phong (src/phong.cpp:149-156).
+DEV float bsdf_roughness(const Bsdf &b, float uDiscrete) {
+    if (b.type == kBsdfPhong && uDiscrete < b.ksWeight) return sqrtf(2.0f / (2.0f + 4.0f * b.exponent));
+    return 1.0f;
+}
+
+// ShadingNormalCorrection<adjoint> of src/path.cpp:39-59.
+template <bool adjoint>
+DEV float shading_normal_correction(const V3 &wi, const Isect &isect, const V3 &wo) {
+    const float cosWi = dot(isect.shadingNormal, wi);
+    const float cosWo = dot(isect.shadingNormal, wo);
+    const float wiDotGeoN = dot(isect.geomNormal, wi);
+    const float woDotGeoN = dot(isect.geomNormal, wo);
+    if (wiDotGeoN * cosWi <= 0.0f || woDotGeoN * cosWo <= 0.0f) return 0.0f;
+    if (adjoint) return fabsf((woDotGeoN * cosWi) / (wiDotGeoN * cosWo));
+    return 1.0f;
+}
+
+// ---------------------------------------------------------------- lights
+// PiecewiseConstant1D::SampleDiscrete (src/distribution.h:45-51): upper_bound on the CDF.
+DEV int sample_discrete(const float *cdf, int count, float u) {
+    int lo = 0, hi = count + 1;   // first index with cdf[i] > u
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid) > u) hi = mid; else lo = mid + 1;
+    }
+    int off = lo - 1;
+    return off < 0 ? 0 : (off > count - 1 ? count - 1 : off);
+}
+
+// PickLight / PickLightProb (src/scene.cpp:113-121).
+DEV int pick_light(const SceneView &s, float u, float &prob) {
+    const int id = sample_discrete(s.lightCdf, s.numLights, u);
+    prob = s.lightFunc[id] / (s.lightFuncInt * float(s.numLights));
+    return id;
+}
+DEV float pick_light_prob(const SceneView &s, int light) {
+    return s.lights[light].samplingWeight / s.lightWeightSum;
+}
+
+// TriangleMesh::Sample(rndParam, ...) + SampleDirect (src/trianglemesh.cpp:315-364).
+DEV void sample_triangle(const SceneView &s, int tri, float r0, float r1, V3 &pos, V3 &normal) {
+    const float *P = s.triP + 9 * tri;
+    const V3 p0 = ld3(P), e1 = ld3(P + 3), e2 = ld3(P + 6);
+    const float *N = s.triN + 9 * tri;
+    const float a = sqrtf(1.0f - r0);
+    const float b1 = 1.0f - a;
+    const float b2 = a * r1;
+    pos = p0 + (e1 * b1) + (e2 * b2);
+    normal = normalize(V3(ld3(N) * (1.0f - b1 - b2) + ld3(N + 3) * b1 + ld3(N + 6) * b2));
+}
+
+// TriangleMesh::GetSampleParam (src/trianglemesh.cpp:238-296).
+DEV void triangle_sample_param(const SceneView &s, int tri, const V3 &position, float &u0, float &u1) {
+    const float *P = s.triP + 9 * tri;
+    const V3 p0 = ld3(P), e1 = ld3(P + 3), e2 = ld3(P + 6);
+    const V3 e0 = position - p0;
+    const float d11 = dot(e1, e1), d12 = dot(e1, e2), d22 = dot(e2, e2);
+    const float d01 = dot(e0, e1), d02 = dot(e0, e2);
+    const float invDenom = 1.0f / (d11 * d22 - d12 * d12);
+    const float b1 = (d22 * d01 - d12 * d02) * invDenom;
+    const float b2 = (d11 * d02 - d12 * d01) * invDenom;
+    const float a = 1.0f - b1;
+    u0 = 1.0f - sq(a);
+    u1 = b2 / a;
+}
+
+DEV int light_tri(const SceneView &s, const Light &L, int lPrim) {
+    return s.shapes[L.shape].triOffset + lPrim;
+}
+
+// AreaLight::SampleDirect (src/arealight.cpp:29-57).
+DEV bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &pos, float r0, float r1,
+                             V3 &dirToLight, float &dist, V3 &contrib, float &cosAtLight,
+                             float &directPdf, float &emissionPdf) {
+    const Light &L = s.lights[li];
+    if (L.type == kLightArea) {
+        V3 p, n;
+        sample_triangle(s, light_tri(s, L, lPrim), r0, r1, p, n);
+        const float shapePdf = L.invTotalArea;
+        dirToLight = p - pos;
+        const float distSq = length_sq(dirToLight);
+        dist = sqrtf(distSq);
+        dirToLight = V3(dirToLight.x / dist, dirToLight.y / dist, dirToLight.z / dist);
+        cosAtLight = -dot(dirToLight, n);
+        if (cosAtLight > kCosEps) {
+            contrib = (cosAtLight / (distSq * shapePdf)) * V3(L.emission[0], L.emission[1], L.emission[2]);
+            directPdf = shapePdf * distSq / cosAtLight;
+            emissionPdf = shapePdf * cosAtLight * kInvPi;
+            return true;
+        }
+        return false;
+    }
+    // PointLight::SampleDirect (src/pointlight.cpp): delta light at a position.
+    const V3 lp(L.pos[0], L.pos[1], L.pos[2]);
+    dirToLight = lp - pos;
+    const float distSq = length_sq(dirToLight);
+    dist = sqrtf(distSq);
+    dirToLight = V3(dirToLight.x / dist, dirToLight.y / dist, dirToLight.z / dist);
+    contrib = V3(L.emission[0], L.emission[1], L.emission[2]) * (1.0f / distSq);
+    cosAtLight = 1.0f;
+    directPdf = distSq;
+    emissionPdf = 1.0f / (4.0f * kPi);
+    return true;
+}
+
+// AreaLight::Emission (src/arealight.cpp:59-76).
+DEV void light_emission(const SceneView &s, int li, const V3 &dirToLight, const V3 &normalOnLight, V3 &emission,
+                        float &directPdf, float &emissionPdf) {
+    const Light &L = s.lights[li];
+    const float cosAtLight = -dot(normalOnLight, dirToLight);
+    if (L.type == kLightArea && cosAtLight > 0.0f) {
+        emission = V3(L.emission[0], L.emission[1], L.emission[2]);
+        directPdf = L.invTotalArea;
+        emissionPdf = cosAtLight * directPdf * kInvPi;
+    } else {
+        emission = V3(0.0f, 0.0f, 0.0f);
+        directPdf = 0.0f;
+        emissionPdf = 0.0f;
+    }
+}
+
+// AreaLight::Emit (src/arealight.cpp:78-102).
+DEV void light_emit(const SceneView &s, int li, int lPrim, float p0, float p1, float d0, float d1, V3 &org,
+                    V3 &dir, V3 &emission, float &cosAtLight, float &emissionPdf, float &directPdf) {
+    const Light &L = s.lights[li];
+    if (L.type == kLightPoint) {  // PointLight::Emit (src/pointlight.cpp:58-72)
+        float jac;
+        org = V3(L.pos[0], L.pos[1], L.pos[2]);
+        dir = sample_sphere(d0, d1, jac);
+        emission = V3(L.emission[0], L.emission[1], L.emission[2]);
+        emissionPdf = 1.0f / (4.0f * kPi);
+        cosAtLight = directPdf = 1.0f;
+        return;
+    }
+    V3 normal;
+    sample_triangle(s, light_tri(s, L, lPrim), p0, p1, org, normal);
+    const float shapePdf = L.invTotalArea;
+    const V3 d = sample_cos_hemisphere(d0, d1);
+    V3 b0, b1;
+    coordinate_system(normal, b0, b1);
+    dir = d.x * b0 + d.y * b1 + d.z * normal;
+    emission = V3(L.emission[0], L.emission[1], L.emission[2]) * (kPi / shapePdf);
+    cosAtLight = d.z;
+    emissionPdf = d.z * kInvPi * shapePdf;
+    directPdf = shapePdf;
+}
+
+DEV bool light_is_delta(const SceneView &s, int li) { return s.lights[li].type == kLightPoint; }
+DEV bool light_is_finite(const SceneView &s, int li) { return s.lights[li].type == kLightArea; }
+
+// ---------------------------------------------------------------- camera
+DEV V3 xform_point(const float *m, const V3 &p) {
+    const float x = m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3];
+    const float y = m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7];
+    const float z = m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11];
+    const float w = m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15];
+    const float invW = 1.0f / w;
+    return V3(x * invW, y * invW, z * invW);
+}
+DEV V3 xform_vector(const float *m, const V3 &v) {
+    return V3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+              m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+
+// SamplePrimary (src/camera.cpp:38-49).
+DEV void sample_primary(const Camera &c, float sx, float sy, V3 &org, V3 &dir, float &minT, float &maxT) {
+    const V3 o = xform_point(c.sampleToCam, V3(sx, sy, 0.0f));
+    const V3 d = normalize(o);
+    const float invZ = 1.0f / d.z;
+    org = xform_point(c.camToWorld, V3(0.0f, 0.0f, 0.0f));
+    dir = xform_vector(c.camToWorld, d);
+    minT = c.nearClip * invZ;
+    maxT = c.farClip * invZ;
+}
+
+// ProjectPoint (src/camera.cpp:58-75).
+DEV bool project_point(const Camera &c, const V3 &p, float &sx, float &sy) {
+    const V3 camP = xform_point(c.worldToCam, p);
+    if (camP.z < c.nearClip || camP.z > c.farClip) return false;
+    const V3 r = xform_point(c.camToSample, camP);
+    if (r.x < 0.0f || r.x > 1.0f || r.y < 0.0f || r.y > 1.0f) return false;
+    sx = r.x;
+    sy = r.y;
+    return true;
+}
+
+}  // namespace drmlt

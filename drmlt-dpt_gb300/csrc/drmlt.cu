@@ -1,0 +1,638 @@
+// Host side of libdrmlt.so: scene upload, prepass orchestration, the chain
+// iteration schedule and the C ABI declared in include/drmlt_capi.h.
+#include "drmlt_capi.h"
+#include "kernels.cuh"
+#include "bvh.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace drmlt;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string &msg) {
+    g_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(DRMLT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+    } while (0)
+
+template <class T>
+int dalloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return fail(DRMLT_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return DRMLT_OK;
+}
+
+template <class T>
+int upload(T **p, const T *src, size_t n) {
+    int rc = dalloc(p, n);
+    if (rc) return rc;
+    if (n) CK(cudaMemcpy(*p, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return DRMLT_OK;
+}
+
+// PiecewiseConstant1D construction (src/distribution.h:9-25) in single precision.
+void piecewise_constant(const std::vector<float> &f, std::vector<float> &cdf, float &funcInt) {
+    const int n = int(f.size());
+    cdf.assign(n + 1, 0.0f);
+    for (int i = 1; i < n + 1; i++) cdf[i] = cdf[i - 1] + f[i - 1] / float(n);
+    funcInt = cdf[n];
+    if (funcInt == 0.0f) {
+        for (int i = 1; i < n + 1; i++) cdf[i] = float(i) / float(n);
+    } else {
+        for (int i = 1; i < n + 1; i++) cdf[i] /= funcInt;
+    }
+}
+
+struct Renderer {
+    drmlt_options opt{};
+    SceneView sv{};
+    int N = 0;
+    int W = 0, H = 0;
+    std::vector<void *> owned;
+    ChainView cv{};
+    float b = 0.0f;
+    bool prepassDone = false;
+    bool directDone = false;
+    long long samplesPerChain = 0, extraChains = 0;
+    long long iterDone = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float lastRunMs = 0.0f;
+    cudaGraphExec_t graph = nullptr;
+    int *dIter = nullptr;
+    unsigned long long bootSeed = 0;
+
+    template <class T>
+    int alloc(T **p, size_t n) {
+        int rc = dalloc(p, n);
+        if (!rc) owned.push_back(*p);
+        return rc;
+    }
+    template <class T>
+    int up(T **p, const T *src, size_t n) {
+        int rc = upload(p, src, n);
+        if (!rc) owned.push_back(*p);
+        return rc;
+    }
+    ~Renderer() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void *p : owned) cudaFree(p);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    RunParams params() const {
+        RunParams p;
+        p.s = sv;
+        p.d = cv;
+        p.N = N;
+        p.samplesPerChain = samplesPerChain;
+        p.extraChains = extraChains;
+        p.b = b;
+        p.sigma1 = opt.perturb_stddev;
+        p.sigma2 = opt.aniso_perturb_stddev;
+        p.largeProb = opt.large_step_prob;
+        p.anisoProb = opt.aniso_perturb_prob;
+        p.drType = opt.dr_type;
+        p.integrator = opt.integrator;
+        p.uniformMix = opt.uniform_mixing_prob;
+        p.accMap = opt.acceptance_map;
+        p.maxDerv = opt.max_derivative_depth;
+        p.seed = opt.seed;
+        return p;
+    }
+
+    int create(const drmlt_scene_desc *sd, const drmlt_options *o) {
+        opt = *o;
+        if (sd->num_tris <= 0 || sd->num_lights <= 0 || sd->width <= 0 || sd->height <= 0)
+            return fail(DRMLT_E_ARG, "scene needs triangles, a light and a film size");
+        if (opt.max_depth > kMaxLen || opt.max_depth < 3)
+            return fail(DRMLT_E_ARG, "max_depth must be in [3, 12]");
+        if (opt.num_chains <= 0) return fail(DRMLT_E_ARG, "num_chains must be positive");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+            return fail(DRMLT_E_CUDA, "no CUDA device available");
+        CK(cudaSetDevice(opt.device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&ev0));
+        CK(cudaEventCreate(&ev1));
+        W = sd->width;
+        H = sd->height;
+        const int T = sd->num_tris;
+        // triangles: p0, e1 = p1 - p0, e2 = p2 - p0 (single precision, as TriangleMesh)
+        std::vector<float> triP(9 * size_t(T)), triN(9 * size_t(T));
+        std::vector<int> triShape(T, -1);
+        for (int t = 0; t < T; t++) {
+            const float *v = sd->positions + 9 * size_t(t);
+            for (int k = 0; k < 3; k++) {
+                triP[9 * t + k] = v[k];
+                triP[9 * t + 3 + k] = v[3 + k] - v[k];
+                triP[9 * t + 6 + k] = v[6 + k] - v[k];
+            }
+            std::memcpy(&triN[9 * t], sd->normals + 9 * size_t(t), 9 * sizeof(float));
+        }
+        std::vector<Shape> shapes(sd->num_shapes);
+        for (int s = 0; s < sd->num_shapes; s++) {
+            shapes[s].bsdf = sd->shape_bsdf[s];
+            shapes[s].areaLight = sd->shape_light[s];
+            shapes[s].triOffset = sd->shape_first_tri[s];
+            shapes[s].numTris = sd->shape_num_tris[s];
+            if (shapes[s].bsdf < 0 || shapes[s].bsdf >= sd->num_bsdfs) return fail(DRMLT_E_ARG, "bad shape bsdf");
+            for (int t = 0; t < shapes[s].numTris; t++) {
+                const int g = shapes[s].triOffset + t;
+                if (g < 0 || g >= T) return fail(DRMLT_E_ARG, "shape triangle range out of bounds");
+                triShape[g] = s;
+            }
+        }
+        for (int t = 0; t < T; t++)
+            if (triShape[t] < 0) return fail(DRMLT_E_ARG, "triangle without shape");
+        std::vector<Bsdf> bsdfs(sd->num_bsdfs);
+        for (int i = 0; i < sd->num_bsdfs; i++) {
+            const drmlt_bsdf &in = sd->bsdfs[i];
+            Bsdf &b0 = bsdfs[i];
+            std::memset(&b0, 0, sizeof(Bsdf));
+            b0.type = in.type;
+            if (in.type == DRMLT_BSDF_ROUGHDIELECTRIC) return fail(DRMLT_E_ARG, "roughdielectric is not supported yet");
+            b0.twoSided = in.two_sided;
+            for (int k = 0; k < 3; k++) {
+                b0.kd[k] = in.kd[k];
+                b0.ks[k] = in.ks[k];
+                b0.kt[k] = in.kt[k];
+            }
+            b0.exponent = in.exponent;
+            // Phong::GetKsWeight (src/phong.cpp:158-167) on the constant textures
+            const float ksAvg = in.ks[0] * 0.212671f + in.ks[1] * 0.715160f + in.ks[2] * 0.072169f;
+            const float kdAvg = in.kd[0] * 0.212671f + in.kd[1] * 0.715160f + in.kd[2] * 0.072169f;
+            const float sum = ksAvg + kdAvg;
+            b0.ksWeight = in.type == DRMLT_BSDF_PHONG ? (sum <= 0.0f ? 0.0f : ksAvg / sum) : 0.0f;
+            b0.intIOR = in.int_ior;
+            b0.extIOR = in.ext_ior;
+            b0.alpha = in.alpha;
+        }
+        // lights, light pick distribution and per-area-light triangle CDFs
+        std::vector<Light> lights(sd->num_lights);
+        std::vector<float> lightFunc(sd->num_lights), lightTriCdf;
+        float weightSum = 0.0f;
+        for (int i = 0; i < sd->num_lights; i++) {
+            const drmlt_light &in = sd->lights[i];
+            Light &L = lights[i];
+            std::memset(&L, 0, sizeof(Light));
+            L.type = in.type;
+            L.shape = in.shape;
+            for (int k = 0; k < 3; k++) {
+                L.emission[k] = in.emission[k];
+                L.pos[k] = in.pos[k];
+            }
+            L.samplingWeight = in.sampling_weight;
+            lightFunc[i] = in.sampling_weight;
+            weightSum += in.sampling_weight;
+            if (in.type == DRMLT_LIGHT_AREA) {
+                if (in.shape < 0 || in.shape >= sd->num_shapes) return fail(DRMLT_E_ARG, "area light shape");
+                const Shape &sh = shapes[in.shape];
+                // TriangleMesh::SetAreaLight (src/trianglemesh.cpp:298-311)
+                std::vector<float> area(sh.numTris);
+                float total = 0.0f;
+                for (int t = 0; t < sh.numTris; t++) {
+                    const float *P = &triP[9 * size_t(sh.triOffset + t)];
+                    const float cx = P[4] * P[8] - P[5] * P[7];
+                    const float cy = P[5] * P[6] - P[3] * P[8];
+                    const float cz = P[3] * P[7] - P[4] * P[6];
+                    area[t] = 0.5f * std::sqrt(cx * cx + cy * cy + cz * cz);
+                    total += area[t];
+                }
+                std::vector<float> cdf;
+                float fi;
+                piecewise_constant(area, cdf, fi);
+                L.triCdfOffset = int(lightTriCdf.size());
+                L.numTris = sh.numTris;
+                L.invTotalArea = 1.0f / total;
+                lightTriCdf.insert(lightTriCdf.end(), cdf.begin(), cdf.end());
+            } else if (in.type != DRMLT_LIGHT_POINT) {
+                return fail(DRMLT_E_ARG, "only area and point lights are supported yet");
+            }
+        }
+        std::vector<float> lightCdf;
+        float lightFuncInt;
+        piecewise_constant(lightFunc, lightCdf, lightFuncInt);
+        // BVH
+        std::vector<BvhNode> nodes;
+        std::vector<Tri> tris;
+        BuildBvh(triP.data(), triShape.data(), T, nodes, tris);
+        Tri *dTris;
+        float *dTriN, *dTriP, *dLightCdf, *dLightFunc, *dLightTriCdf;
+        int *dTriShape;
+        BvhNode *dNodes;
+        Shape *dShapes;
+        Bsdf *dBsdfs;
+        Light *dLights;
+        int rc;
+        if ((rc = up(&dTris, tris.data(), tris.size()))) return rc;
+        if ((rc = up(&dTriN, triN.data(), triN.size()))) return rc;
+        if ((rc = up(&dTriP, triP.data(), triP.size()))) return rc;
+        if ((rc = up(&dTriShape, triShape.data(), triShape.size()))) return rc;
+        if ((rc = up(&dNodes, nodes.data(), nodes.size()))) return rc;
+        if ((rc = up(&dShapes, shapes.data(), shapes.size()))) return rc;
+        if ((rc = up(&dBsdfs, bsdfs.data(), bsdfs.size()))) return rc;
+        if ((rc = up(&dLights, lights.data(), lights.size()))) return rc;
+        if ((rc = up(&dLightCdf, lightCdf.data(), lightCdf.size()))) return rc;
+        if ((rc = up(&dLightFunc, lightFunc.data(), lightFunc.size()))) return rc;
+        if ((rc = up(&dLightTriCdf, lightTriCdf.data(), lightTriCdf.size()))) return rc;
+        sv.tris = dTris;
+        sv.triN = dTriN;
+        sv.triP = dTriP;
+        sv.triShape = dTriShape;
+        sv.nodes = dNodes;
+        sv.shapes = dShapes;
+        sv.bsdfs = dBsdfs;
+        sv.lights = dLights;
+        sv.lightCdf = dLightCdf;
+        sv.lightFunc = dLightFunc;
+        sv.lightTriCdf = dLightTriCdf;
+        sv.numLights = sd->num_lights;
+        sv.numTris = T;
+        sv.lightFuncInt = lightFuncInt;
+        sv.lightWeightSum = weightSum;
+        for (int k = 0; k < 3; k++) sv.bsCenter[k] = sd->bsphere_center[k];
+        sv.bsRadius = sd->bsphere_radius;
+        std::memcpy(sv.cam.sampleToCam, sd->sample_to_cam, 64);
+        std::memcpy(sv.cam.camToSample, sd->cam_to_sample, 64);
+        std::memcpy(sv.cam.camToWorld, sd->cam_to_world, 64);
+        std::memcpy(sv.cam.worldToCam, sd->world_to_cam, 64);
+        sv.cam.dist = sd->cam_dist;
+        sv.cam.nearClip = sd->near_clip;
+        sv.cam.farClip = sd->far_clip;
+        sv.cam.width = W;
+        sv.cam.height = H;
+        sv.opt.roughnessThreshold = opt.roughness_threshold;
+        sv.opt.useLightCoordinateSampling = opt.use_light_coordinate_sampling;
+        sv.opt.discreteStdDev = opt.discrete_stddev;
+        sv.opt.minDepth = opt.min_depth;
+        sv.opt.maxDepth = opt.max_depth;
+        // chain state
+        N = opt.num_chains;
+        if ((rc = alloc(&cv.slots, size_t(N) * 3))) return rc;
+        if ((rc = alloc(&cv.gauss, size_t(N) * 3 * kGaussStride))) return rc;
+        if ((rc = alloc(&cv.perm, size_t(N) * 3))) return rc;
+        if ((rc = alloc(&cv.scr, size_t(N)))) return rc;
+        if ((rc = alloc(&cv.listX, size_t(N)))) return rc;
+        if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
+        if ((rc = alloc(&cv.counters, 4))) return rc;
+        if ((rc = alloc(&cv.grad, size_t(N) * kMaxDim))) return rc;
+        if ((rc = alloc(&cv.hess, size_t(N) * kMaxDim * kMaxDim))) return rc;
+        if ((rc = alloc(&cv.stats, kNumStats))) return rc;
+        if ((rc = alloc(&cv.film, size_t(W) * H * 3))) return rc;
+        if ((rc = alloc(&cv.direct, size_t(W) * H * 3))) return rc;
+        CK(cudaMemset(cv.stats, 0, kNumStats * sizeof(unsigned long long)));
+        CK(cudaMemset(cv.film, 0, size_t(W) * H * 3 * sizeof(float)));
+        CK(cudaMemset(cv.direct, 0, size_t(W) * H * 3 * sizeof(float)));
+        CK(cudaMemset(cv.counters, 0, 4 * sizeof(int)));
+        // sample split of delayed.cpp:205-210, including its extra-sample rule
+        const long long totalSamples = (long long)opt.spp * W * H;
+        samplesPerChain = totalSamples / N;
+        extraChains = samplesPerChain % N;
+        bootSeed = opt.seed ^ 0x5EEDull;
+        return DRMLT_OK;
+    }
+
+    int prepass(float *bOut) {
+        const int minDepth = std::max(opt.min_depth, 3);
+        const int ns = opt.num_init_samples;
+        if (ns <= 0) return fail(DRMLT_E_ARG, "num_init_samples must be positive");
+        const int cap = ns * 8;
+        BootRecord *dRec;
+        int *dCount;
+        int rc;
+        if ((rc = dalloc(&dRec, size_t(cap)))) return rc;
+        if ((rc = dalloc(&dCount, 2))) return rc;
+        CK(cudaMemsetAsync(dCount, 0, 2 * sizeof(int), stream));
+        k_bootstrap<<<(ns + 127) / 128, 128, 0, stream>>>(sv, bootSeed, ns, minDepth, opt.max_depth, dRec, dCount, cap,
+                                                          dCount + 1);
+        CK(cudaGetLastError());
+        int hc[2];
+        CK(cudaMemcpyAsync(hc, dCount, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (hc[1]) {
+            cudaFree(dRec);
+            cudaFree(dCount);
+            return fail(DRMLT_E_OVERFLOW, "bootstrap contribution buffer overflow");
+        }
+        std::vector<BootRecord> recs(hc[0]);
+        if (hc[0]) CK(cudaMemcpy(recs.data(), dRec, size_t(hc[0]) * sizeof(BootRecord), cudaMemcpyDeviceToHost));
+        cudaFree(dRec);
+        cudaFree(dCount);
+        if (recs.empty()) return fail(DRMLT_E_STATE, "bootstrap found no contributing path");
+        // deterministic order: by sample, then technique
+        std::sort(recs.begin(), recs.end(), [](const BootRecord &a, const BootRecord &c) {
+            if (a.sample != c.sample) return a.sample < c.sample;
+            if (a.c != c.c) return a.c < c.c;
+            return a.l < c.l;
+        });
+        // totalScore, lengthContrib (delayed.cpp:97-117)
+        double totalScore = 0.0;
+        std::vector<float> lengthContrib;
+        for (const BootRecord &r : recs) {
+            totalScore += r.ls;
+            const int len = r.c + r.l - 1;
+            if (len >= int(lengthContrib.size())) lengthContrib.resize(len + 1, 0.0f);
+            lengthContrib[len] += r.ls;
+        }
+        std::vector<float> lcdf;
+        float lfi;
+        piecewise_constant(lengthContrib, lcdf, lfi);
+        float *dLcdf, *dLfunc;
+        if ((rc = up(&dLcdf, lcdf.data(), lcdf.size()))) return rc;
+        if ((rc = up(&dLfunc, lengthContrib.data(), lengthContrib.size()))) return rc;
+        cv.lengthCdf = dLcdf;
+        cv.lengthFunc = dLfunc;
+        cv.lengthCount = int(lengthContrib.size());
+        cv.lengthFuncInt = lfi;
+        // equal-spaced seeding (delayed.cpp:125-167)
+        std::vector<double> cdf(recs.size() + 1, 0.0);
+        for (size_t i = 0; i < recs.size(); i++) cdf[i + 1] = cdf[i] + recs[i].ls;
+        const double interval = cdf.back() / double(N);
+        // offset in [0, interval) from a fixed hash of the record count
+        unsigned long long h = 0x9E3779B97F4A7C15ull * (recs.size() + 1) ^ opt.seed;
+        h ^= h >> 33;
+        h *= 0xff51afd7ed558ccdull;
+        h ^= h >> 33;
+        double pos = double(h >> 11) * (1.0 / 9007199254740992.0) * interval;
+        std::vector<int> sampleOf(N), techC(N), techL(N);
+        size_t cdfPos = 0;
+        for (int i = 0; i < N; i++) {
+            while (pos > cdf[cdfPos]) cdfPos = std::min(cdfPos + 1, recs.size() - 1 + 1);
+            const size_t ri = cdfPos == 0 ? 0 : cdfPos - 1;
+            sampleOf[i] = recs[ri].sample;
+            techC[i] = recs[ri].c;
+            techL[i] = recs[ri].l;
+            pos += interval;
+        }
+        int *dS, *dC, *dL;
+        if ((rc = dalloc(&dS, N)) || (rc = dalloc(&dC, N)) || (rc = dalloc(&dL, N))) return rc;
+        CK(cudaMemcpy(dS, sampleOf.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dC, techC.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dL, techL.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+        b = float(totalScore) * (1.0f / float(ns));
+        k_seed<<<(N + 127) / 128, 128, 0, stream>>>(params(), bootSeed, dS, dC, dL, minDepth, opt.max_depth);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(stream));
+        cudaFree(dS);
+        cudaFree(dC);
+        cudaFree(dL);
+        prepassDone = true;
+        iterDone = 0;
+        if (bOut) *bOut = b;
+        return DRMLT_OK;
+    }
+
+    int direct() {
+        if (opt.min_depth > 2 || opt.max_depth < 1 || opt.direct_spp <= 0) {
+            directDone = true;
+            return DRMLT_OK;
+        }
+        const long long n = (long long)W * H * opt.direct_spp;
+        k_direct<<<unsigned((n + 127) / 128), 128, 0, stream>>>(sv, opt.seed, opt.direct_spp,
+                                                                std::min(opt.min_depth, 2), std::min(opt.max_depth, 2),
+                                                                cv.direct);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(stream));
+        directDone = true;
+        return DRMLT_OK;
+    }
+
+    // One Markov-chain iteration: the per-stage launches.
+    void launch_iteration(int iter) {
+        const RunParams p = params();
+        const int nb = (N + 127) / 128;
+        const int nbWarp = (N * 32 + 127) / 128;
+        const int nbG = (N + 63) / 64;
+        k_reset_counters<<<1, 32, 0, stream>>>(cv.counters);
+        k_stage1<<<nb, 128, 0, stream>>>(p, iter);
+        k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
+        k_gauss<<<nbG, 64, 0, stream>>>(p, 0);
+        k_stage2<<<nb, 128, 0, stream>>>(p, iter);
+        k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
+        k_gauss<<<nbG, 64, 0, stream>>>(p, 2);
+        k_finish<<<nb, 128, 0, stream>>>(p, iter);
+    }
+
+    // The same iterations with CUDA events around each stage (on the launching
+    // stream); accumulates per-stage milliseconds into ms[kNumStages].
+    static constexpr int kNumStages = 7;
+    int profile(long long iterations, float *ms, long long *done) {
+        if (!prepassDone) return fail(DRMLT_E_STATE, "profile before prepass");
+        const long long end = std::min(iterDone + iterations, total_iterations());
+        cudaEvent_t ev[kNumStages + 1];
+        for (int k = 0; k <= kNumStages; k++) CK(cudaEventCreate(&ev[k]));
+        for (int k = 0; k < kNumStages; k++) ms[k] = 0.0f;
+        long long mutations = 0;
+        const int nb = (N + 127) / 128, nbWarp = (N * 32 + 127) / 128, nbG = (N + 63) / 64;
+        for (long long it = iterDone; it < end; it++) {
+            const RunParams p = params();
+            const int iter = int(it);
+            cudaEventRecord(ev[0], stream);
+            k_reset_counters<<<1, 32, 0, stream>>>(cv.counters);
+            k_stage1<<<nb, 128, 0, stream>>>(p, iter);
+            cudaEventRecord(ev[1], stream);
+            k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
+            cudaEventRecord(ev[2], stream);
+            k_gauss<<<nbG, 64, 0, stream>>>(p, 0);
+            cudaEventRecord(ev[3], stream);
+            k_stage2<<<nb, 128, 0, stream>>>(p, iter);
+            cudaEventRecord(ev[4], stream);
+            k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
+            cudaEventRecord(ev[5], stream);
+            k_gauss<<<nbG, 64, 0, stream>>>(p, 2);
+            cudaEventRecord(ev[6], stream);
+            k_finish<<<nb, 128, 0, stream>>>(p, iter);
+            cudaEventRecord(ev[7], stream);
+            CK(cudaEventSynchronize(ev[7]));
+            for (int k = 0; k < kNumStages; k++) {
+                float t;
+                cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+                ms[k] += t;
+            }
+            mutations += (it < samplesPerChain) ? N : extraChains;
+        }
+        CK(cudaGetLastError());
+        for (int k = 0; k <= kNumStages; k++) cudaEventDestroy(ev[k]);
+        iterDone = end;
+        if (done) *done = mutations;
+        return DRMLT_OK;
+    }
+
+    long long total_iterations() const { return samplesPerChain + (extraChains > 0 ? 1 : 0); }
+
+    int run(long long iterations, long long *done) {
+        if (!prepassDone) return fail(DRMLT_E_STATE, "run before prepass");
+        const long long end = std::min(iterDone + iterations, total_iterations());
+        long long mutations = 0;
+        CK(cudaEventRecord(ev0, stream));
+        for (long long it = iterDone; it < end; it++) {
+            launch_iteration(int(it));
+            mutations += (it < samplesPerChain) ? N : extraChains;
+        }
+        CK(cudaEventRecord(ev1, stream));
+        CK(cudaGetLastError());
+        CK(cudaEventSynchronize(ev1));
+        CK(cudaEventElapsedTime(&lastRunMs, ev0, ev1));
+        iterDone = end;
+        if (done) *done = mutations;
+        return DRMLT_OK;
+    }
+
+    int film(float *rgb) {
+        const size_t n = size_t(W) * H * 3;
+        std::vector<float> ind(n), dir(n);
+        CK(cudaMemcpy(ind.data(), cv.film, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(dir.data(), cv.direct, n * sizeof(float), cudaMemcpyDeviceToHost));
+        // MergeBuffer (src/image.h:76-93, delayed.cpp:681-685)
+        const float dw = opt.direct_spp > 0 ? 1.0f / float(opt.direct_spp) : 0.0f;
+        const float iw = opt.spp > 0 ? 1.0f / float(opt.spp) : 0.0f;
+        for (size_t i = 0; i < n; i++) {
+            float v = 0.0f;
+            v += dw * dir[i];
+            v += iw * ind[i];
+            rgb[i] = v;
+        }
+        return DRMLT_OK;
+    }
+};
+
+}  // namespace
+
+// ============================================================================ C ABI
+extern "C" {
+
+void drmlt_default_options(drmlt_options *o) {
+    std::memset(o, 0, sizeof(*o));
+    o->integrator = DRMLT_INTEGRATOR_DRMLT;
+    o->dr_type = DRMLT_DR_GREEN;
+    o->aniso_perturb_prob = 0.5f;
+    o->aniso_perturb_stddev = 0.0025f;
+    o->acceptance_map = 0;
+    o->perturb_stddev = 0.01f;
+    o->large_step_prob = 0.3f;
+    o->roughness_threshold = 0.03f;
+    o->discrete_stddev = 0.01f;
+    o->uniform_mixing_prob = 0.2f;
+    o->num_chains = 1024;
+    o->num_init_samples = 100000;
+    o->spp = 16;
+    o->direct_spp = 16;
+    o->min_depth = -1;
+    o->max_depth = -1;
+    o->seed_offset = 0;
+    o->use_light_coordinate_sampling = 1;
+    o->max_derivative_depth = 9;
+    o->seed = 0x1234ABCDull;
+    o->device = 0;
+    o->use_graph = 0;
+}
+
+const char *drmlt_last_error(void) { return g_error.c_str(); }
+
+int drmlt_create(const drmlt_scene_desc *scene, const drmlt_options *opt, void **handle) {
+    if (!scene || !opt || !handle) return fail(DRMLT_E_ARG, "null argument");
+    Renderer *r = new Renderer();
+    const int rc = r->create(scene, opt);
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    *handle = r;
+    return DRMLT_OK;
+}
+
+int drmlt_destroy(void *handle) {
+    delete static_cast<Renderer *>(handle);
+    return DRMLT_OK;
+}
+
+int drmlt_prepass(void *handle, float *b_out) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    return static_cast<Renderer *>(handle)->prepass(b_out);
+}
+
+int drmlt_direct(void *handle) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    return static_cast<Renderer *>(handle)->direct();
+}
+
+int drmlt_run(void *handle, int64_t iterations, int64_t *done) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    long long d = 0;
+    const int rc = static_cast<Renderer *>(handle)->run(iterations, &d);
+    if (done) *done = d;
+    return rc;
+}
+
+int drmlt_render(void *handle) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    Renderer *r = static_cast<Renderer *>(handle);
+    int rc = r->direct();
+    if (rc) return rc;
+    rc = r->prepass(nullptr);
+    if (rc) return rc;
+    return r->run(r->total_iterations(), nullptr);
+}
+
+int drmlt_get_film(void *handle, float *rgb) {
+    if (!handle || !rgb) return fail(DRMLT_E_ARG, "null argument");
+    return static_cast<Renderer *>(handle)->film(rgb);
+}
+
+int drmlt_get_stats(void *handle, drmlt_stats *st) {
+    if (!handle || !st) return fail(DRMLT_E_ARG, "null argument");
+    Renderer *r = static_cast<Renderer *>(handle);
+    unsigned long long h[kNumStats];
+    CK(cudaMemcpy(h, r->cv.stats, sizeof(h), cudaMemcpyDeviceToHost));
+    st->large_step = h[kStatLarge];
+    st->large_step_accepted = h[kStatLargeAcc];
+    st->stage1 = h[kStatStage1];
+    st->stage1_accepted = h[kStatStage1Acc];
+    st->stage2_iso = h[kStatIso];
+    st->stage2_iso_accepted = h[kStatIsoAcc];
+    st->stage2_h2mc = h[kStatH2mc];
+    st->stage2_h2mc_accepted = h[kStatH2mcAcc];
+    st->mutations = h[kStatMutations];
+    return DRMLT_OK;
+}
+
+int drmlt_profile(void *handle, int64_t iterations, float *stage_ms, int64_t *done) {
+    if (!handle || !stage_ms) return fail(DRMLT_E_ARG, "null argument");
+    long long d = 0;
+    const int rc = static_cast<Renderer *>(handle)->profile(iterations, stage_ms, &d);
+    if (done) *done = d;
+    return rc;
+}
+
+int drmlt_total_iterations(void *handle, int64_t *iterations) {
+    if (!handle || !iterations) return fail(DRMLT_E_ARG, "null argument");
+    *iterations = static_cast<Renderer *>(handle)->total_iterations();
+    return DRMLT_OK;
+}
+
+int drmlt_last_run_ms(void *handle, float *ms) {
+    if (!handle || !ms) return fail(DRMLT_E_ARG, "null argument");
+    *ms = static_cast<Renderer *>(handle)->lastRunMs;
+    return DRMLT_OK;
+}
+
+}  // extern "C"
+
+#include "parity.cuh"

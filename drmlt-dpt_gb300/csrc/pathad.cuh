@@ -1,0 +1,553 @@
+// Derivatives of f(u) = log Luminance(contribution) with respect to the
+// primary sample vector u of a fixed technique path, on fixed triangles.
+//
+// f is the function the reference's chad code generator differentiates
+// (RegisterPathFuncBidir, src/path.cpp:2987-3175, static mode: time excluded),
+// including that builder's own rules: no occlusion tests, re-intersection with
+// the stored triangle's plane, BSDF forms without the primal epsilon checks
+// (src/lambertian.cpp:92-150, src/phong.cpp:168-392), the emitter's
+// accMISWThis taken only for point lights (src/path.cpp:2600-2608), ADEpsilon
+// 1e-6 clamps (src/utils.h:442-449), and branches selected by value with
+// derivatives flowing through the taken branch (src/chad.cpp:70-110).
+//
+// The scalar type is templated: float for values, HyperDual for exact second
+// derivatives. A HyperDual carries (f, df/du_i, df/du_j, d2f/du_i du_j): one
+// evaluation yields one Hessian entry and two gradient entries, so a chain's
+// D(D+1)/2 Hessian entries are independent threads that follow the same
+// control flow (branches depend on values only).
+#pragma once
+#include "path.cuh"
+
+namespace drmlt {
+
+struct HyperDual {
+    float v, a, b, ab;
+    HD HyperDual() {}
+    HD explicit HyperDual(float x) : v(x), a(0.0f), b(0.0f), ab(0.0f) {}
+    HD HyperDual(float x, float da, float db, float dab) : v(x), a(da), b(db), ab(dab) {}
+};
+HD HyperDual operator+(const HyperDual &x, const HyperDual &y) { return HyperDual(x.v + y.v, x.a + y.a, x.b + y.b, x.ab + y.ab); }
+HD HyperDual operator-(const HyperDual &x, const HyperDual &y) { return HyperDual(x.v - y.v, x.a - y.a, x.b - y.b, x.ab - y.ab); }
+HD HyperDual operator-(const HyperDual &x) { return HyperDual(-x.v, -x.a, -x.b, -x.ab); }
+HD HyperDual operator*(const HyperDual &x, const HyperDual &y) {
+    return HyperDual(x.v * y.v, x.a * y.v + x.v * y.a, x.b * y.v + x.v * y.b,
+                     x.ab * y.v + x.a * y.b + x.b * y.a + x.v * y.ab);
+}
+HD HyperDual operator*(const HyperDual &x, float s) { return HyperDual(x.v * s, x.a * s, x.b * s, x.ab * s); }
+HD HyperDual operator*(float s, const HyperDual &x) { return x * s; }
+HD HyperDual operator+(const HyperDual &x, float s) { return HyperDual(x.v + s, x.a, x.b, x.ab); }
+HD HyperDual operator+(float s, const HyperDual &x) { return x + s; }
+HD HyperDual operator-(const HyperDual &x, float s) { return HyperDual(x.v - s, x.a, x.b, x.ab); }
+HD HyperDual operator-(float s, const HyperDual &x) { return HyperDual(s - x.v, -x.a, -x.b, -x.ab); }
+// Generic unary rule: f(x) with first and second derivative d1, d2 at x.v.
+HD HyperDual chain(const HyperDual &x, float f, float d1, float d2) {
+    return HyperDual(f, d1 * x.a, d1 * x.b, d1 * x.ab + d2 * x.a * x.b);
+}
+HD HyperDual inv(const HyperDual &x) {
+    const float r = 1.0f / x.v;
+    return chain(x, r, -r * r, 2.0f * r * r * r);
+}
+HD HyperDual operator/(const HyperDual &x, const HyperDual &y) { return x * inv(y); }
+HD HyperDual operator/(const HyperDual &x, float s) { return x * (1.0f / s); }
+HD HyperDual operator/(float s, const HyperDual &y) { return s * inv(y); }
+HD HyperDual sqrt(const HyperDual &x) {
+    const float r = sqrtf(x.v);
+    return chain(x, r, 0.5f / r, -0.25f / (r * x.v));
+}
+HD HyperDual sin(const HyperDual &x) {
+    float s, c;
+    sincosf(x.v, &s, &c);
+    return chain(x, s, c, -s);
+}
+HD HyperDual cos(const HyperDual &x) {
+    float s, c;
+    sincosf(x.v, &s, &c);
+    return chain(x, c, -s, -c);
+}
+HD HyperDual log(const HyperDual &x) {
+    const float r = 1.0f / x.v;
+    return chain(x, logf(x.v), r, -r * r);
+}
+HD HyperDual pow(const HyperDual &x, float e) {
+    const float p = powf(x.v, e);
+    const float d1 = e * powf(x.v, e - 1.0f);
+    const float d2 = e * (e - 1.0f) * powf(x.v, e - 2.0f);
+    return chain(x, p, d1, d2);
+}
+HD HyperDual fabs(const HyperDual &x) { return x.v >= 0.0f ? x : -x; }
+HD HyperDual fmax(const HyperDual &x, float c) { return x.v >= c ? x : HyperDual(c); }
+HD float sqrt(float x) { return sqrtf(x); }
+HD float sin(float x) { return sinf(x); }
+HD float cos(float x) { return cosf(x); }
+HD float log(float x) { return logf(x); }
+HD float fabs(float x) { return fabsf(x); }
+HD float fmax(float x, float c) { return fmaxf(x, c); }
+HD float val(const HyperDual &x) { return x.v; }
+HD float val(float x) { return x; }
+HD float pow(float x, float e) { return powf(x, e); }
+
+template <class T> using TV3 = Vec3<T>;
+
+template <class T> HD T tlen(const TV3<T> &v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+template <class T> HD TV3<T> tnorm(const TV3<T> &v) { T il = 1.0f / tlen(v); return v * il; }
+template <class T> HD TV3<T> tv(const V3 &v) { return TV3<T>(T(v.x), T(v.y), T(v.z)); }
+template <class T> HD TV3<T> treflect(const TV3<T> &wi, const TV3<T> &n) { return (2.0f * dot(wi, n)) * n - wi; }
+template <class T> HD T tmis(const T &x) { return x * x; }
+template <class T> HD T tlum(const TV3<T> &v) { return v.x * 0.212671f + v.y * 0.715160f + v.z * 0.072169f; }
+
+template <class T>
+HD void tframe(const TV3<T> &n, TV3<T> &b1, TV3<T> &b2) {
+    if (val(n.z) < float(-1.0 + 1e-6)) {
+        b1 = TV3<T>(T(0.0f), T(-1.0f), T(0.0f));
+        b2 = TV3<T>(T(-1.0f), T(0.0f), T(0.0f));
+        return;
+    }
+    const T a = 1.0f / (1.0f + n.z);
+    const T b = -n.x * n.y * a;
+    b1 = TV3<T>(1.0f - n.x * n.x * a, b, -n.x);
+    b2 = TV3<T>(b, 1.0f - n.y * n.y * a, -n.y);
+}
+
+template <class T>
+HD TV3<T> tcos_hemisphere(const T &u0, const T &u1) {
+    const T phi = kTwoPi * u0;
+    const T tmp = sqrt(fmax(1.0f - u1, 1e-6f));
+    return TV3<T>(cos(phi) * tmp, sin(phi) * tmp, sqrt(fmax(u1, 1e-6f)));
+}
+
+template <class T>
+struct TIsect {
+    TV3<T> position, shadingNormal, geomNormal;
+};
+
+template <class T>
+struct TState {
+    TIsect<T> isect;
+    TV3<T> wi;
+    T prev, cur;  // accMISWPrev, accMISWThis
+    TV3<T> throughput;
+};
+
+template <class T>
+struct TBsdf {
+    TV3<T> contrib;
+    T cosWo, pdf, revPdf;
+};
+
+// EvaluateLambertian / EvaluatePhong (AD forms).
+template <class T>
+DEV void ad_evaluate(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo, TBsdf<T> &o) {
+    T cosWi = dot(normal, wi);
+    TV3<T> n = normal;
+    if (!(val(cosWi) > 0.0f)) {
+        n = -normal;
+        cosWi = -cosWi;
+    }
+    o.cosWo = dot(n, wo);
+    const V3 kd = kd_of(b);
+    if (b.type == kBsdfLambertian) {
+        const T fwd = o.cosWo * kInvPi;
+        o.contrib = fwd * tv<T>(kd);
+        o.pdf = fwd;
+        o.revPdf = cosWi * kInvPi;
+        return;
+    }
+    TV3<T> spec(T(0.0f), T(0.0f), T(0.0f));
+    T specPdf(0.0f);
+    if (b.ksWeight > 0.0f) {
+        const T alpha = dot(treflect(wi, n), wo);
+        const float wv = powf(val(alpha), b.exponent) * kInvTwoPi;
+        if (wv > 1e-10f) {
+            const T weight = pow(alpha, b.exponent) * kInvTwoPi;
+            spec = tv<T>(ks_of(b)) * ((b.exponent + 2.0f) * weight);
+            specPdf = b.ksWeight * (b.exponent + 1.0f) * weight;
+        }
+    }
+    o.contrib = spec;
+    o.pdf = specPdf;
+    o.revPdf = specPdf;
+    if (b.ksWeight < 1.0f) {
+        const float tmp = (1.0f - b.ksWeight) * kInvPi;
+        o.contrib = o.contrib + tv<T>(kd * kInvPi);
+        o.pdf = o.pdf + tmp * o.cosWo;
+        o.revPdf = o.revPdf + tmp * cosWi;
+    }
+    o.contrib = o.contrib * o.cosWo;
+}
+
+// SampleLambertian / SamplePhong (AD forms, fixDiscrete = false).
+template <class T>
+DEV void ad_sample(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const T &r0, const T &r1, float uDiscrete,
+                   TV3<T> &wo, TBsdf<T> &o) {
+    T cosWi = dot(wi, normal);
+    TV3<T> n = normal;
+    if (!(val(cosWi) > 0.0f)) {
+        n = -normal;
+        cosWi = -cosWi;
+    }
+    if (b.type == kBsdfLambertian) {
+        TV3<T> b0, b1;
+        tframe(n, b0, b1);
+        const TV3<T> l = tcos_hemisphere(r0, r1);
+        wo = l.x * b0 + l.y * b1 + l.z * n;
+        o.cosWo = l.z;
+        o.pdf = l.z * kInvPi;
+        o.contrib = tv<T>(kd_of(b));
+        o.revPdf = cosWi * kInvPi;
+        return;
+    }
+    const TV3<T> R = treflect(wi, n);
+    if (uDiscrete > b.ksWeight) {
+        const TV3<T> l = tcos_hemisphere(r0, r1);
+        TV3<T> b0, b1;
+        tframe(n, b0, b1);
+        wo = l.x * b0 + l.y * b1 + l.z * n;
+    } else {
+        const float power = 1.0f / (b.exponent + 1.0f);
+        const T cosAlpha = pow(r1, power);
+        const T sinAlpha = sqrt(fmax(1.0f - cosAlpha * cosAlpha, 1e-6f));
+        const T phi = kTwoPi * r0;
+        const TV3<T> l(sinAlpha * cos(phi), sinAlpha * sin(phi), cosAlpha);
+        TV3<T> b0, b1;
+        tframe(R, b0, b1);
+        wo = l.x * b0 + l.y * b1 + l.z * R;
+    }
+    o.cosWo = dot(n, wo);
+    TV3<T> spec(T(0.0f), T(0.0f), T(0.0f));
+    T specPdf(0.0f);
+    if (b.ksWeight > 0.0f) {
+        const T alpha = dot(R, wo);
+        const float wv = powf(val(alpha), b.exponent) * kInvTwoPi;
+        if (wv > 1e-10f) {
+            const T weight = pow(alpha, b.exponent) * kInvTwoPi;
+            spec = tv<T>(ks_of(b)) * ((b.exponent + 2.0f) * weight);
+            specPdf = b.ksWeight * (b.exponent + 1.0f) * weight;
+        }
+    }
+    o.contrib = spec;
+    o.pdf = specPdf;
+    o.revPdf = specPdf;
+    if (b.ksWeight < 1.0f) {
+        const float tmp = (1.0f - b.ksWeight) * kInvPi;
+        o.contrib = o.contrib + tv<T>(kd_of(b) * kInvPi);
+        o.pdf = o.pdf + tmp * o.cosWo;
+        o.revPdf = o.revPdf + tmp * cosWi;
+    }
+    o.contrib = o.contrib * o.cosWo;
+    o.contrib = o.contrib * (1.0f / o.pdf);
+}
+
+template <class T>
+DEV T ad_snc(const TV3<T> &wi, const TIsect<T> &is, const TV3<T> &wo) {
+    const T cosWi = dot(is.shadingNormal, wi);
+    const T cosWo = dot(is.shadingNormal, wo);
+    const T wiDotGeoN = dot(is.geomNormal, wi);
+    const T woDotGeoN = dot(is.geomNormal, wo);
+    return fabs((woDotGeoN * cosWi) / (wiDotGeoN * cosWo));
+}
+
+// IntersectTriangleMesh (AD, static) on a known triangle.
+template <class T>
+DEV void ad_intersect(const SceneView &s, int tri, const TV3<T> &org, const TV3<T> &dir, TIsect<T> &is) {
+    const float *P = s.triP + 9 * tri;
+    const V3 p0 = ld3(P), e1 = ld3(P + 3), e2 = ld3(P + 6);
+    const float *N = s.triN + 9 * tri;
+    const V3 gn = normalize(cross(e1, e2));
+    is.geomNormal = tv<T>(gn);
+    const TV3<T> E1 = tv<T>(e1), E2 = tv<T>(e2);
+    const TV3<T> s1 = cross(dir, E2);
+    const T divisor = dot(s1, E1);
+    const T invDivisor = 1.0f / divisor;
+    const TV3<T> sv = org - tv<T>(p0);
+    const T u = dot(sv, s1) * invDivisor;
+    const TV3<T> s2 = cross(sv, E1);
+    const T v = dot(dir, s2) * invDivisor;
+    const T t = dot(E2, s2) * invDivisor;
+    const T w = 1.0f - u - v;
+    is.position = org + t * dir;
+    is.shadingNormal = tnorm(TV3<T>(w * tv<T>(ld3(N)) + u * tv<T>(ld3(N + 3)) + v * tv<T>(ld3(N + 6))));
+}
+
+// SampleShape (AD) on a triangle: a = sqrt((1 + 1e-6) - r0).
+template <class T>
+DEV void ad_sample_triangle(const SceneView &s, int tri, const T &r0, const T &r1, TV3<T> &pos, TV3<T> &normal) {
+    const float *P = s.triP + 9 * tri;
+    const float *N = s.triN + 9 * tri;
+    const T a = sqrt((1.0f + 1e-6f) - r0);
+    const T b1 = 1.0f - a;
+    const T b2 = a * r1;
+    pos = tv<T>(ld3(P)) + (tv<T>(ld3(P + 3)) * b1) + (tv<T>(ld3(P + 6)) * b2);
+    normal = tnorm(TV3<T>(tv<T>(ld3(N)) * (1.0f - b1 - b2) + tv<T>(ld3(N + 3)) * b1 + tv<T>(ld3(N + 6)) * b2));
+}
+
+template <class T>
+DEV TV3<T> ad_xform_point(const float *m, const TV3<T> &p) {
+    const T x = m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3];
+    const T y = m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7];
+    const T z = m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11];
+    const T w = m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15];
+    const T invW = 1.0f / w;
+    return TV3<T>(x * invW, y * invW, z * invW);
+}
+template <class T>
+DEV TV3<T> ad_xform_vector(const float *m, const TV3<T> &v) {
+    return TV3<T>(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+                  m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+template <class T>
+DEV void ad_sample_primary(const Camera &c, const T &sx, const T &sy, TV3<T> &org, TV3<T> &dir) {
+    const TV3<T> o = ad_xform_point(c.sampleToCam, TV3<T>(sx, sy, T(0.0f)));
+    const TV3<T> d = tnorm(o);
+    org = ad_xform_point(c.camToWorld, TV3<T>(T(0.0f), T(0.0f), T(0.0f)));
+    dir = ad_xform_vector(c.camToWorld, d);
+}
+
+// BSDFSampling<adjoint, false> (AD, src/path.cpp:2671-2762).
+template <class T, bool adjoint>
+DEV void ad_bsdf_sampling(const SceneView &s, int tri, const T &r0, const T &r1, float disc, bool useAbs,
+                          int lcsTri, TState<T> &ps, TV3<T> &dir) {
+    const Bsdf &b = bsdf_of_tri(s, tri);
+    TBsdf<T> o;
+    T jacobian(1.0f);
+    if (lcsTri >= 0) {
+        TV3<T> nextPos, nextNormal;
+        ad_sample_triangle(s, lcsTri, r0, r1, nextPos, nextNormal);
+        const float shapePdf = s.lights[area_light_of_tri(s, lcsTri)].invTotalArea;
+        dir = nextPos - ps.isect.position;
+        const T distSq = dot(dir, dir);
+        const T invDistSq = 1.0f / distSq;
+        const T invDist = sqrt(invDistSq);
+        dir = dir * invDist;
+        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o);
+        jacobian = fabs(dot(nextNormal, dir) * invDistSq) / shapePdf;
+    } else if (!useAbs) {
+        ad_sample(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dir, o);
+    } else {
+        const T scaledTheta = kTwoPi * r0;
+        const T scaledPhi = kPi * r1;
+        const T sinPhi = sin(scaledPhi);
+        const T cosPhi = cos(scaledPhi);
+        jacobian = fabs(sinPhi);
+        dir = TV3<T>(sinPhi * cos(scaledTheta), sinPhi * sin(scaledTheta), cosPhi);
+        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o);
+    }
+    TV3<T> contrib = o.contrib;
+    if (adjoint) contrib = contrib * ad_snc(ps.wi, ps.isect, dir);
+    contrib = contrib * jacobian;
+    ps.cur = tmis(o.cosWo / o.pdf) * (ps.cur * tmis(o.revPdf) + ps.prev);
+    ps.prev = tmis(1.0f / o.pdf);
+    ps.throughput = cmul(ps.throughput, contrib);
+}
+
+// Evaluates f = log Luminance(contribution) of technique path `r` at primary
+// vector u (length 2(c+l-1), GetPathPos order) the way the generated
+// evaluate_path_bidir_<c>_<l>_static does.
+template <class T>
+DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
+    const int c = r.c, l = r.l;
+    const int nl = n_lgt(l), nc = c - 1;
+    const float pixelCount = float(s.cam.width * s.cam.height);
+    int k = 0;
+    TState<T> lp;
+    TV3<T> contrib(T(0.0f), T(0.0f), T(0.0f));
+    int lgtVertTri = -1;
+    if (l > 1) {
+        const int li = r.lgtLight;
+        const Light &L = s.lights[li];
+        const float pick = pick_light_prob(s, li);
+        const T p0 = u[k++], p1 = u[k++], d0 = u[k++], d1 = u[k++];
+        TV3<T> org, dir;
+        T cosLight, emissionPdf, directPdf;
+        if (L.type == kLightArea) {  // EmitAreaLight (AD)
+            TV3<T> nrm;
+            ad_sample_triangle(s, light_tri(s, L, r.lgtPrim), p0, p1, org, nrm);
+            const TV3<T> d = tcos_hemisphere(d0, d1);
+            TV3<T> b0, b1;
+            tframe(nrm, b0, b1);
+            dir = d.x * b0 + d.y * b1 + d.z * nrm;
+            lp.throughput = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2]) * (kPi / L.invTotalArea));
+            cosLight = d.z;
+            emissionPdf = d.z * kInvPi * L.invTotalArea;
+            directPdf = T(L.invTotalArea);
+        } else {  // EmitPointLight (AD)
+            org = tv<T>(V3(L.pos[0], L.pos[1], L.pos[2]));
+            const T scaledTheta = kTwoPi * d0;
+            const T scaledPhi = kPi * d1;
+            const T sinPhi = sin(scaledPhi);
+            dir = TV3<T>(sinPhi * cos(scaledTheta), sinPhi * sin(scaledTheta), cos(scaledPhi));
+            lp.throughput = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2]));
+            emissionPdf = T(1.0f / (4.0f * kPi));
+            cosLight = T(1.0f);
+            directPdf = T(1.0f);
+        }
+        emissionPdf = emissionPdf * pick;
+        directPdf = directPdf * pick;
+        lp.throughput = lp.throughput * (1.0f / pick);
+        lp.prev = tmis(directPdf / emissionPdf);
+        lp.cur = L.type == kLightPoint ? tmis(cosLight / emissionPdf) : T(0.0f);
+        for (int d = 0; d < nl; d++) {
+            const int tri = r.tri[d];
+            ad_intersect(s, tri, org, dir, lp.isect);
+            lp.wi = -dir;
+            if (d == 0) {  // ConvertMISLightEmit
+                const T conv = L.type == kLightEnv ? T(1.0f) : tmis(dot(org - lp.isect.position, org - lp.isect.position));
+                const T invCos = 1.0f / tmis(fabs(dot(dir, lp.isect.shadingNormal)));
+                lp.prev = lp.prev * (invCos * conv);
+                lp.cur = lp.cur * invCos;
+            } else {
+                lp.prev = lp.prev * tmis(dot(org - lp.isect.position, org - lp.isect.position));
+                const T invCos = 1.0f / tmis(fabs(dot(dir, lp.isect.shadingNormal)));
+                lp.prev = lp.prev * invCos;
+                lp.cur = lp.cur * invCos;
+            }
+            if (d == nl - 1) {
+                if (c == 1) {  // ConnectToCamera (AD)
+                    TV3<T> camOrg, camDir;
+                    ad_sample_primary(s.cam, T(0.5f), T(0.5f), camOrg, camDir);
+                    TV3<T> dirToCamera = camOrg - lp.isect.position;
+                    const T distSq = dot(dirToCamera, dirToCamera);
+                    const T dist = sqrt(distSq);
+                    dirToCamera = dirToCamera * (1.0f / dist);
+                    TBsdf<T> o;
+                    ad_evaluate(bsdf_of_tri(s, tri), lp.wi, lp.isect.shadingNormal, dirToCamera, o);
+                    const TV3<T> bsdfContrib = o.contrib * ad_snc(lp.wi, lp.isect, dirToCamera);
+                    const T invCosAtCamera = -(1.0f / dot(camDir, dirToCamera));
+                    const T ip = s.cam.dist * invCosAtCamera;
+                    const T imageToSolidAngleFactor = (ip * ip) * invCosAtCamera;
+                    const T imageToSurfaceFactor = imageToSolidAngleFactor * fabs(o.cosWo) / distSq;
+                    const T wLight = tmis(imageToSurfaceFactor / pixelCount) * (lp.prev + lp.cur * tmis(o.revPdf));
+                    const T misWeight = 1.0f / (wLight + 1.0f);
+                    const T surfaceToImageFactor = o.cosWo / imageToSurfaceFactor;
+                    const T denom = pixelCount * surfaceToImageFactor;
+                    const TV3<T> cc = (misWeight * bsdfContrib) * (1.0f / denom);
+                    contrib = cmul(cc, lp.throughput);
+                }
+                lgtVertTri = tri;
+                break;
+            }
+            const T r0 = u[k++], r1 = u[k++];
+            ad_bsdf_sampling<T, true>(s, tri, r0, r1, r.disc[d], (r.useAbs >> d) & 1u, -1, lp, dir);
+            lp.throughput = lp.throughput * r.rr[d];
+            org = lp.isect.position;
+        }
+    }
+    if (c > 1) {
+        const T sx = u[k++], sy = u[k++];
+        TV3<T> co, cd, org, dir;
+        ad_sample_primary(s.cam, T(0.5f), T(0.5f), co, cd);
+        ad_sample_primary(s.cam, sx, sy, org, dir);
+        TState<T> cp;
+        {
+            const T cosAtCamera = dot(cd, dir);
+            const T ip = s.cam.dist / cosAtCamera;
+            const T cameraPdf = (ip * ip) / cosAtCamera;
+            cp.throughput = TV3<T>(T(1.0f), T(1.0f), T(1.0f));
+            cp.prev = tmis(pixelCount / cameraPdf);
+            cp.cur = T(0.0f);
+        }
+        for (int d = 0; d < nc; d++) {
+            const int vi = nl + d;
+            const int tri = r.tri[vi];
+            ad_intersect(s, tri, org, dir, cp.isect);
+            cp.wi = -dir;
+            if (d == nc - 1 && l == 0) {
+                // ConvertMISLightHit + HandleHitLight (AD)
+                const int li = area_light_of_tri(s, tri);
+                const Light &L = s.lights[li];
+                const T dsq = tmis(dot(org - cp.isect.position, org - cp.isect.position));
+                const T invCos = 1.0f / tmis(fabs(dot(dir, cp.isect.shadingNormal)));
+                cp.prev = cp.prev * (invCos * dsq);
+                cp.cur = cp.cur * invCos;
+                const T cosAtLight = -dot(cp.isect.shadingNormal, dir);
+                T directPdf(L.invTotalArea);
+                T emissionPdf = cosAtLight * directPdf * kInvPi;
+                cp.throughput = cmul(cp.throughput, tv<T>(V3(L.emission[0], L.emission[1], L.emission[2])));
+                const float pick = pick_light_prob(s, li);
+                directPdf = directPdf * pick;
+                emissionPdf = emissionPdf * pick;
+                const T wCamera = tmis(directPdf) * cp.prev + tmis(emissionPdf) * cp.cur;
+                cp.throughput = cp.throughput * (1.0f / (1.0f + wCamera));
+                contrib = cp.throughput;
+                break;
+            }
+            cp.prev = cp.prev * tmis(dot(org - cp.isect.position, org - cp.isect.position));
+            {
+                const T invCos = 1.0f / tmis(fabs(dot(dir, cp.isect.shadingNormal)));
+                cp.prev = cp.prev * invCos;
+                cp.cur = cp.cur * invCos;
+            }
+            if (d == nc - 1) {
+                const Bsdf &b = bsdf_of_tri(s, tri);
+                if (l == 1) {  // DirectLighting (AD)
+                    const T r0 = u[k++], r1 = u[k++];
+                    const Light &L = s.lights[r.dlLight];
+                    TV3<T> dirToLight, lightContrib;
+                    T cosAtLight, directPdf, emissionPdf;
+                    if (L.type == kLightArea) {
+                        TV3<T> pl, nl2;
+                        ad_sample_triangle(s, light_tri(s, L, r.dlPrim), r0, r1, pl, nl2);
+                        dirToLight = pl - cp.isect.position;
+                        const T distSq = dot(dirToLight, dirToLight);
+                        const T dist = sqrt(distSq);
+                        dirToLight = TV3<T>(dirToLight.x / dist, dirToLight.y / dist, dirToLight.z / dist);
+                        cosAtLight = -dot(dirToLight, nl2);
+                        directPdf = L.invTotalArea * distSq / cosAtLight;
+                        const TV3<T> E = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2]));
+                        lightContrib = TV3<T>(E.x / directPdf, E.y / directPdf, E.z / directPdf);
+                        emissionPdf = L.invTotalArea * cosAtLight * kInvPi;
+                    } else {
+                        dirToLight = tv<T>(V3(L.pos[0], L.pos[1], L.pos[2])) - cp.isect.position;
+                        const T distSq = dot(dirToLight, dirToLight);
+                        directPdf = distSq;
+                        const T dist = sqrt(distSq);
+                        dirToLight = TV3<T>(dirToLight.x / dist, dirToLight.y / dist, dirToLight.z / dist);
+                        lightContrib = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2])) * (1.0f / distSq);
+                        emissionPdf = T(1.0f / (4.0f * kPi));
+                        cosAtLight = T(1.0f);
+                    }
+                    TBsdf<T> o;
+                    ad_evaluate(b, cp.wi, cp.isect.shadingNormal, dirToLight, o);
+                    const float pick = pick_light_prob(s, r.dlLight);
+                    cp.throughput = cmul(cp.throughput, o.contrib);
+                    cp.throughput = cmul(cp.throughput, lightContrib) * (1.0f / pick);
+                    const T wLight = L.type == kLightPoint ? T(0.0f) : tmis(o.pdf / (pick * directPdf));
+                    const T wCamera = tmis(emissionPdf * o.cosWo / (directPdf * cosAtLight)) * (cp.prev + cp.cur * tmis(o.revPdf));
+                    cp.throughput = cp.throughput * (1.0f / (wLight + 1.0f + wCamera));
+                } else {  // ConnectVertex (AD)
+                    TV3<T> dirToLight = lp.isect.position - cp.isect.position;
+                    const T distSq = dot(dirToLight, dirToLight);
+                    const T dist = sqrt(distSq);
+                    dirToLight = dirToLight * (1.0f / dist);
+                    TBsdf<T> cb, lb;
+                    ad_evaluate(b, cp.wi, cp.isect.shadingNormal, dirToLight, cb);
+                    ad_evaluate(bsdf_of_tri(s, lgtVertTri), lp.wi, lp.isect.shadingNormal, -dirToLight, lb);
+                    const TV3<T> lgtF = lb.contrib * ad_snc(lp.wi, lp.isect, -dirToLight);
+                    const T G = 1.0f / distSq;
+                    const T camA = cb.pdf * lb.cosWo * G;
+                    const T lgtA = lb.pdf * cb.cosWo * G;
+                    const T wLight = tmis(camA) * (lp.prev + lp.cur * tmis(lb.revPdf));
+                    const T wCamera = tmis(lgtA) * (cp.prev + cp.cur * tmis(cb.revPdf));
+                    const T misWeight = 1.0f / (wLight + 1.0f + wCamera);
+                    cp.throughput = cmul(lp.throughput, cp.throughput);
+                    cp.throughput = cmul(cp.throughput, cb.contrib);
+                    cp.throughput = cmul(cp.throughput, lgtF) * (G * misWeight);
+                }
+                contrib = cp.throughput;
+                break;
+            }
+            const T r0 = u[k++], r1 = u[k++];
+            int lcsTri = -1;
+            if (l == 0 && d == nc - 2 && s.opt.useLightCoordinateSampling) {
+                const int lastTri = r.tri[nl + nc - 1];
+                const int li = lastTri >= 0 ? area_light_of_tri(s, lastTri) : -1;
+                if (li >= 0 && s.lights[li].type == kLightArea) lcsTri = lastTri;
+            }
+            ad_bsdf_sampling<T, false>(s, tri, r0, r1, r.disc[vi], (r.useAbs >> vi) & 1u, lcsTri, cp, dir);
+            cp.throughput = cp.throughput * r.rr[vi];
+            org = cp.isect.position;
+        }
+    }
+    return log(tlum(contrib));
+}
+
+}  // namespace drmlt

@@ -1,0 +1,230 @@
+"""Host-side integrator surface over libdrmlt.so.
+
+Mirrors the reference's plugin interface: ``Integrator`` with ``Render()`` and
+``PrePass()`` (src/integrator.h:9-22), constructed from a parsed scene, with
+``output_name`` / ``verbose`` / ``deterministic`` attributes, dispatched on the
+scene's ``integrator`` option like main() (src/main.cpp:104-120). The work runs
+on the GPU through the C ABI; this module only marshals arguments.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .scene import SceneData, SceneDescHolder, load_scene
+
+_INTEGRATORS = {"drmlt": capi.INTEGRATOR_DRMLT, "h2mc": capi.INTEGRATOR_H2MC, "mcmc": capi.INTEGRATOR_MCMC}
+
+
+def make_options(sd: SceneData, *, seed: int = 0x1234ABCD, device: int = 0,
+                 max_derivative_depth: int = 9, **override) -> capi.Options:
+    """drmlt_options from the scene's <dpt> block (unknown DR type -> green, delayed.cpp:352-362)."""
+    o = capi.default_options()
+    d = sd.options
+    if d.integrator not in _INTEGRATORS:
+        raise ValueError("Unknown integrator %r" % d.integrator)
+    o.integrator = _INTEGRATORS[d.integrator]
+    o.dr_type = capi.DR_MIRA if d.type == "mira" else capi.DR_GREEN
+    o.aniso_perturb_prob = d.anisoPerturbProb
+    o.aniso_perturb_stddev = d.anisoperturbstddev
+    o.acceptance_map = int(d.acceptanceMap)
+    o.perturb_stddev = d.perturbStdDev
+    o.large_step_prob = d.largeStepProb
+    o.roughness_threshold = d.roughnessThreshold
+    o.discrete_stddev = d.discreteStdDev
+    o.uniform_mixing_prob = d.uniformMixingProbability
+    o.num_chains = d.numChains
+    o.num_init_samples = d.numInitSamples
+    o.spp = d.spp
+    o.direct_spp = d.directSpp
+    o.min_depth = d.minDepth
+    o.max_depth = d.maxDepth
+    o.seed_offset = d.seedOffset
+    o.use_light_coordinate_sampling = int(d.useLightCoordinateSampling)
+    o.max_derivative_depth = max_derivative_depth
+    o.seed = (seed + d.seedOffset) & 0xFFFFFFFFFFFFFFFF
+    o.device = device
+    for k, v in override.items():
+        setattr(o, k, v)
+    return o
+
+
+class Renderer:
+    """Owns one libdrmlt handle (scene on the device + chain state + film)."""
+
+    def __init__(self, sd: SceneData, options: capi.Options | None = None, **kw):
+        self.scene = sd
+        self.options = options if options is not None else make_options(sd, **kw)
+        self._desc = SceneDescHolder(sd)
+        h = C.c_void_p()
+        capi.check(capi.lib().drmlt_create(C.byref(self._desc.desc), C.byref(self.options), C.byref(h)))
+        self.handle = h
+        self.b = None
+
+    def close(self):
+        if self.handle:
+            capi.lib().drmlt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def prepass(self) -> float:
+        b = C.c_float()
+        capi.check(capi.lib().drmlt_prepass(self.handle, C.byref(b)))
+        self.b = b.value
+        return self.b
+
+    def direct(self):
+        capi.check(capi.lib().drmlt_direct(self.handle))
+
+    def run(self, iterations: int) -> int:
+        done = C.c_int64()
+        capi.check(capi.lib().drmlt_run(self.handle, int(iterations), C.byref(done)))
+        return done.value
+
+    def render(self):
+        capi.check(capi.lib().drmlt_render(self.handle))
+
+    def last_run_ms(self) -> float:
+        ms = C.c_float()
+        capi.check(capi.lib().drmlt_last_run_ms(self.handle, C.byref(ms)))
+        return ms.value
+
+    STAGES = ("stage1", "derivs_x", "gauss_x", "stage2", "derivs_z", "gauss_z", "finish")
+
+    def profile(self, iterations: int):
+        ms = np.zeros(len(self.STAGES), np.float32)
+        done = C.c_int64()
+        capi.check(capi.lib().drmlt_profile(self.handle, int(iterations), capi.ptr(ms), C.byref(done)))
+        return dict(zip(self.STAGES, ms.tolist())), done.value
+
+    def total_iterations(self) -> int:
+        n = C.c_int64()
+        capi.check(capi.lib().drmlt_total_iterations(self.handle, C.byref(n)))
+        return n.value
+
+    def film(self) -> np.ndarray:
+        out = np.zeros((self.scene.height, self.scene.width, 3), np.float32)
+        capi.check(capi.lib().drmlt_get_film(self.handle, capi.ptr(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = capi.Stats()
+        capi.check(capi.lib().drmlt_get_stats(self.handle, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in capi.Stats._fields_}
+
+    # ---- per-path entry points
+    def path_eval(self, paths: np.ndarray, u: np.ndarray) -> np.ndarray:
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        u = np.ascontiguousarray(u, np.float32).reshape(len(paths), capi.MAX_DIM)
+        out = np.zeros(len(paths), np.float32)
+        capi.check(capi.lib().drmlt_path_eval(self.handle, capi.ptr(paths), capi.ptr(u), len(paths), capi.ptr(out)))
+        return out
+
+    def path_grad_hess(self, paths: np.ndarray, u: np.ndarray):
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        u = np.ascontiguousarray(u, np.float32).reshape(n, capi.MAX_DIM)
+        g = np.zeros((n, capi.MAX_DIM), np.float32)
+        h = np.zeros((n, capi.MAX_DIM * capi.MAX_DIM), np.float32)
+        capi.check(capi.lib().drmlt_path_grad_hess(self.handle, capi.ptr(paths), capi.ptr(u), n, capi.ptr(g),
+                                                    capi.ptr(h)))
+        return g, h
+
+    def perturb(self, paths: np.ndarray, offsets: np.ndarray):
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        off = np.ascontiguousarray(offsets, np.float32).reshape(n, capi.MAX_DIM)
+        out = np.zeros(n, capi.PATH_DTYPE)
+        ct = np.zeros(n, capi.CONTRIB_DTYPE)
+        capi.check(capi.lib().drmlt_perturb(self.handle, capi.ptr(paths), capi.ptr(off), n, capi.ptr(out),
+                                             capi.ptr(ct)))
+        return out, ct
+
+    def replay(self, mode: int, tapes: list, cam_len=None, lgt_len=None, max_contribs: int = 64):
+        n = len(tapes)
+        stride = max(1, max(len(t) for t in tapes))
+        T = np.zeros((n, stride), np.float32)
+        lens = np.zeros(n, np.int32)
+        for i, t in enumerate(tapes):
+            T[i, :len(t)] = t
+            lens[i] = len(t)
+        mc = max_contribs if mode != 1 else 1
+        cnt = np.zeros(n, np.int32)
+        tech = np.zeros((n, mc, 2), np.int32)
+        ct = np.zeros((n, mc), capi.CONTRIB_DTYPE)
+        pth = np.zeros(n, capi.PATH_DTYPE)
+        cons = np.zeros(n, np.int32)
+        cl = np.ascontiguousarray(cam_len if cam_len is not None else np.zeros(n), np.int32)
+        ll = np.ascontiguousarray(lgt_len if lgt_len is not None else np.zeros(n), np.int32)
+        capi.check(capi.lib().drmlt_replay(self.handle, mode, capi.ptr(T), capi.ptr(lens), stride, n, capi.ptr(cl),
+                                            capi.ptr(ll), mc, capi.ptr(cnt), capi.ptr(tech), capi.ptr(ct),
+                                            capi.ptr(pth), capi.ptr(cons)))
+        return cnt, tech, ct, pth, cons
+
+    def trace_rays(self, org, dirs, tmin=1e-3, tmax=float("inf"), any_hit=False):
+        org = np.ascontiguousarray(org, np.float32).reshape(-1, 3)
+        dirs = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        n = len(org)
+        tri = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        capi.check(capi.lib().drmlt_trace_rays(self.handle, capi.ptr(org), capi.ptr(dirs), tmin, tmax, n,
+                                                int(any_hit), capi.ptr(tri), capi.ptr(t)))
+        return tri, t
+
+    def compute_gaussian(self, dims, ss, grad, hess):
+        n = len(dims)
+        dims = np.ascontiguousarray(dims, np.int32)
+        ss = np.ascontiguousarray(ss, np.float32)
+        grad = np.ascontiguousarray(grad, np.float32).reshape(n, capi.MAX_DIM)
+        hess = np.ascontiguousarray(hess, np.float32).reshape(n, capi.MAX_DIM * capi.MAX_DIM)
+        mean = np.zeros((n, capi.MAX_DIM))
+        ic = np.zeros((n, capi.MAX_DIM * capi.MAX_DIM))
+        cv = np.zeros((n, capi.MAX_DIM * capi.MAX_DIM))
+        ld = np.zeros(n)
+        capi.check(capi.lib().drmlt_compute_gaussian(self.handle, capi.ptr(dims), capi.ptr(ss), capi.ptr(grad),
+                                                      capi.ptr(hess), n, capi.ptr(mean), capi.ptr(ic),
+                                                      capi.ptr(cv), capi.ptr(ld)))
+        return mean, ic, cv, ld
+
+
+class Integrator:
+    """src/integrator.h:9-22: Render() writes the film; PrePass() returns b."""
+
+    def __init__(self, scene: SceneData, **kw):
+        self.scene = scene
+        self.output_name = ""
+        self.verbose = True
+        self.deterministic = False
+        self.renderer = Renderer(scene, **kw)
+
+    def PrePass(self) -> float:
+        return self.renderer.prepass()
+
+    def Render(self) -> np.ndarray:
+        self.renderer.render()
+        return self.renderer.film()
+
+
+class DRIntegrator(Integrator):
+    """Delayed-rejection MLT (src/integrators/delayed/delayed.cpp)."""
+
+
+def make_integrator(xml_path: str, **kw) -> Integrator:
+    """main()'s dispatch on the scene's integrator (src/main.cpp:104-120)."""
+    sd = load_scene(xml_path)
+    if sd.options.integrator == "drmlt":
+        return DRIntegrator(sd, **kw)
+    raise NotImplementedError("integrator %r is not implemented on the GPU path yet" % sd.options.integrator)

@@ -1,0 +1,175 @@
+"""Seeded synthetic scenes written in the reference's scene-XML + OBJ format.
+
+The same files are read by the reference renderer (src/parsescene.cpp:566-599,
+src/parseobj.cpp) and by this library's loader (drmlt/scene.py), so both sides
+render identical geometry, materials and options.
+
+Workloads:
+  * ``cornell``: Cornell box of 34 triangles (5 wall quads + 2 axis-aligned boxes,
+    one OBJ shape each) plus a 0.25 x 0.25 area-light quad (2 triangles) of
+    radiance 15. Walls/boxes are Lambertian with reflectance U[0.2, 0.8]^3, or
+    Phong (exponent log-U[10, 1000], ks U[0.1, 0.5]) when ``phong=True``.
+    Pinhole camera, fov 40 degrees.
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Quads are (corner, edge_u, edge_v) with the normal = edge_u x edge_v pointing
+# into the room; each becomes two triangles (0,1,2) (0,2,3).
+_WALLS = {
+    "floor": ((-1.0, -1.0, 1.0), (2.0, 0.0, 0.0), (0.0, 0.0, -2.0)),
+    "ceiling": ((-1.0, 1.0, -1.0), (2.0, 0.0, 0.0), (0.0, 0.0, 2.0)),
+    "back": ((-1.0, -1.0, -1.0), (2.0, 0.0, 0.0), (0.0, 2.0, 0.0)),
+    "left": ((-1.0, -1.0, 1.0), (0.0, 0.0, -2.0), (0.0, 2.0, 0.0)),
+    "right": ((1.0, -1.0, -1.0), (0.0, 0.0, 2.0), (0.0, 2.0, 0.0)),
+}
+
+# Axis-aligned boxes: (min corner, max corner).
+_BOXES = {
+    "shortbox": ((0.05, -1.0, 0.0), (0.65, -0.4, 0.6)),
+    "tallbox": ((-0.65, -1.0, -0.65), (-0.05, 0.2, -0.05)),
+}
+
+
+def _quad_tris(corner, eu, ev):
+    c = np.asarray(corner, np.float64)
+    eu = np.asarray(eu, np.float64)
+    ev = np.asarray(ev, np.float64)
+    v = np.stack([c, c + eu, c + eu + ev, c + ev])
+    n = np.cross(eu, ev)
+    n /= np.linalg.norm(n)
+    return v, n
+
+
+def _box_quads(lo, hi):
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    dx, dy, dz = x1 - x0, y1 - y0, z1 - z0
+    # outward normals
+    return [
+        ((x0, y1, z1), (dx, 0, 0), (0, 0, -dz)),   # top (+y)
+        ((x0, y0, z0), (dx, 0, 0), (0, 0, dz)),    # bottom (-y)
+        ((x0, y0, z1), (dx, 0, 0), (0, dy, 0)),    # front (+z)
+        ((x1, y0, z0), (-dx, 0, 0), (0, dy, 0)),   # back (-z)
+        ((x1, y0, z1), (0, 0, -dz), (0, dy, 0)),   # right (+x)
+        ((x0, y0, z0), (0, 0, dz), (0, dy, 0)),    # left (-x)
+    ]
+
+
+def _write_obj(path, quads):
+    lines = []
+    vi = 1
+    for corner, eu, ev in quads:
+        v, n = _quad_tris(corner, eu, ev)
+        for p in v:
+            lines.append("v %.9g %.9g %.9g" % tuple(p))
+        lines.append("vn %.9g %.9g %.9g" % tuple(n))
+        ni = len([l for l in lines if l.startswith("vn ")])
+        lines.append("f %d//%d %d//%d %d//%d" % (vi, ni, vi + 1, ni, vi + 2, ni))
+        lines.append("f %d//%d %d//%d %d//%d" % (vi, ni, vi + 2, ni, vi + 3, ni))
+        vi += 4
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+@dataclass
+class SceneOptions:
+    """The reference's ``<dpt>`` option block (src/dptoptions.h:7-38)."""
+
+    integrator: str = "drmlt"
+    type: str = "green"
+    spp: int = 64
+    numinitsamples: int = 100000
+    numchains: int = 4096
+    maxdepth: int = 5
+    mindepth: int = -1
+    directspp: int = 16
+    perturbstddev: float = 1.0 / 64.0
+    largestepprob: float = 0.3
+    anisoperturbprob: float = 0.5
+    anisoperturbstddev: float = 0.0025
+    acceptanceMap: bool = False
+    seedoffset: int = 0
+    extra: dict = field(default_factory=dict)
+
+    def xml(self) -> str:
+        rows = [
+            ("string", "integrator", self.integrator),
+            ("string", "type", self.type),
+            ("integer", "spp", self.spp),
+            ("integer", "numinitsamples", self.numinitsamples),
+            ("integer", "numchains", self.numchains),
+            ("integer", "maxdepth", self.maxdepth),
+            ("integer", "mindepth", self.mindepth),
+            ("integer", "directspp", self.directspp),
+            ("float", "perturbstddev", "%.9g" % self.perturbstddev),
+            ("float", "largestepprob", "%.9g" % self.largestepprob),
+            ("float", "anisoperturbprob", "%.9g" % self.anisoperturbprob),
+            ("float", "anisoperturbstddev", "%.9g" % self.anisoperturbstddev),
+            ("boolean", "acceptanceMap", "true" if self.acceptanceMap else "false"),
+            ("integer", "seedoffset", self.seedoffset),
+        ]
+        for k, v in self.extra.items():
+            rows.append(("string", k, v))
+        body = "\n".join('    <%s name="%s" value="%s"/>' % r for r in rows)
+        return "  <dpt>\n%s\n  </dpt>\n" % body
+
+
+def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int = 256,
+                  phong: bool = False, options: SceneOptions | None = None,
+                  filename: str = "scene.xml") -> str:
+    """Writes the Cornell-box workload; returns the XML path."""
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    options = options or SceneOptions()
+    shapes = []
+    names = list(_WALLS) + list(_BOXES)
+    for name in names:
+        quads = [_WALLS[name]] if name in _WALLS else _box_quads(*_BOXES[name])
+        _write_obj(os.path.join(outdir, name + ".obj"), quads)
+        kd = rng.uniform(0.2, 0.8, 3)
+        if phong:
+            expo = float(np.exp(rng.uniform(np.log(10.0), np.log(1000.0))))
+            ks = float(rng.uniform(0.1, 0.5))
+            bsdf = ('<bsdf type="phong"><rgb name="diffuseReflectance" value="%.9g %.9g %.9g"/>'
+                    '<rgb name="specularReflectance" value="%.9g %.9g %.9g"/>'
+                    '<float name="exponent" value="%.9g"/></bsdf>'
+                    % (*kd, ks, ks, ks, expo))
+        else:
+            bsdf = '<bsdf type="diffuse"><rgb name="reflectance" value="%.9g %.9g %.9g"/></bsdf>' % tuple(kd)
+        shapes.append('  <shape type="obj"><string name="filename" value="%s.obj"/>%s</shape>'
+                      % (name, bsdf))
+    # Area light: 0.25 x 0.25 quad just below the ceiling, facing down.
+    _write_obj(os.path.join(outdir, "light.obj"),
+               [((-0.125, 0.999, -0.125), (0.25, 0.0, 0.0), (0.0, 0.0, 0.25))])
+    shapes.append('  <shape type="obj"><string name="filename" value="light.obj"/>'
+                  '<bsdf type="diffuse"><rgb name="reflectance" value="0 0 0"/></bsdf>'
+                  '<emitter type="area"><rgb name="radiance" value="15 15 15"/></emitter></shape>')
+    sensor = ('  <sensor type="perspective">\n'
+              '    <float name="fov" value="40"/>\n'
+              '    <transform name="toWorld"><lookat origin="0, 0, 3.5" target="0, 0, 0" up="0, 1, 0"/></transform>\n'
+              '    <film type="hdrfilm"><integer name="width" value="%d"/><integer name="height" value="%d"/>'
+              '<string name="filename" value="image.exr"/></film>\n'
+              '  </sensor>\n' % (width, height))
+    xml = ('<?xml version="1.0" encoding="utf-8"?>\n<scene version="0.5.0">\n'
+           + options.xml() + sensor + "\n".join(shapes) + "\n</scene>\n")
+    path = os.path.join(outdir, filename)
+    with open(path, "w") as f:
+        f.write(xml)
+    return path
+
+
+def config1(outdir: str) -> str:
+    """Plain DRMLT (green) on the 256x256 Lambertian Cornell box, max depth 5, 4096 chains."""
+    return write_cornell(outdir, seed=1, width=256, height=256, phong=False,
+                         options=SceneOptions(maxdepth=5, numchains=4096, spp=64, type="green"))
+
+
+def config2(outdir: str, dr_type: str = "mira") -> str:
+    """H2MC second stage on the Phong Cornell box at 1024x1024, max depth 8, 16384 chains."""
+    return write_cornell(outdir, seed=2, width=1024, height=1024, phong=True,
+                         options=SceneOptions(maxdepth=8, numchains=16384, spp=64, type=dr_type))

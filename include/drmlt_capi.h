@@ -1,0 +1,232 @@
+/*
+ * drmlt_capi.h -- C ABI of the GB300 DRMLT hot path (libdrmlt.so).
+ *
+ * One handle owns a scene uploaded to one CUDA device, the Markov-chain state
+ * of one render and its film. Handles are not thread-safe; use one per host
+ * thread / stream. Every call returns 0 on success or a negative DRMLT_E*
+ * code; drmlt_last_error() gives a message. All pointers are host pointers.
+ *
+ * Reference interfaces replaced (joeylitalien/drmlt-dpt):
+ *   Integrator{Render, PrePass}            src/integrator.h:9-22
+ *   DRIntegrator                           src/integrators/delayed/delayed.{h,cpp}
+ *   H2MCIntegrator / MCMCIntegrator        src/integrators/h2mc.cpp, src/integrators/mcmc.cpp
+ *   DptOptions (<dpt> XML block)           src/dptoptions.h:7-38, src/parsescene.cpp:505-564
+ *   PathFuncDerv (chad-generated library)  src/path.h:145-160
+ */
+#ifndef DRMLT_CAPI_H
+#define DRMLT_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DRMLT_OK 0
+#define DRMLT_E_ARG (-1)       /* invalid argument */
+#define DRMLT_E_CUDA (-2)      /* CUDA error (device missing, launch failure, ...) */
+#define DRMLT_E_STATE (-3)     /* call out of order (e.g. run before prepass) */
+#define DRMLT_E_OVERFLOW (-4)  /* a fixed-capacity buffer overflowed */
+
+#define DRMLT_MAX_LEN 12           /* longest path (segments) a chain may hold */
+#define DRMLT_MAX_DIM 24           /* 2 * DRMLT_MAX_LEN */
+
+/* BSDF kinds (src/bsdf.h:7) */
+#define DRMLT_BSDF_LAMBERTIAN 0
+#define DRMLT_BSDF_PHONG 1
+#define DRMLT_BSDF_ROUGHDIELECTRIC 2
+/* light kinds (src/light.h:7) */
+#define DRMLT_LIGHT_POINT 0
+#define DRMLT_LIGHT_AREA 1
+#define DRMLT_LIGHT_ENV 2
+/* integrators (src/main.cpp:104-120) and DR frameworks (delayed.h:22-25) */
+#define DRMLT_INTEGRATOR_DRMLT 0
+#define DRMLT_INTEGRATOR_H2MC 1
+#define DRMLT_INTEGRATOR_MCMC 2
+#define DRMLT_DR_GREEN 0
+#define DRMLT_DR_MIRA 1
+
+typedef struct drmlt_bsdf {
+    int32_t type;
+    int32_t two_sided;
+    float kd[3];         /* Lambertian reflectance / Phong diffuse */
+    float ks[3];         /* Phong specular */
+    float exponent;      /* Phong exponent */
+    float int_ior, ext_ior, alpha;  /* rough dielectric (not yet supported) */
+    float kt[3];
+} drmlt_bsdf;
+
+typedef struct drmlt_light {
+    int32_t type;
+    int32_t shape;       /* area light: emitting shape index */
+    float emission[3];   /* area: radiance, point: intensity */
+    float pos[3];        /* point light position */
+    float sampling_weight;
+} drmlt_light;
+
+/* Triangles are listed shape by shape (shape k owns a contiguous range).
+ * Matrices are row-major 4x4, exactly the reference camera's
+ * sampleToCam / camToSample / camToWorld / worldToCamera (src/camera.cpp:11-28). */
+typedef struct drmlt_scene_desc {
+    int32_t num_tris;
+    const float *positions;   /* num_tris x 3 vertices x xyz */
+    const float *normals;     /* num_tris x 3 vertices x xyz (shading normals) */
+    int32_t num_shapes;
+    const int32_t *shape_first_tri;
+    const int32_t *shape_num_tris;
+    const int32_t *shape_bsdf;
+    const int32_t *shape_light;  /* area light index or -1 */
+    int32_t num_bsdfs;
+    const drmlt_bsdf *bsdfs;
+    int32_t num_lights;
+    const drmlt_light *lights;
+    float sample_to_cam[16], cam_to_sample[16], cam_to_world[16], world_to_cam[16];
+    float cam_dist, near_clip, far_clip;
+    int32_t width, height;
+    float bsphere_center[3], bsphere_radius;
+} drmlt_scene_desc;
+
+/* DptOptions (src/dptoptions.h:7-38) plus GPU controls. */
+typedef struct drmlt_options {
+    int32_t integrator;          /* DRMLT_INTEGRATOR_* */
+    int32_t dr_type;             /* DRMLT_DR_GREEN | DRMLT_DR_MIRA */
+    float aniso_perturb_prob;    /* anisoperturbprob */
+    float aniso_perturb_stddev;  /* second-stage isotropic sigma (reference keeps 0.0025, see DESIGN) */
+    int32_t acceptance_map;
+    float perturb_stddev;
+    float large_step_prob;
+    float roughness_threshold;
+    float discrete_stddev;
+    float uniform_mixing_prob;   /* h2mc integrator */
+    int32_t num_chains;
+    int32_t num_init_samples;
+    int32_t spp;
+    int32_t direct_spp;
+    int32_t min_depth;
+    int32_t max_depth;
+    int32_t seed_offset;
+    int32_t use_light_coordinate_sampling;
+    int32_t max_derivative_depth; /* --max-derivatives-depth (default 9) */
+    uint64_t seed;                /* GPU random-stream key */
+    int32_t device;               /* CUDA device ordinal */
+    int32_t use_graph;            /* capture each iteration as a CUDA graph */
+} drmlt_options;
+
+/* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels). */
+typedef struct drmlt_stats {
+    uint64_t large_step, large_step_accepted;
+    uint64_t stage1, stage1_accepted;
+    uint64_t stage2_iso, stage2_iso_accepted;
+    uint64_t stage2_h2mc, stage2_h2mc_accepted;
+    uint64_t mutations;
+} drmlt_stats;
+
+/* A technique path (one Markov state): SubpathContrib camDepth c / lightDepth l,
+ * the primary sample vector u (GetPathPos order, src/path.cpp:2393-2439, 2(c+l-1)
+ * entries), and per surface vertex (light-subpath vertices first, then camera
+ * ones) the hit triangle (global index), bsdfDiscrete, rrWeight and
+ * useAbsoluteParam bit. */
+typedef struct drmlt_path {
+    int32_t c, l;
+    int32_t lgt_light, lgt_prim;
+    int32_t dl_light, dl_prim;
+    uint32_t use_abs;
+    float u[DRMLT_MAX_DIM];
+    int32_t tri[DRMLT_MAX_LEN];
+    float disc[DRMLT_MAX_LEN];
+    float rr[DRMLT_MAX_LEN];
+} drmlt_path;
+
+/* A contribution (SubpathContrib, src/path.h:12-24): screen[2], rgb[3], ls, ss, valid. */
+typedef struct drmlt_contrib {
+    float screen[2];
+    float rgb[3];
+    float ls, ss;
+    int32_t valid;
+} drmlt_contrib;
+
+/* Fills *opt with the reference's DptOptions defaults. */
+void drmlt_default_options(drmlt_options *opt);
+
+const char *drmlt_last_error(void);
+
+/* Integrator construction: uploads the scene and builds the BVH
+ * (replaces Scene::Scene + DRIntegrator ctor, src/scene.cpp:10-54, delayed.cpp:7-8). */
+int drmlt_create(const drmlt_scene_desc *scene, const drmlt_options *opt, void **handle);
+int drmlt_destroy(void *handle);
+
+/* PrePass (delayed.cpp:14-173): bootstrap sampling, length distribution,
+ * equal-spaced chain seeding. Writes the normalisation b. */
+int drmlt_prepass(void *handle, float *b_out);
+
+/* DirectLighting pass (src/integrator.h:33-75). */
+int drmlt_direct(void *handle);
+
+/* Runs `iterations` Markov-chain iterations on every chain (each chain runs at
+ * most its share spp*W*H/numChains, the reference's sample split, delayed.cpp:205-210).
+ * Returns the number of mutations done in *done (may be NULL). */
+int drmlt_run(void *handle, int64_t iterations, int64_t *done);
+
+/* Integrator::Render (delayed.cpp:181-686): prepass + direct + all iterations. */
+int drmlt_render(void *handle);
+
+/* Final film (direct/directSpp + indirect/spp, delayed.cpp:681-685), W*H*3 floats. */
+int drmlt_get_film(void *handle, float *rgb);
+int drmlt_get_stats(void *handle, drmlt_stats *stats);
+/* Device time of the last drmlt_run in milliseconds (CUDA events). */
+int drmlt_last_run_ms(void *handle, float *ms);
+
+/* drmlt_run with CUDA events around each stage kernel (same work, serialised
+ * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,
+ * derivs(z), gauss(z), finish milliseconds. */
+int drmlt_profile(void *handle, int64_t iterations, float *stage_ms, int64_t *done);
+
+/* Iterations a full render runs (spp*W*H/numChains, plus one for the chains
+ * that get an extra sample). */
+int drmlt_total_iterations(void *handle, int64_t *iterations);
+
+/* ---- per-path entry points (parity harness; n paths per call) ---- */
+
+/* Forward: log Luminance(contribution) of each technique path at primary vector
+ * u (2(c+l-1) floats per path, DRMLT_MAX_DIM stride), as the chad-generated
+ * evaluate_path_bidir_<c>_<l>_static computes it (src/path.cpp:2987-3175). */
+int drmlt_path_eval(void *handle, const drmlt_path *paths, const float *u, int n, float *logf);
+
+/* Backward pair of drmlt_path_eval: gradient (DRMLT_MAX_DIM stride) and Hessian
+ * (DRMLT_MAX_DIM^2 stride, row-major) of log f, the PathFuncDerv call of
+ * drsmallstep.cpp:128-158. */
+int drmlt_path_grad_hess(void *handle, const drmlt_path *paths, const float *u, int n, float *grad,
+                         float *hess);
+
+/* PerturbPathBidir (src/path.cpp:1480-1628) with discrete jitter off:
+ * offsets (DRMLT_MAX_DIM stride) -> perturbed paths and contributions. */
+int drmlt_perturb(void *handle, const drmlt_path *in, const float *offset, int n, drmlt_path *out,
+                  drmlt_contrib *contrib);
+
+/* Replays recorded uniform streams through GeneratePathBidir (mode 0,
+ * src/path.cpp:978-1121), GenerateSubpath (mode 1, camLength/lgtLength per
+ * stream in cam_len/lgt_len, src/path.cpp:1123-1269) or the direct-lighting
+ * GeneratePath (mode 2, pixel x/y in cam_len/lgt_len, src/path.cpp:343-445 as
+ * called by src/integrator.h:33-75). tapes: n x stride floats, tape_len[i] used.
+ * Modes 0 and 2 write up to max_contribs contributions per stream (c, l in
+ * out_tech[2*k], count in out_count); mode 1 writes one path and contribution. */
+int drmlt_replay(void *handle, int mode, const float *tapes, const int32_t *tape_len, int stride, int n,
+                 const int32_t *cam_len, const int32_t *lgt_len, int max_contribs, int32_t *out_count,
+                 int32_t *out_tech, drmlt_contrib *out_contrib, drmlt_path *out_path, int32_t *out_consumed);
+
+/* Closest-hit (any_hit = 0) or occlusion (any_hit = 1) ray casts against the
+ * scene BVH, the rtcIntersect / rtcOccluded calls of src/scene.cpp:80-111.
+ * org/dir: n x 3 floats. Writes the global triangle index (-1 = miss) and hit t. */
+int drmlt_trace_rays(void *handle, const float *org, const float *dir, float tmin, float tmax, int n, int any_hit,
+                     int32_t *tri, float *t);
+
+/* ComputeGaussian (drsmallstep.cpp:219-266) in FP64: returns mean (MAX_DIM),
+ * invCov and cov (MAX_DIM^2 each, row-major) and logDet per input. */
+int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, const float *grad,
+                           const float *hess, int n, double *mean, double *inv_cov, double *cov,
+                           double *log_det);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DRMLT_CAPI_H */

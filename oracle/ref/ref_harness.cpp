@@ -1,0 +1,404 @@
+// Golden-vector harness around the reference's own functions (test
+// infrastructure; links the reference objects built by oracle/ref/Makefile).
+//
+// It calls, unmodified:
+//   GeneratePathBidir      src/path.cpp:978-1121  (prepass / bootstrap sampler)
+//   GenerateSubpath        src/path.cpp:1123-1269 (multiplexed large step)
+//   GeneratePath           src/path.cpp:343-445   (direct-lighting pass)
+//   PerturbPathBidir       src/path.cpp:1480-1628 (small steps, Green y*)
+//   GetPathPos / Serialize src/path.cpp:2303-2439
+//   chad static path function + derivative (generated pathlibbidir.so)
+//   PH2MCSmallStep::ComputeGaussian src/integrators/delayed/drsmallstep.cpp:219-266
+// and writes JSON lines. Every random number a sampler consumed is recorded
+// (the reference draws them with std::uniform_real_distribution from a
+// pcg32_k64_fast stream), so a replay of the same stream must reproduce the
+// same path exactly. Perturbations run with discreteStdDev = 0 so that only
+// the continuous offsets move the path.
+//
+// usage: ref_harness <scene.xml> <libdir> <maxDervDepth> <out.jsonl> <mode> <seed0> <count> [extra]
+//   mode = bidir | subpath | direct | tech
+#include "parsescene.h"
+#include "path.h"
+#include "scene.h"
+#include "shape.h"
+#include "light.h"
+#include "camera.h"
+#include "gaussian.h"
+#include "integrators/delayed/drsmallstep.h"
+#include "texturesystem.h"
+#include <cstdio>
+#include <unistd.h>
+
+namespace {
+
+const Scene *g_scene = nullptr;
+FILE *g_out = nullptr;
+
+int ShapeIndex(const Shape *s) {
+    if (s == nullptr) return -1;
+    for (size_t i = 0; i < g_scene->objects.size(); i++)
+        if (g_scene->objects[i].get() == s) return int(i);
+    return -2;
+}
+
+int LightIndex(const Light *l) {
+    if (l == nullptr) return -1;
+    for (size_t i = 0; i < g_scene->lights.size(); i++)
+        if (g_scene->lights[i].get() == l) return int(i);
+    return -2;
+}
+
+void F(double v) {
+    if (std::isfinite(v)) fprintf(g_out, "%.9g", v);
+    else fprintf(g_out, "null");
+}
+
+template <typename V>
+void Arr(const V &v, int n) {
+    fputc('[', g_out);
+    for (int i = 0; i < n; i++) {
+        if (i) fputc(',', g_out);
+        F(double(v[i]));
+    }
+    fputc(']', g_out);
+}
+
+void DumpVertex(const SurfaceVertex &v) {
+    fprintf(g_out, "{\"shape\":%d,\"prim\":%d,\"bsdfRnd\":", ShapeIndex(v.shapeInst.obj),
+            v.shapeInst.obj ? v.shapeInst.primID : -1);
+    Arr(v.bsdfRndParam, 2);
+    fprintf(g_out, ",\"disc\":");
+    F(v.bsdfDiscrete);
+    fprintf(g_out, ",\"useAbs\":");
+    F(v.useAbsoluteParam);
+    fprintf(g_out, ",\"rr\":");
+    F(v.rrWeight);
+    fprintf(g_out, ",\"dlLight\":%d,\"dlPrim\":%d,\"dlRnd\":", LightIndex(v.directLightInst.light),
+            v.directLightInst.light ? v.directLightInst.lPrimID : -1);
+    Arr(v.directLightRndParam, 2);
+    fputc('}', g_out);
+}
+
+void DumpPath(const Path &p) {
+    fprintf(g_out, "{\"time\":");
+    F(p.time);
+    fprintf(g_out, ",\"lgtLight\":%d,\"lgtPrim\":%d,\"lgtPos\":", LightIndex(p.lgtVertex.lightInst.light),
+            p.lgtVertex.lightInst.light ? p.lgtVertex.lightInst.lPrimID : -1);
+    Arr(p.lgtVertex.rndParamPos, 2);
+    fprintf(g_out, ",\"lgtDir\":");
+    Arr(p.lgtVertex.rndParamDir, 2);
+    fprintf(g_out, ",\"screen\":");
+    Arr(p.camVertex.screenPos, 2);
+    fprintf(g_out, ",\"lgtSurf\":[");
+    for (size_t i = 0; i < p.lgtSurfaceVertex.size(); i++) {
+        if (i) fputc(',', g_out);
+        DumpVertex(p.lgtSurfaceVertex[i]);
+    }
+    fprintf(g_out, "],\"camSurf\":[");
+    for (size_t i = 0; i < p.camSurfaceVertex.size(); i++) {
+        if (i) fputc(',', g_out);
+        DumpVertex(p.camSurfaceVertex[i]);
+    }
+    fprintf(g_out, "],\"isSubpath\":%d,\"camDepth\":%d,\"lgtDepth\":%d}", int(p.isSubpath),
+            p.isSubpath ? p.camDepth : -1, p.isSubpath ? p.lgtDepth : -1);
+}
+
+void DumpContribs(const std::vector<SubpathContrib> &cs) {
+    fputc('[', g_out);
+    for (size_t i = 0; i < cs.size(); i++) {
+        const SubpathContrib &c = cs[i];
+        if (i) fputc(',', g_out);
+        fprintf(g_out, "{\"camDepth\":%d,\"lightDepth\":%d,\"screen\":", c.camDepth, c.lightDepth);
+        Arr(c.screenPos, 2);
+        fprintf(g_out, ",\"contrib\":");
+        Arr(c.contrib, 3);
+        fprintf(g_out, ",\"ls\":");
+        F(c.lsScore);
+        fprintf(g_out, ",\"ss\":");
+        F(c.ssScore);
+        fprintf(g_out, ",\"mis\":");
+        F(c.misWeight);
+        fputc('}', g_out);
+    }
+    fputc(']', g_out);
+}
+
+// Records the uniforms a sampler seeded with `seed` will hand out, and after the
+// sampler ran, how many it consumed.
+struct UniformTape {
+    std::vector<float> values;
+    RNG start;
+    explicit UniformTape(uint64_t seed, int n) : start(seed) {
+        RNG copy = start;
+        std::uniform_real_distribution<Float> uni(Float(0.0), Float(1.0));
+        for (int i = 0; i < n; i++) values.push_back(uni(copy));
+    }
+    // Number of uniforms consumed: the position in the recorded stream where the
+    // sampler's remaining draws continue.
+    int Consumed(const RNG &after) const {
+        RNG next = after;
+        std::uniform_real_distribution<Float> uni(Float(0.0), Float(1.0));
+        float probe[8];
+        for (int k = 0; k < 8; k++) probe[k] = uni(next);
+        for (int i = 0; i + 8 <= int(values.size()); i++) {
+            bool same = true;
+            for (int k = 0; k < 8 && same; k++) same = values[i + k] == probe[k];
+            if (same) return i;
+        }
+        return -1;
+    }
+    void Dump(int consumed) {
+        fprintf(g_out, "\"uniforms\":");
+        Arr(values, consumed < 0 ? int(values.size()) : consumed);
+        fprintf(g_out, ",\"consumed\":%d", consumed);
+    }
+};
+
+void ModeBidir(uint64_t seed0, int count, int minDepth, int maxDepth) {
+    for (int s = 0; s < count; s++) {
+        UniformTape tape(seed0 + s, 512);
+        RNG rng = tape.start;
+        Path path;
+        std::vector<SubpathContrib> contribs;
+        GeneratePathBidir(g_scene, Vector2i(-1, -1), minDepth, maxDepth, path, contribs, rng);
+        fprintf(g_out, "{\"mode\":\"bidir\",\"seed\":%llu,", (unsigned long long)(seed0 + s));
+        tape.Dump(tape.Consumed(rng));
+        fprintf(g_out, ",\"minDepth\":%d,\"maxDepth\":%d,\"path\":", minDepth, maxDepth);
+        DumpPath(path);
+        fprintf(g_out, ",\"contribs\":");
+        DumpContribs(contribs);
+        fprintf(g_out, "}\n");
+    }
+}
+
+void ModeSubpath(uint64_t seed0, int count, int maxDepth) {
+    for (int s = 0; s < count; s++) {
+        // Technique from the seed, the same way LargeStep::Mutate draws it
+        // (src/mutation.cpp:32-42) but from a separate stream.
+        RNG pick(1000003u * (seed0 + s) + 7u);
+        std::uniform_real_distribution<Float> uni(Float(0.0), Float(1.0));
+        const int length = 3 + std::min(int(uni(pick) * (maxDepth - 2)), maxDepth - 3);
+        const int lgtLength = Clamp(int(uni(pick) * (length + 1)), 0, length);
+        const int camLength = length - lgtLength + 1;
+        UniformTape tape(seed0 + s, 256);
+        RNG rng = tape.start;
+        Path path;
+        std::vector<SubpathContrib> contribs;
+        GenerateSubpath(g_scene, Vector2i(-1, -1), camLength, lgtLength, true, path, contribs, rng);
+        fprintf(g_out, "{\"mode\":\"subpath\",\"seed\":%llu,\"camLength\":%d,\"lgtLength\":%d,",
+                (unsigned long long)(seed0 + s), camLength, lgtLength);
+        tape.Dump(tape.Consumed(rng));
+        fprintf(g_out, ",\"path\":");
+        DumpPath(path);
+        fprintf(g_out, ",\"contribs\":");
+        DumpContribs(contribs);
+        fprintf(g_out, "}\n");
+    }
+}
+
+void ModeDirect(uint64_t seed0, int count) {
+    const Camera *camera = g_scene->camera.get();
+    const int w = GetPixelWidth(camera), h = GetPixelHeight(camera);
+    for (int s = 0; s < count; s++) {
+        const int x = int((seed0 + s) * 7919u % unsigned(w));
+        const int y = int((seed0 + s) * 104729u % unsigned(h));
+        UniformTape tape(seed0 + s, 64);
+        RNG rng = tape.start;
+        Path path;
+        std::vector<SubpathContrib> contribs;
+        GeneratePath(g_scene, Vector2i(x, y), std::min(g_scene->options->minDepth, 2),
+                     std::min(g_scene->options->maxDepth, 2), path, contribs, rng);
+        fprintf(g_out, "{\"mode\":\"direct\",\"seed\":%llu,\"pixel\":[%d,%d],",
+                (unsigned long long)(seed0 + s), x, y);
+        tape.Dump(tape.Consumed(rng));
+        fprintf(g_out, ",\"contribs\":");
+        DumpContribs(contribs);
+        fprintf(g_out, "}\n");
+    }
+}
+
+void ModeTech(uint64_t seed0, int count, int nPerturb, const PathFuncLib &lib, int maxDervDepth) {
+    const int maxDepth = g_scene->options->maxDepth;
+    const int minDepth = std::max(g_scene->options->minDepth, 3);
+    AlignedStdVector sceneParams(GetSceneSerializedSize());
+    Serialize(g_scene, &sceneParams[0]);
+    SerializedSubpath ssub;
+    ssub.primary.resize(GetPrimaryParamSize(maxDervDepth, maxDervDepth));
+    ssub.vertParams.resize(GetVertParamSize(maxDervDepth, maxDervDepth));
+    PH2MCSmallStep h2mc(g_scene, maxDervDepth, g_scene->options->perturbStdDev);
+    const Float sigmas[3] = {g_scene->options->perturbStdDev, Float(0.0025), Float(0.05)};
+    int written = 0;
+    for (int s = 0; written < count && s < 100 * count; s++) {
+        RNG rng(seed0 + s);
+        Path full;
+        std::vector<SubpathContrib> contribs;
+        GeneratePathBidir(g_scene, Vector2i(-1, -1), minDepth, maxDepth, full, contribs, rng);
+        for (const SubpathContrib &c : contribs) {
+            if (written >= count) break;
+            Path path = full;
+            path.Initialize(c.camDepth, c.lightDepth);
+            const int dim = GetDimension(path);
+            const Vector x = GetPathPos(path);
+            fprintf(g_out, "{\"mode\":\"tech\",\"seed\":%llu,\"dim\":%d,\"path\":",
+                    (unsigned long long)(seed0 + s), dim);
+            DumpPath(path);
+            fprintf(g_out, ",\"contrib\":");
+            DumpContribs({c});
+            fprintf(g_out, ",\"pos\":");
+            Arr(x, dim);
+            // Derivatives of log Lum(contrib) from the chad library (static mode,
+            // time excluded), as PH2MCSmallStep::Mutate calls them
+            // (src/integrators/delayed/drsmallstep.cpp:128-158).
+            AlignedStdVector grad(dim, Float(0.0)), hess(dim * dim, Float(0.0));
+            auto dit = lib.staticDervFuncMap.find({c.camDepth, c.lightDepth});
+            auto fit = lib.staticFuncMap.find({c.camDepth, c.lightDepth});
+            bool haveDerv = dit != lib.staticDervFuncMap.end();
+            Float logf = Float(0.0);
+            bool scrubbed = false;
+            if (haveDerv && c.ssScore > Float(1e-15)) {
+                Serialize(g_scene, path, ssub);
+                dit->second(&c.screenPos[0], &ssub.primary[0], &sceneParams[0], &ssub.vertParams[0],
+                            &grad[0], &hess[0]);
+                if (fit != lib.staticFuncMap.end())
+                    fit->second(&c.screenPos[0], &ssub.primary[0], &sceneParams[0], &ssub.vertParams[0],
+                                &logf);
+                if (!IsFinite(grad) || !IsFinite(hess)) {
+                    scrubbed = true;
+                    std::fill(grad.begin(), grad.end(), Float(0.0));
+                    std::fill(hess.begin(), hess.end(), Float(0.0));
+                }
+            }
+            // Central differences of the chad gradient (h = 1e-3, same library): a
+            // consistency check of chad's own Hessian.
+            std::vector<double> fdH(size_t(dim) * dim, 0.0);
+            if (haveDerv && c.ssScore > Float(1e-15)) {
+                AlignedStdVector g2(dim), h2(dim * dim);
+                for (int j = 0; j < dim; j++) {
+                    for (int sgn = -1; sgn <= 1; sgn += 2) {
+                        Path q = path;
+                        SerializedSubpath sq = ssub;
+                        Serialize(g_scene, q, sq);
+                        sq.primary[1 + j] += Float(sgn) * Float(1e-3);
+                        dit->second(&c.screenPos[0], &sq.primary[0], &sceneParams[0], &sq.vertParams[0], &g2[0], &h2[0]);
+                        for (int i = 0; i < dim; i++) fdH[size_t(i) * dim + j] += double(sgn) * double(g2[i]) / 2e-3;
+                    }
+                }
+            }
+            fprintf(g_out, ",\"fdHess\":");
+            Arr(fdH, dim * dim);
+            fprintf(g_out, ",\"haveDerv\":%d,\"scrubbed\":%d,\"logf\":", int(haveDerv), int(scrubbed));
+            F(logf);
+            fprintf(g_out, ",\"grad\":");
+            Arr(grad, dim);
+            fprintf(g_out, ",\"hess\":");
+            Arr(hess, dim * dim);
+            Gaussian g;
+            if (haveDerv) {
+                h2mc.ComputeGaussian(h2mc.param, c.ssScore, grad, hess, g);
+            } else {
+                IsotropicGaussian(dim, h2mc.param.sigma, g);
+            }
+            fprintf(g_out, ",\"gauss\":{\"mean\":");
+            Arr(g.mean, dim);
+            Matrix cov = g.covL * g.covL.transpose();
+            fprintf(g_out, ",\"invCov\":");
+            Arr(g.invCov.data(), dim * dim);
+            fprintf(g_out, ",\"covL\":");
+            Arr(g.covL.data(), dim * dim);
+            fprintf(g_out, ",\"cov\":");
+            Arr(cov.data(), dim * dim);
+            fprintf(g_out, ",\"logDet\":");
+            F(g.logDet);
+            fprintf(g_out, "},\"perturb\":[");
+            for (int p = 0; p < nPerturb; p++) {
+                RNG prng(7777u * (seed0 + s) + 31u * written + p);
+                std::normal_distribution<Float> nd(Float(0.0), sigmas[p % 3]);
+                Vector offset(dim);
+                for (int i = 0; i < dim; i++) offset[i] = nd(prng);
+                Path y = path;
+                std::vector<SubpathContrib> ycs;
+                PerturbPathBidir(g_scene, offset, y, ycs, prng);
+                if (p) fputc(',', g_out);
+                fprintf(g_out, "{\"offset\":");
+                Arr(offset, dim);
+                fprintf(g_out, ",\"logpdf\":");
+                F(GaussianLogPdf(offset, g));
+                fprintf(g_out, ",\"ypos\":");
+                Arr(GetPathPos(y), dim);
+                fprintf(g_out, ",\"path\":");
+                DumpPath(y);
+                fprintf(g_out, ",\"contribs\":");
+                DumpContribs(ycs);
+                fputc('}', g_out);
+            }
+            fprintf(g_out, "]}\n");
+            written++;
+        }
+    }
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc < 8) {
+        fprintf(stderr, "usage: %s scene.xml libdir maxDervDepth out.jsonl mode seed0 count [extra]\n", argv[0]);
+        return 2;
+    }
+    TextureSystem::Init();
+    std::unique_ptr<Scene> scene = ParseScene(argv[1]);
+    scene->options->bidirectional = true;
+    scene->options->discreteStdDev = Float(0.0);
+    g_scene = scene.get();
+    const std::string libdir = argv[2];
+    const int maxDervDepth = atoi(argv[3]);
+    g_out = fopen(argv[4], "w");
+    const std::string mode = argv[5];
+    const uint64_t seed0 = strtoull(argv[6], nullptr, 10);
+    const int count = atoi(argv[7]);
+    const int extra = argc > 8 ? atoi(argv[8]) : 0;
+    if (mode == "camera") {
+        // The reference camera's matrices (src/camera.cpp:11-28, animatedtransform.cpp:33-44).
+        const Camera *cam = scene->camera.get();
+        const Matrix4x4 c2w = Interpolate(cam->camToWorld, Float(0.0));
+        const Matrix4x4 w2c = Interpolate(cam->worldToCamera, Float(0.0));
+        auto M = [&](const char *name, const Matrix4x4 &m) {
+            fprintf(g_out, "\"%s\":[", name);
+            for (int r = 0; r < 4; r++)
+                for (int c = 0; c < 4; c++) {
+                    if (r || c) fputc(',', g_out);
+                    F(m(r, c));
+                }
+            fprintf(g_out, "],");
+        };
+        fputc('{', g_out);
+        M("sampleToCam", cam->sampleToCam);
+        M("camToSample", cam->camToSample);
+        M("camToWorld", c2w);
+        M("worldToCam", w2c);
+        fprintf(g_out, "\"dist\":");
+        F(cam->dist);
+        fprintf(g_out, ",\"near\":");
+        F(cam->nearClip);
+        fprintf(g_out, ",\"far\":");
+        F(cam->farClip);
+        fprintf(g_out, ",\"bsCenter\":");
+        Arr(scene->bSphere.center, 3);
+        fprintf(g_out, ",\"bsRadius\":");
+        F(scene->bSphere.radius);
+        fprintf(g_out, "}\n");
+    } else if (mode == "bidir") {
+        ModeBidir(seed0, count, std::max(scene->options->minDepth, 3), scene->options->maxDepth);
+    } else if (mode == "subpath") {
+        ModeSubpath(seed0, count, scene->options->maxDepth);
+    } else if (mode == "direct") {
+        ModeDirect(seed0, count);
+    } else if (mode == "tech") {
+        if (chdir(libdir.c_str()) != 0) return 3;
+        std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);
+        ModeTech(seed0, count, extra, *lib, maxDervDepth);
+    } else {
+        return 2;
+    }
+    fclose(g_out);
+    return 0;
+}

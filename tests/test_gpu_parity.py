@@ -1,0 +1,216 @@
+"""CUDA path vs the reference's own outputs (golden fixtures from tests/golden/make_golden.py).
+
+Every call goes through libdrmlt.so's C ABI. Tolerances: f (contribution,
+ls, ss) relative 1e-4; derivatives 1e-3 relative to the largest entry of the
+reference's gradient / Hessian; Gaussian (FP64 here, FP32 Eigen in the
+reference) 1e-3 relative. A small fraction of records may legitimately take a
+different branch (a ray grazing a triangle edge resolves differently in the
+reference's double-precision brute-force intersector than in the float BVH);
+each test bounds that fraction explicitly.
+"""
+import numpy as np
+import pytest
+
+from helpers import golden, path_record, rel_err
+
+pytestmark = pytest.mark.gpu
+
+CFGS = ["cfg1", "cfg2"]
+
+
+def _need(cfg, mode):
+    g = golden(cfg, mode)
+    if g is None:
+        pytest.skip("no golden fixture %s_%s" % (cfg, mode))
+    return g
+
+
+def _first_tri(r):
+    return r.scene.shape_first_tri
+
+
+def _cmp_contrib(mine, ref, tol=1e-4):
+    ok = True
+    ok &= np.allclose(mine["screen"], ref["screen"], atol=2e-5, rtol=0)
+    ok &= bool(np.all(rel_err(mine["rgb"], ref["contrib"], 1e-12) < tol) or
+               np.allclose(mine["rgb"], ref["contrib"], rtol=tol, atol=1e-9))
+    ok &= bool(rel_err(mine["ls"], ref["ls"], 1e-12) < tol)
+    ok &= bool(rel_err(mine["ss"], ref["ss"], 1e-12) < tol or (ref["ss"] == 0 and mine["ss"] == 0))
+    return ok
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_bootstrap_sampler_replay(renderers, cfg):
+    """GeneratePathBidir fed the reference's uniform stream reproduces its contributions."""
+    recs = _need(cfg, "bidir")
+    r = renderers(cfg)
+    tapes = [rec["uniforms"] for rec in recs]
+    cnt, tech, ct, _, cons = r.replay(0, tapes)
+    bad = 0
+    for i, rec in enumerate(recs):
+        ref = {(c["camDepth"], c["lightDepth"]): c for c in rec["contribs"]}
+        mine = {(int(tech[i, k, 0]), int(tech[i, k, 1])): ct[i, k] for k in range(cnt[i])}
+        good = cons[i] == rec["consumed"] and set(ref) == set(mine)
+        if good:
+            good = all(_cmp_contrib(mine[k], ref[k]) for k in ref)
+        bad += 0 if good else 1
+    assert bad <= max(1, len(recs) // 50), "%d / %d bootstrap samples differ" % (bad, len(recs))
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_large_step_sampler_replay(renderers, cfg):
+    """GenerateSubpath (multiplexed large step) reproduces path, primary vector and contribution."""
+    recs = _need(cfg, "subpath")
+    r = renderers(cfg)
+    tapes = [rec["uniforms"] for rec in recs]
+    cl = np.array([rec["camLength"] for rec in recs])
+    ll = np.array([rec["lgtLength"] for rec in recs])
+    cnt, tech, ct, pth, cons = r.replay(1, tapes, cl, ll)
+    bad = 0
+    nvalid = 0
+    for i, rec in enumerate(recs):
+        good = cons[i] == rec["consumed"] and cnt[i] == len(rec["contribs"])
+        if good and cnt[i]:
+            nvalid += 1
+            good = _cmp_contrib(ct[i, 0], rec["contribs"][0])
+            exp = path_record(rec["path"], rec["camLength"], rec["lgtLength"], _first_tri(r))
+            L = rec["camLength"] + rec["lgtLength"] - 1
+            nv = (rec["lgtLength"] - 1 if rec["lgtLength"] > 1 else 0) + rec["camLength"] - 1
+            good = good and np.array_equal(pth[i]["tri"][:nv], exp["tri"][:nv])
+            good = good and np.allclose(pth[i]["u"][:2 * L], exp["u"][:2 * L], atol=2e-5)
+            good = good and np.array_equal(pth[i]["disc"][:nv], exp["disc"][:nv])
+        bad += 0 if good else 1
+    assert nvalid > len(recs) // 10
+    assert bad <= max(1, len(recs) // 50), "%d / %d large steps differ" % (bad, len(recs))
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_direct_pass_replay(renderers, cfg):
+    """The direct-lighting GeneratePath (depth <= 2) reproduces the reference's splats."""
+    recs = _need(cfg, "direct")
+    r = renderers(cfg)
+    tapes = [rec["uniforms"] for rec in recs]
+    px = np.array([rec["pixel"][0] for rec in recs])
+    py = np.array([rec["pixel"][1] for rec in recs])
+    cnt, tech, ct, _, cons = r.replay(2, tapes, px, py, max_contribs=8)
+    bad = 0
+    for i, rec in enumerate(recs):
+        good = cons[i] == rec["consumed"] and cnt[i] == len(rec["contribs"])
+        if good:
+            for k, c in enumerate(rec["contribs"]):
+                good = good and (tech[i, k, 0], tech[i, k, 1]) == (c["camDepth"], c["lightDepth"])
+                good = good and np.allclose(ct[i, k]["rgb"], c["contrib"], rtol=1e-4, atol=1e-9)
+        bad += 0 if good else 1
+    assert bad <= max(1, len(recs) // 50), "%d / %d direct samples differ" % (bad, len(recs))
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_small_step_perturbation(renderers, cfg):
+    """PerturbPathBidir: same perturbed primary vector, hit triangles and contribution."""
+    recs = _need(cfg, "tech")
+    r = renderers(cfg)
+    paths, offs, refs = [], [], []
+    for rec in recs:
+        c, l = rec["path"]["camDepth"], rec["path"]["lgtDepth"]
+        base = path_record(rec["path"], c, l, _first_tri(r), rec["pos"])
+        for pt in rec["perturb"]:
+            paths.append(base)
+            o = np.zeros(24, np.float32)
+            o[:rec["dim"]] = pt["offset"]
+            offs.append(o)
+            refs.append((rec, pt))
+    out, ct = r.perturb(np.array(paths), np.array(offs))
+    bad = 0
+    nvalid = 0
+    for i, (rec, pt) in enumerate(refs):
+        dim = rec["dim"]
+        good = np.allclose(out[i]["u"][:dim], pt["ypos"], atol=2e-6)
+        good = good and bool(ct[i]["valid"]) == (len(pt["contribs"]) == 1)
+        if good and ct[i]["valid"]:
+            nvalid += 1
+            good = _cmp_contrib(ct[i], pt["contribs"][0])
+        bad += 0 if good else 1
+    assert nvalid > len(refs) // 4
+    assert bad <= max(1, len(refs) // 50), "%d / %d perturbations differ" % (bad, len(refs))
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_path_derivatives_vs_chad(renderers, cfg):
+    """log f and gradient vs the chad-generated library; Hessian vs the exact Hessian.
+
+    chad's own Hessian is not always the derivative of chad's own gradient (its
+    reverse-over-forward emission loses terms on some paths; the fixture stores
+    central differences of chad's gradient, h = 1e-3, as `fdHess`). The CUDA
+    Hessian is compared with chad's Hessian where chad is self-consistent (chad
+    vs its own differences within 1%), and with the differences everywhere.
+    """
+    recs = [rec for rec in _need(cfg, "tech") if rec["haveDerv"] and not rec["scrubbed"]
+            and rec["contrib"][0]["ss"] > 1e-15]
+    r = renderers(cfg)
+    paths, us = [], []
+    for rec in recs:
+        c, l = rec["path"]["camDepth"], rec["path"]["lgtDepth"]
+        paths.append(path_record(rec["path"], c, l, _first_tri(r), rec["pos"]))
+        u = np.zeros(24, np.float32)
+        u[:rec["dim"]] = rec["pos"]
+        us.append(u)
+    paths = np.array(paths)
+    us = np.array(us)
+    logf = r.path_eval(paths, us)
+    g, h = r.path_grad_hess(paths, us)
+    bad_fg, bad_h_chad, bad_h_fd, n_consistent = [], [], [], 0
+    for i, rec in enumerate(recs):
+        d = rec["dim"]
+        gr = np.array(rec["grad"])
+        hr = np.array(rec["hess"]).reshape(d, d)
+        hfd = np.array(rec["fdHess"]).reshape(d, d)
+        gm = g[i, :d]
+        hm = h[i, :d * d].reshape(d, d)
+        e_f = abs(logf[i] - rec["logf"]) / max(1.0, abs(rec["logf"]))
+        e_g = np.max(np.abs(gm - gr)) / max(np.max(np.abs(gr)), 1e-6)
+        if not (e_f < 1e-4 and e_g < 1e-3):
+            bad_fg.append((i, e_f, e_g))
+        scale = max(np.max(np.abs(hfd)), 1e-6)
+        if np.max(np.abs(hr - hfd)) / scale < 1e-2:
+            n_consistent += 1
+            if np.max(np.abs(hm - hr)) / max(np.max(np.abs(hr)), 1e-6) > 1e-3:
+                bad_h_chad.append(i)
+        if np.linalg.norm(hm - hfd) / max(np.linalg.norm(hfd), 1e-6) > 2e-2:
+            bad_h_fd.append(i)
+    tol = max(1, len(recs) // 50)
+    assert len(bad_fg) <= tol, "f/gradient mismatches: %s" % bad_fg[:5]
+    assert n_consistent >= len(recs) // 2
+    assert len(bad_h_chad) <= tol, "Hessian vs self-consistent chad: %s" % bad_h_chad[:10]
+    assert len(bad_h_fd) <= max(2, len(recs) // 20), "Hessian vs differences of chad's gradient: %s" % bad_h_fd[:10]
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_compute_gaussian_vs_reference(renderers, cfg):
+    """FP64 ComputeGaussian vs the reference's FP32 Eigen result on the same gradient/Hessian."""
+    recs = _need(cfg, "tech")
+    r = renderers(cfg)
+    dims, ss, gs, hs = [], [], [], []
+    for rec in recs:
+        d = rec["dim"]
+        dims.append(d)
+        ss.append(rec["contrib"][0]["ss"])
+        g = np.zeros(24, np.float32)
+        g[:d] = rec["grad"]
+        h = np.zeros(576, np.float32)
+        h[:d * d] = rec["hess"]
+        gs.append(g)
+        hs.append(h)
+    mean, ic, cv, ld = r.compute_gaussian(np.array(dims), np.array(ss), np.array(gs), np.array(hs))
+    worst = []
+    for i, rec in enumerate(recs):
+        d = dims[i]
+        G = rec["gauss"]
+        icr = np.array(G["invCov"]).reshape(d, d).T  # Eigen column-major dump
+        cvr = np.array(G["cov"]).reshape(d, d).T
+        e_ic = np.max(np.abs(ic[i, :d * d].reshape(d, d) - icr)) / np.max(np.abs(icr))
+        e_cv = np.max(np.abs(cv[i, :d * d].reshape(d, d) - cvr)) / np.max(np.abs(cvr))
+        e_m = np.max(np.abs(mean[i, :d] - np.array(G["mean"]))) / max(np.max(np.abs(G["mean"])), 1e-3)
+        e_ld = abs(ld[i] - G["logDet"]) / max(1.0, abs(G["logDet"]))
+        worst.append(max(e_ic, e_cv, e_m, e_ld))
+    worst = np.array(worst)
+    assert np.mean(worst < 1e-3) >= 0.98, "Gaussian mismatch: max %g" % worst.max()
