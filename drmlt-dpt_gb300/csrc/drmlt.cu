@@ -636,3 +636,50 @@ int drmlt_last_run_ms(void *handle, float *ms) {
 }  // extern "C"
 
 #include "parity.cuh"
+
+// ============================================================================ no-allocation entry point
+// Scratch for drmlt_compute_gaussian_noalloc: the FP64 eigen-basis store of up
+// to kNoAllocMaxGaussians Gaussians (kGaussStride doubles each, 1.29 MB). It is
+// a file-scope device array, so every GPU that loads libdrmlt.so holds it until
+// the process exits, and it needs no cudaMalloc.
+namespace {
+constexpr int kNoAllocMaxGaussians = 256;
+__device__ __align__(256) double g_noallocGaussStore[size_t(kNoAllocMaxGaussians) * kGaussStride];
+
+// Device address of g_noallocGaussStore, looked up once per device. In host
+// code the symbol name is only a host-side stand-in, never a device address.
+constexpr int kNoAllocMaxDevices = 64;
+double *g_noallocStorePtr[kNoAllocMaxDevices] = {nullptr};
+}  // namespace
+
+extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const float *ss, const float *grad,
+                                              const float *hess, float sigma, double *mean, double *inv_cov,
+                                              double *cov, double *log_det, void *stream) {
+    if (n < 0) return fail(DRMLT_E_ARG, "n must be non-negative");
+    if (n > kNoAllocMaxGaussians)
+        return fail(DRMLT_E_ARG, "drmlt_compute_gaussian_noalloc: n = " + std::to_string(n) +
+                                     " exceeds the fixed scratch capacity of " +
+                                     std::to_string(kNoAllocMaxGaussians) + " Gaussians per call");
+    if (n == 0) return DRMLT_OK;
+    if (!dims || !ss || !grad || !hess || !mean || !inv_cov || !cov || !log_det)
+        return fail(DRMLT_E_ARG, "null device pointer");
+    if (!(sigma > 0.0f)) return fail(DRMLT_E_ARG, "sigma must be positive");
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(DRMLT_E_ARG, "device ordinal out of range");
+    if (g_noallocStorePtr[dev] == nullptr) {
+        // set-up on this device's first call (the device is current here)
+        double *p = nullptr;
+        CK(cudaGetSymbolAddress((void **)&p, g_noallocGaussStore));
+        g_noallocStorePtr[dev] = p;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // entries past each Gaussian's dimension are zero, as in drmlt_compute_gaussian
+    CK(cudaMemsetAsync(mean, 0, size_t(n) * kMaxDim * sizeof(double), st));
+    CK(cudaMemsetAsync(inv_cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
+    CK(cudaMemsetAsync(cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
+    k_gauss_batch<<<(n + 63) / 64, 64, 0, st>>>(dims, ss, grad, hess, n, sigma, g_noallocStorePtr[dev], mean, inv_cov,
+                                                cov, log_det);
+    CK(cudaGetLastError());
+    return DRMLT_OK;
+}

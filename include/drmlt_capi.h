@@ -226,6 +226,28 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
                            const float *hess, int n, double *mean, double *inv_cov, double *cov,
                            double *log_det);
 
+/* No counterpart in the reference. drmlt_compute_gaussian without any device
+ * allocation, for callers that cannot call cudaMalloc: a host renderer that
+ * hands the library buffers carved from its own pre-allocated device pool, or
+ * code that must not hit cudaMalloc's implicit device-wide synchronisation
+ * while other streams are running. All array arguments are DEVICE pointers the
+ * caller owns (same layouts as drmlt_compute_gaussian; dims/ss/log_det have n
+ * entries, grad/mean DRMLT_MAX_DIM per Gaussian, hess/inv_cov/cov
+ * DRMLT_MAX_DIM^2). sigma is the H2MC prior (perturbstddev). The work is queued
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * returns without synchronising.
+ *
+ * Scratch lives in a fixed library-owned device array sized for 256 Gaussians
+ * (about 1.3 MB, held on every device that loads the library until the process
+ * exits); n > 256 is rejected with DRMLT_E_ARG. The first call on each device
+ * looks the array's device address up (cudaGetSymbolAddress), so make that
+ * first call before any stream capture. Every call shares the one array:
+ * calls that overlap on the GPU (on different streams, or from different host
+ * threads) race on it and must be serialised by the caller. */
+int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const float *ss, const float *grad,
+                                   const float *hess, float sigma, double *mean, double *inv_cov, double *cov,
+                                   double *log_det, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

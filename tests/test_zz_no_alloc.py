@@ -1,0 +1,90 @@
+"""drmlt_compute_gaussian_noalloc: the FP64 H2MC Gaussian for callers that cannot
+allocate device memory (they own every device buffer, e.g. carved from their own
+pool, and the library must not call cudaMalloc behind their back).
+
+The test owns the device buffers (torch tensors), calls the entry point twice in
+a row through the C ABI -- the second call reuses the library's fixed scratch
+array left over from the first -- and checks each result against
+drmlt_compute_gaussian (which allocates its own temporaries) within the
+Gaussian tolerance of the parity tests (1e-3 relative). It also checks that a
+batch larger than the fixed scratch is rejected with DRMLT_E_ARG.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import golden
+
+pytestmark = pytest.mark.gpu
+
+MAX = 24
+TOL = 1e-3  # Gaussian tolerance used by test_gpu_parity
+
+
+def _inputs(recs):
+    n = len(recs)
+    dims = np.array([r["dim"] for r in recs], np.int32)
+    ss = np.array([r["contrib"][0]["ss"] for r in recs], np.float32)
+    grad = np.zeros((n, MAX), np.float32)
+    hess = np.zeros((n, MAX * MAX), np.float32)
+    for i, r in enumerate(recs):
+        d = r["dim"]
+        grad[i, :d] = r["grad"]
+        hess[i, :d * d] = r["hess"]
+    return dims, ss, grad, hess
+
+
+def _noalloc(capi, torch, dims, ss, grad, hess, sigma):
+    dev = torch.device("cuda:0")
+    n = len(dims)
+    t_dims = torch.from_numpy(dims).to(dev)
+    t_ss = torch.from_numpy(ss).to(dev)
+    t_grad = torch.from_numpy(grad).to(dev)
+    t_hess = torch.from_numpy(hess).to(dev)
+    # poison the outputs: the entry point must overwrite every entry
+    t_mean = torch.full((n, MAX), 7.0, dtype=torch.float64, device=dev)
+    t_ic = torch.full((n, MAX * MAX), 7.0, dtype=torch.float64, device=dev)
+    t_cv = torch.full((n, MAX * MAX), 7.0, dtype=torch.float64, device=dev)
+    t_ld = torch.full((n,), 7.0, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rc = capi.lib().drmlt_compute_gaussian_noalloc(
+        n, C.c_void_p(t_dims.data_ptr()), C.c_void_p(t_ss.data_ptr()), C.c_void_p(t_grad.data_ptr()),
+        C.c_void_p(t_hess.data_ptr()), C.c_float(sigma), C.c_void_p(t_mean.data_ptr()),
+        C.c_void_p(t_ic.data_ptr()), C.c_void_p(t_cv.data_ptr()), C.c_void_p(t_ld.data_ptr()), C.c_void_p(stream))
+    capi.check(rc)
+    torch.cuda.synchronize(dev)
+    return t_mean.cpu().numpy(), t_ic.cpu().numpy(), t_cv.cpu().numpy(), t_ld.cpu().numpy()
+
+
+def _close(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.max(np.abs(b)), 1e-12)
+    return np.max(np.abs(a - b)) / scale <= TOL
+
+
+def test_noalloc_gaussian_matches_allocating_entry(renderers):
+    torch = pytest.importorskip("torch")
+    from drmlt import capi
+    recs = golden("cfg1", "tech")
+    assert recs, "golden fixture cfg1_tech missing"
+    r = renderers("cfg1")
+    sigma = r.options.perturb_stddev
+    batches = [recs[:100], recs[100:][::-1]]  # two calls in a row, different contents
+    for batch in batches:
+        dims, ss, grad, hess = _inputs(batch)
+        mean, ic, cv, ld = _noalloc(capi, torch, dims, ss, grad, hess, sigma)
+        rm, ric, rcv, rld = r.compute_gaussian(dims, ss, grad, hess)
+        for i in range(len(batch)):
+            assert _close(mean[i], rm[i]) and _close(ic[i], ric[i]) and _close(cv[i], rcv[i]), i
+            assert abs(ld[i] - rld[i]) <= TOL * max(1.0, abs(rld[i])), i
+
+
+def test_noalloc_rejects_oversized_batch(built_lib):
+    from drmlt import capi
+    null = C.c_void_p(0)
+    rc = capi.lib().drmlt_compute_gaussian_noalloc(257, null, null, null, null, C.c_float(0.01), null, null, null,
+                                                   null, null)
+    assert rc == -1
+    assert b"exceeds" in capi.lib().drmlt_last_error()
