@@ -419,14 +419,14 @@ struct Renderer {
         const RunParams p = params();
         const int nb = (N + 127) / 128;
         const int nbWarp = (N * 32 + 127) / 128;
-        const int nbG = (N + 63) / 64;
+        const int nbG = (N + kGaussWarps - 1) / kGaussWarps;
         k_reset_counters<<<1, 32, 0, stream>>>(cv.counters);
         k_stage1<<<nb, 128, 0, stream>>>(p, iter);
         k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
-        k_gauss<<<nbG, 64, 0, stream>>>(p, 0);
+        k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 0);
         k_stage2<<<nb, 128, 0, stream>>>(p, iter);
         k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
-        k_gauss<<<nbG, 64, 0, stream>>>(p, 2);
+        k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 2);
         k_finish<<<nb, 128, 0, stream>>>(p, iter);
     }
 
@@ -440,7 +440,7 @@ struct Renderer {
         for (int k = 0; k <= kNumStages; k++) CK(cudaEventCreate(&ev[k]));
         for (int k = 0; k < kNumStages; k++) ms[k] = 0.0f;
         long long mutations = 0;
-        const int nb = (N + 127) / 128, nbWarp = (N * 32 + 127) / 128, nbG = (N + 63) / 64;
+        const int nb = (N + 127) / 128, nbWarp = (N * 32 + 127) / 128, nbG = (N + kGaussWarps - 1) / kGaussWarps;
         for (long long it = iterDone; it < end; it++) {
             const RunParams p = params();
             const int iter = int(it);
@@ -450,13 +450,13 @@ struct Renderer {
             cudaEventRecord(ev[1], stream);
             k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
             cudaEventRecord(ev[2], stream);
-            k_gauss<<<nbG, 64, 0, stream>>>(p, 0);
+            k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 0);
             cudaEventRecord(ev[3], stream);
             k_stage2<<<nb, 128, 0, stream>>>(p, iter);
             cudaEventRecord(ev[4], stream);
             k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
             cudaEventRecord(ev[5], stream);
-            k_gauss<<<nbG, 64, 0, stream>>>(p, 2);
+            k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 2);
             cudaEventRecord(ev[6], stream);
             k_finish<<<nb, 128, 0, stream>>>(p, iter);
             cudaEventRecord(ev[7], stream);
@@ -678,7 +678,7 @@ extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const 
     CK(cudaMemsetAsync(mean, 0, size_t(n) * kMaxDim * sizeof(double), st));
     CK(cudaMemsetAsync(inv_cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
     CK(cudaMemsetAsync(cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
-    k_gauss_batch<<<(n + 63) / 64, 64, 0, st>>>(dims, ss, grad, hess, n, sigma, g_noallocStorePtr[dev], mean, inv_cov,
+    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps, 0, st>>>(dims, ss, grad, hess, n, sigma, g_noallocStorePtr[dev], mean, inv_cov,
                                                 cov, log_det);
     CK(cudaGetLastError());
     return DRMLT_OK;

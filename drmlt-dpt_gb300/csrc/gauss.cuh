@@ -59,78 +59,130 @@ DEV void gauss_isotropic(int dim, double sigma, GaussView g) {
     *g.dimv = double(dim);
 }
 
-// Cyclic Jacobi: A (n x n, row-major, symmetric) is destroyed; on return its
-// diagonal holds the eigenvalues and V the eigenvectors (columns).
-DEV void jacobi_eigen(double *A, double *V, int n) {
-    for (int i = 0; i < n; i++)
-        for (int k = 0; k < n; k++) V[i * n + k] = i == k ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 60; sweep++) {
+// Warp-cooperative two-sided Jacobi with round-robin (Brent-Luk) ordering:
+// each round rotates n/2 disjoint index pairs at once, so the 32 lanes of a
+// warp share the row and column updates of one matrix held in shared memory.
+// A (n x n, row-major, symmetric, n even) is destroyed: on return its diagonal
+// holds the eigenvalues and V (row-major) the eigenvectors as columns.
+// cs: 2 * kMaxDim doubles of shared scratch for the rotations of a round.
+DEV int rr_partner(int k, int round, int n, bool second) {
+    // circle method: position 0 is fixed, positions 1..n-1 rotate by `round`
+    const int m = n - 1;
+    auto player = [&](int pos) { return pos == 0 ? 0 : 1 + (pos - 1 + round) % m; };
+    return second ? player(n - 1 - k) : player(k);
+}
+
+DEV void jacobi_eigen_warp(double *A, double *V, double *cs, int n) {
+    const int lane = threadIdx.x & 31;
+    for (int e = lane; e < n * n; e += 32) V[e] = (e / n == e % n) ? 1.0 : 0.0;
+    __syncwarp();
+    const int half = n / 2;
+    for (int sweep = 0; sweep < 30; sweep++) {
         double off = 0.0, diag = 0.0;
-        for (int i = 0; i < n; i++) {
-            diag += A[i * n + i] * A[i * n + i];
-            for (int k = i + 1; k < n; k++) off += A[i * n + k] * A[i * n + k];
+        for (int e = lane; e < n * n; e += 32) {
+            const int i = e / n, k = e % n;
+            if (i == k) diag += A[e] * A[e];
+            else if (k > i) off += A[e] * A[e];
         }
-        if (off <= 1e-30 * diag || off == 0.0) break;
-        for (int p = 0; p < n - 1; p++) {
-            for (int q = p + 1; q < n; q++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            diag += __shfl_xor_sync(0xffffffffu, diag, o);
+        }
+        // stop once the off-diagonal mass is at FP64 round-off of the diagonal
+        if (off <= 1e-26 * diag || off == 0.0) break;
+        for (int round = 0; round < n - 1; round++) {
+            if (lane < half) {
+                int p = rr_partner(lane, round, n, false), q = rr_partner(lane, round, n, true);
+                if (p > q) { const int t = p; p = q; q = t; }
                 const double apq = A[p * n + q];
-                if (apq == 0.0) continue;
-                const double app = A[p * n + p], aqq = A[q * n + q];
-                const double theta = (aqq - app) / (2.0 * apq);
-                const double t = (theta >= 0.0 ? 1.0 : -1.0) / (::fabs(theta) + ::sqrt(theta * theta + 1.0));
-                const double c = 1.0 / ::sqrt(t * t + 1.0);
-                const double s = t * c;
-                for (int k = 0; k < n; k++) {  // rotate columns p, q
-                    const double akp = A[k * n + p], akq = A[k * n + q];
-                    A[k * n + p] = c * akp - s * akq;
-                    A[k * n + q] = s * akp + c * akq;
+                double c = 1.0, s = 0.0;
+                if (apq != 0.0) {
+                    const double theta = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+                    const double t = (theta >= 0.0 ? 1.0 : -1.0) / (::fabs(theta) + ::sqrt(theta * theta + 1.0));
+                    c = 1.0 / ::sqrt(t * t + 1.0);
+                    s = t * c;
                 }
-                for (int k = 0; k < n; k++) {  // rotate rows p, q
-                    const double apk = A[p * n + k], aqk = A[q * n + k];
-                    A[p * n + k] = c * apk - s * aqk;
-                    A[q * n + k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < n; k++) {
-                    const double vkp = V[k * n + p], vkq = V[k * n + q];
-                    V[k * n + p] = c * vkp - s * vkq;
-                    V[k * n + q] = s * vkp + c * vkq;
-                }
+                cs[2 * lane] = c;
+                cs[2 * lane + 1] = s;
             }
+            __syncwarp();
+            // rows p, q of every pair
+            for (int task = lane; task < half * n; task += 32) {
+                const int k = task / n, j = task % n;
+                int p = rr_partner(k, round, n, false), q = rr_partner(k, round, n, true);
+                if (p > q) { const int t = p; p = q; q = t; }
+                const double c = cs[2 * k], s = cs[2 * k + 1];
+                const double apj = A[p * n + j], aqj = A[q * n + j];
+                A[p * n + j] = c * apj - s * aqj;
+                A[q * n + j] = s * apj + c * aqj;
+            }
+            __syncwarp();
+            // columns p, q of every pair, and the eigenvector columns
+            for (int task = lane; task < half * n; task += 32) {
+                const int k = task / n, i = task % n;
+                int p = rr_partner(k, round, n, false), q = rr_partner(k, round, n, true);
+                if (p > q) { const int t = p; p = q; q = t; }
+                const double c = cs[2 * k], s = cs[2 * k + 1];
+                const double aip = A[i * n + p], aiq = A[i * n + q];
+                A[i * n + p] = c * aip - s * aiq;
+                A[i * n + q] = s * aip + c * aiq;
+                const double vip = V[i * n + p], viq = V[i * n + q];
+                V[i * n + p] = c * vip - s * viq;
+                V[i * n + q] = s * vip + c * viq;
+            }
+            __syncwarp();
         }
     }
 }
 
-// grad: D, hess: D x D (row-major). Non-finite derivatives are scrubbed to zero
-// first (drsmallstep.cpp:149-154). `work` holds D*D doubles.
-DEV void compute_gaussian(int dim, const H2mcParam &prm, float ss, const float *grad, const float *hess,
-                          double *work, GaussView g) {
+// ComputeGaussian with one warp: grad (D floats), hess (D x D floats,
+// row-major) in global memory; A, V (kMaxDim^2 doubles each) and cs (2 kMaxDim)
+// in this warp's shared memory. Non-finite derivatives are scrubbed to zero
+// first (drsmallstep.cpp:149-154). All 32 lanes must call it.
+DEV void compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const float *grad, const float *hess,
+                               double *A, double *V, double *cs, GaussView g) {
+    const int lane = threadIdx.x & 31;
     bool finite = true;
-    for (int i = 0; i < dim; i++) finite = finite && isfinite(grad[i]);
-    for (int i = 0; i < dim * dim; i++) finite = finite && isfinite(hess[i]);
+    for (int i = lane; i < dim; i += 32) finite = finite && isfinite(grad[i]);
+    for (int i = lane; i < dim * dim; i += 32) finite = finite && isfinite(hess[i]);
+    finite = __all_sync(0xffffffffu, finite);
     double fro = 0.0;
-    for (int i = 0; i < dim * dim; i++) {
-        const double h = finite ? double(hess[i]) : 0.0;
-        work[i] = h;
+    for (int e = lane; e < dim * dim; e += 32) {
+        const double h = finite ? double(hess[e]) : 0.0;
         fro += h * h;
     }
+    for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
     const double sigma = double(prm.sigma);
+    const double invSigmaSq = 1.0 / (sigma * sigma);
     if (ss <= 1e-15f || ::sqrt(fro) < 0.5 / (sigma * sigma)) {
-        gauss_isotropic(dim, sigma, g);
+        for (int e = lane; e < dim * dim; e += 32) g.V[e] = (e / dim == e % dim) ? 1.0 : 0.0;
+        for (int i = lane; i < dim; i += 32) {
+            g.p[i] = invSigmaSq;
+            g.mean[i] = 0.0;
+        }
+        if (lane == 0) {
+            *g.logDet = double(dim) * ::log(invSigmaSq);
+            *g.dimv = double(dim);
+        }
+        __syncwarp();
         return;
     }
     // symmetrise: the reference maps the row-major Hessian as a column-major
     // matrix and SelfAdjointEigenSolver reads its lower triangle, i.e. the
     // row-major upper triangle
-    for (int i = 0; i < dim; i++)
-        for (int k = i + 1; k < dim; k++) work[k * dim + i] = work[i * dim + k];
-    jacobi_eigen(work, g.V, dim);
-    const double invSigmaSq = 1.0 / (sigma * sigma);
-    double logDet = 0.0;
-    double mt[kMaxDim];
-    for (int k = 0; k < dim; k++) {
-        const double lam = work[k * dim + k];
+    for (int e = lane; e < dim * dim; e += 32) {
+        const int i = e / dim, k = e % dim;
+        A[e] = finite ? double(hess[i <= k ? e : k * dim + i]) : 0.0;
+    }
+    __syncwarp();
+    jacobi_eigen_warp(A, V, cs, dim);
+    // per eigenvalue (lane k): H2MC bounding and the drifted mean's eigen-coordinates
+    double mt = 0.0, logp = 0.0;
+    if (lane < dim) {
+        const int k = lane;
+        const double lam = A[k * dim + k];
         double vg = 0.0;
-        for (int i = 0; i < dim; i++) vg += g.V[i * dim + k] * (finite ? double(grad[i]) : 0.0);
+        for (int i = 0; i < dim; i++) vg += V[i * dim + k] * (finite ? double(grad[i]) : 0.0);
         double eb = ::fabs(lam) > 1e-10 ? 1.0 / ::fabs(lam) : 0.0;
         const double ob = eb * vg;
         double s2, o;
@@ -151,16 +203,23 @@ DEV void compute_gaussian(int dim, const H2mcParam &prm, float ss, const float *
         eb = eb > 1e-10 ? 1.0 / eb : 0.0;
         const double post = eb + invSigmaSq;
         g.p[k] = post;
-        mt[k] = eb / post * o;
-        logDet += ::log(post);
+        mt = eb / post * o;
+        logp = ::log(post);
+        cs[k] = mt;
     }
-    for (int i = 0; i < dim; i++) {
+    for (int o = 16; o > 0; o >>= 1) logp += __shfl_xor_sync(0xffffffffu, logp, o);
+    __syncwarp();
+    for (int e = lane; e < dim * dim; e += 32) g.V[e] = V[e];
+    for (int i = lane; i < dim; i += 32) {
         double m = 0.0;
-        for (int k = 0; k < dim; k++) m += g.V[i * dim + k] * mt[k];
+        for (int k = 0; k < dim; k++) m += V[i * dim + k] * cs[k];
         g.mean[i] = m;
     }
-    *g.logDet = logDet;
-    *g.dimv = double(dim);
+    if (lane == 0) {
+        *g.logDet = logp;
+        *g.dimv = double(dim);
+    }
+    __syncwarp();
 }
 
 // GaussianLogPdf (src/gaussian.cpp:18-26) in FP64.

@@ -274,17 +274,24 @@ __global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
                     p.d.hess + size_t(w) * kMaxDim * kMaxDim);
 }
 
-__global__ void __launch_bounds__(64) k_gauss(RunParams p, int which) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per listed chain; 4 warps per block share nothing but the block.
+constexpr int kGaussWarps = 4;
+constexpr int kGaussSmem = 2 * kMaxDim * kMaxDim + 2 * kMaxDim;  // doubles per warp
+
+__global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int which) {
+    __shared__ double sm[kGaussWarps][kGaussSmem];
+    const int wib = threadIdx.x >> 5;
+    const int w = blockIdx.x * kGaussWarps + wib;
     const int n = p.d.counters[which == 0 ? 0 : 1];
     if (w >= n) return;
     const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
     Slot &st = slot_of(p.d, chain, which);
-    double work[kMaxDim * kMaxDim];
     const int dim = path_dim(st.rec.c, st.rec.l);
-    compute_gaussian(dim, H2mcParam(p.sigma1), st.ss, p.d.grad + size_t(w) * kMaxDim,
-                     p.d.hess + size_t(w) * kMaxDim * kMaxDim, work, GaussView(gauss_of(p.d, chain, which)));
-    st.gaussInit = 1;
+    double *A = sm[wib];
+    compute_gaussian_warp(dim, H2mcParam(p.sigma1), st.ss, p.d.grad + size_t(w) * kMaxDim,
+                          p.d.hess + size_t(w) * kMaxDim * kMaxDim, A, A + kMaxDim * kMaxDim,
+                          A + 2 * kMaxDim * kMaxDim, GaussView(gauss_of(p.d, chain, which)));
+    if ((threadIdx.x & 31) == 0) st.gaussInit = 1;
 }
 
 // ------------------------------------------------------------- stage 2 proposal

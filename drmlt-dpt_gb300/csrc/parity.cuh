@@ -130,29 +130,33 @@ __global__ void k_replay(SceneView s, int mode, const float *tapes, const int *t
     outConsumed[i] = rng.pos;
 }
 
-__global__ void k_gauss_batch(const int *dims, const float *ss, const float *grad, const float *hess, int n,
-                              float sigma, double *store, double *mean, double *invCov, double *cov, double *logDet) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * kGaussWarps) k_gauss_batch(const int *dims, const float *ss, const float *grad,
+                                                                 const float *hess, int n, float sigma, double *store,
+                                                                 double *mean, double *invCov, double *cov,
+                                                                 double *logDet) {
+    __shared__ double sm[kGaussWarps][kGaussSmem];
+    const int wib = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kGaussWarps + wib;
     if (i >= n) return;
     const int dim = dims[i];
-    double work[kMaxDim * kMaxDim];
     GaussView g(store + size_t(i) * kGaussStride);
-    compute_gaussian(dim, H2mcParam(sigma), ss[i], grad + size_t(i) * kMaxDim, hess + size_t(i) * kMaxDim * kMaxDim,
-                     work, g);
-    for (int r = 0; r < dim; r++) {
-        mean[size_t(i) * kMaxDim + r] = g.mean[r];
-        for (int c = 0; c < dim; c++) {
-            double ic = 0.0, cv = 0.0;
-            for (int k = 0; k < dim; k++) {
-                const double vr = g.V[r * dim + k], vc = g.V[c * dim + k];
-                ic += vr * g.p[k] * vc;
-                cv += vr * vc / g.p[k];
-            }
-            invCov[size_t(i) * kMaxDim * kMaxDim + r * dim + c] = ic;
-            cov[size_t(i) * kMaxDim * kMaxDim + r * dim + c] = cv;
+    double *A = sm[wib];
+    compute_gaussian_warp(dim, H2mcParam(sigma), ss[i], grad + size_t(i) * kMaxDim, hess + size_t(i) * kMaxDim * kMaxDim,
+                          A, A + kMaxDim * kMaxDim, A + 2 * kMaxDim * kMaxDim, g);
+    for (int r = lane; r < dim; r += 32) mean[size_t(i) * kMaxDim + r] = g.mean[r];
+    for (int e = lane; e < dim * dim; e += 32) {
+        const int r = e / dim, c = e % dim;
+        double ic = 0.0, cv = 0.0;
+        for (int k = 0; k < dim; k++) {
+            const double vr = g.V[r * dim + k], vc = g.V[c * dim + k];
+            ic += vr * g.p[k] * vc;
+            cv += vr * vc / g.p[k];
         }
+        invCov[size_t(i) * kMaxDim * kMaxDim + r * dim + c] = ic;
+        cov[size_t(i) * kMaxDim * kMaxDim + r * dim + c] = cv;
     }
-    logDet[i] = *g.logDet;
+    if (lane == 0) logDet[i] = *g.logDet;
 }
 
 __global__ void k_trace_rays(SceneView s, const float *org, const float *dir, float tmin, float tmax, int n,
@@ -333,7 +337,7 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
     CK(cudaMemset(dm.p, 0, size_t(n) * kMaxDim * sizeof(double)));
     CK(cudaMemset(dic.p, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double)));
     CK(cudaMemset(dc.p, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double)));
-    k_gauss_batch<<<(n + 63) / 64, 64>>>(dd.p, dss.p, dg.p, dh.p, n, r->opt.perturb_stddev, dstore.p, dm.p, dic.p, dc.p,
+    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps>>>(dd.p, dss.p, dg.p, dh.p, n, r->opt.perturb_stddev, dstore.p, dm.p, dic.p, dc.p,
                                          dl.p);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
