@@ -1,0 +1,162 @@
+"""The oracle (CPU restatement, oracle/oracle.cpp) pinned against the reference's
+own outputs (golden fixtures made by tests/golden/make_golden.py from the
+reference built from its sources). CPU only."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from helpers import REPO, golden, path_record, scene_xml
+
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+CFGS = ["cfg1", "cfg2"]
+
+
+@pytest.fixture(scope="module")
+def oracles(scene_root):
+    import oracle_dr
+    from drmlt import scene as dscene
+    cache = {}
+
+    def get(cfg):
+        if cfg not in cache:
+            cache[cfg] = oracle_dr.Oracle(dscene.load_scene(scene_xml(cfg, scene_root)))
+        return cache[cfg]
+
+    yield get
+    for o in cache.values():
+        o.close()
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_oracle_bootstrap_sampler(oracles, cfg):
+    recs = golden(cfg, "bidir")
+    o = oracles(cfg)
+    cnt, tech, ct, _, cons = o.replay(0, [r["uniforms"] for r in recs])
+    for i, rec in enumerate(recs):
+        ref = {(c["camDepth"], c["lightDepth"]): c for c in rec["contribs"]}
+        mine = {(int(tech[i, k, 0]), int(tech[i, k, 1])): ct[i, k] for k in range(cnt[i])}
+        assert cons[i] == rec["consumed"], i
+        assert set(ref) == set(mine), i
+        for k, c in ref.items():
+            np.testing.assert_allclose(mine[k]["rgb"], c["contrib"], rtol=1e-4, atol=1e-12)
+            np.testing.assert_allclose(mine[k]["ss"], c["ss"], rtol=1e-4, atol=1e-30)
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_oracle_large_step_sampler(oracles, cfg):
+    recs = golden(cfg, "subpath")
+    o = oracles(cfg)
+    cnt, tech, ct, pth, cons = o.replay(1, [r["uniforms"] for r in recs], [r["camLength"] for r in recs],
+                                        [r["lgtLength"] for r in recs])
+    for i, rec in enumerate(recs):
+        assert cons[i] == rec["consumed"] and cnt[i] == len(rec["contribs"]), i
+        if cnt[i]:
+            np.testing.assert_allclose(ct[i, 0]["ls"], rec["contribs"][0]["ls"], rtol=1e-4)
+            exp = path_record(rec["path"], rec["camLength"], rec["lgtLength"], o.scene.shape_first_tri)
+            L = rec["camLength"] + rec["lgtLength"] - 1
+            np.testing.assert_allclose(pth[i]["u"][:2 * L], exp["u"][:2 * L], atol=2e-5)
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_oracle_direct_pass(oracles, cfg):
+    recs = golden(cfg, "direct")
+    o = oracles(cfg)
+    cnt, tech, ct, _, cons = o.replay(2, [r["uniforms"] for r in recs], [r["pixel"][0] for r in recs],
+                                      [r["pixel"][1] for r in recs], 8)
+    for i, rec in enumerate(recs):
+        assert cons[i] == rec["consumed"] and cnt[i] == len(rec["contribs"]), i
+        for k, c in enumerate(rec["contribs"]):
+            np.testing.assert_allclose(ct[i, k]["rgb"], c["contrib"], rtol=1e-4, atol=1e-12)
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_oracle_perturbation(oracles, cfg):
+    recs = golden(cfg, "tech")
+    o = oracles(cfg)
+    paths, offs, refs = [], [], []
+    for rec in recs:
+        base = path_record(rec["path"], rec["path"]["camDepth"], rec["path"]["lgtDepth"], o.scene.shape_first_tri,
+                           rec["pos"])
+        for pt in rec["perturb"]:
+            off = np.zeros(24, np.float32)
+            off[:rec["dim"]] = pt["offset"]
+            paths.append(base)
+            offs.append(off)
+            refs.append((rec, pt))
+    out, ct = o.perturb(np.array(paths), np.array(offs))
+    for i, (rec, pt) in enumerate(refs):
+        np.testing.assert_allclose(out[i]["u"][:rec["dim"]], pt["ypos"], atol=2e-6)
+        assert bool(ct[i]["valid"]) == (len(pt["contribs"]) == 1), i
+        if ct[i]["valid"]:
+            np.testing.assert_allclose(ct[i]["ss"], pt["contribs"][0]["ss"], rtol=1e-4, atol=1e-30)
+
+
+def _deriv_records(cfg, o):
+    recs = [r for r in golden(cfg, "tech") if r["haveDerv"] and not r["scrubbed"] and r["contrib"][0]["ss"] > 1e-15]
+    P = np.array([path_record(r["path"], r["path"]["camDepth"], r["path"]["lgtDepth"], o.scene.shape_first_tri,
+                              r["pos"]) for r in recs])
+    U = np.zeros((len(recs), 24))
+    for i, r in enumerate(recs):
+        U[i, :r["dim"]] = r["pos"]
+    return recs, P, U
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_oracle_derivatives(oracles, cfg):
+    """Forward-over-reverse (FP64 tape) vs chad and vs FP64 central differences (h = 1e-4).
+
+    Gradient vs chad 1e-3 everywhere. Hessian vs chad 1e-3 except technique c = 1,
+    where chad's Hessian is not the derivative of its own gradient. Hessian vs
+    FP64 differences 1e-3 on at least 90% of paths (differences straddling a
+    branch of the path function are not derivatives)."""
+    o = oracles(cfg)
+    recs, P, U = _deriv_records(cfg, o)
+    f, gfd, hfd = o.fd_derivs(P, U, 1e-4)
+    g, h = o.tape_derivs(P, U.astype(np.float32))
+    n_fd_ok = 0
+    for i, r in enumerate(recs):
+        d = r["dim"]
+        assert abs(f[i] - r["logf"]) <= 1e-4 * max(1.0, abs(r["logf"])), i
+        assert np.max(np.abs(g[i, :d] - r["grad"])) <= 1e-3 * np.max(np.abs(r["grad"])), i
+        hr = np.array(r["hess"])
+        if r["path"]["camDepth"] != 1:
+            assert np.max(np.abs(h[i, :d * d] - hr)) <= 1e-3 * np.max(np.abs(hr)), i
+        if np.max(np.abs(h[i, :d * d] - hfd[i, :d * d])) <= 1e-3 * np.max(np.abs(hfd[i, :d * d])):
+            n_fd_ok += 1
+    assert n_fd_ok >= 0.9 * len(recs), (n_fd_ok, len(recs))
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_oracle_gaussian(oracles, cfg):
+    recs = golden(cfg, "tech")
+    o = oracles(cfg)
+    n = len(recs)
+    dims = np.array([r["dim"] for r in recs])
+    ss = np.array([r["contrib"][0]["ss"] for r in recs], np.float32)
+    G = np.zeros((n, 24), np.float32)
+    H = np.zeros((n, 576), np.float32)
+    for i, r in enumerate(recs):
+        G[i, :r["dim"]] = r["grad"]
+        H[i, :r["dim"] ** 2] = r["hess"]
+    mean, ic, cv, ld = o.compute_gaussian(dims, ss, G, H)
+    ok = 0
+    for i, r in enumerate(recs):
+        d = r["dim"]
+        icr = np.array(r["gauss"]["invCov"]).reshape(d, d).T
+        e = np.max(np.abs(ic[i, :d * d].reshape(d, d) - icr)) / np.max(np.abs(icr))
+        ok += e < 1e-3 and abs(ld[i] - r["gauss"]["logDet"]) <= 1e-3 * max(1.0, abs(r["gauss"]["logDet"]))
+    assert ok >= 0.98 * n
+
+
+def test_oracle_dr_loop_runs(oracles):
+    """A short CPU chain loop: finite film, counters consistent with the reference's loop."""
+    o = oracles("cfg1")
+    r = o.dr_run(num_chains=64, iterations=20, threads=2, num_init=2000)
+    st = r["stats"]
+    assert r["mutations"] == 64 * 20 == st[8]
+    assert st[0] + st[2] == st[8]            # every iteration is a large step or a stage-1 small step
+    assert st[4] + st[6] <= st[2] - st[3]    # second stages only after rejected small steps
+    assert np.isfinite(r["film"]).all() and r["film"].sum() > 0
