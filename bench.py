@@ -157,12 +157,13 @@ def run_ours(args, world, rank, local):
         done_all = done
     value = done_all / (dev_ms * 1e-3)
 
-    # ---- end to end through the C ABI: host scene -> film on the host
+    # ---- end to end through the C ABI: host scene -> film on the host (scene
+    # upload, bootstrap prepass, K steps, film readback; the direct-lighting pass
+    # is not part of the mutation metric and is left out on both arms)
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     r2 = Renderer(sd, device=local, seed=seed + 1)
-    r2.direct()
     r2.prepass()
     e_done = r2.run(args.steps)
     film = r2.film()
@@ -242,7 +243,7 @@ def run_reference(args, world, rank):
         import oracle_dr
     except Exception as e:
         return {"impl": "reference", "unavailable": "oracle CPU port not built: %s" % e}
-    per = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    per = min(15.0, max(0.25, 90.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         oracle_dr.cpu_throughput(xml, seconds=per)
     vals = [oracle_dr.cpu_throughput(xml, seconds=per) for _ in range(args.steps)]

@@ -163,13 +163,13 @@ def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int =
     return path
 
 
-def config1(outdir: str) -> str:
+def config1(outdir: str, spp: int = 64) -> str:
     """Plain DRMLT (green) on the 256x256 Lambertian Cornell box, max depth 5, 4096 chains."""
     return write_cornell(outdir, seed=1, width=256, height=256, phong=False,
-                         options=SceneOptions(maxdepth=5, numchains=4096, spp=64, type="green"))
+                         options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type="green"))
 
 
-def config2(outdir: str, dr_type: str = "mira") -> str:
+def config2(outdir: str, dr_type: str = "mira", spp: int = 64) -> str:
     """H2MC second stage on the Phong Cornell box at 1024x1024, max depth 8, 16384 chains."""
     return write_cornell(outdir, seed=2, width=1024, height=1024, phong=True,
-                         options=SceneOptions(maxdepth=8, numchains=16384, spp=64, type=dr_type))
+                         options=SceneOptions(maxdepth=8, numchains=16384, spp=spp, type=dr_type))

@@ -39,6 +39,7 @@ def lib():
         l.ora_fd_derivs.argtypes = [V, V, V, C.c_int, C.c_double, V, V, V]
         l.ora_tape_derivs.argtypes = [V, V, V, C.c_int, V, V]
         l.ora_compute_gaussian.argtypes = [V, V, V, V, C.c_int, C.c_float, V, V, V, V]
+        l.ora_trace_rays.argtypes = [V, V, V, C.c_float, C.c_float, C.c_int, C.c_int, V, V]
         l.ora_dr_run.restype = C.c_longlong
         l.ora_dr_run.argtypes = [V, C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_int, C.c_uint64, V, V, V, V]
         _lib = l
@@ -162,6 +163,15 @@ class Oracle:
         lib().ora_compute_gaussian(_p(dims), _p(ss), _p(grad), _p(hess), n, self.options.perturb_stddev, _p(mean),
                                    _p(ic), _p(cv), _p(ld))
         return mean, ic, cv, ld
+
+    def trace_rays(self, org, dirs, tmin=1e-3, tmax=float("inf"), any_hit=False):
+        org = np.ascontiguousarray(org, np.float32).reshape(-1, 3)
+        dirs = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        n = len(org)
+        tri = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        lib().ora_trace_rays(self.h, _p(org), _p(dirs), tmin, tmax, n, int(any_hit), _p(tri), _p(t))
+        return tri, t
 
     def dr_run(self, num_chains, iterations, seconds=0.0, threads=None, num_init=None, seed=0x1234):
         threads = threads or os.cpu_count() or 1

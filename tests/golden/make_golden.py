@@ -10,14 +10,19 @@ synthetic Cornell-box scenes of drmlt/scenegen.py and writes gzipped JSON lines:
   <cfg>_direct.jsonl.gz   GeneratePath direct-lighting pass: stream + pixel -> contributions
   <cfg>_tech.jsonl.gz     technique paths with chad log f, gradient, Hessian,
                           ComputeGaussian output and PerturbPathBidir results
+  <cfg>_render*.json.gz   a full `dpt -d` render of the scene (the reference's
+                          DRIntegrator::Render): its printed acceptance counters
+                          and the final image averaged over 16 x 16 blocks
 
 usage (in a container that has the reference at /root/reference):
-  python tests/golden/make_golden.py [cfg1] [cfg2]
+  python tests/golden/make_golden.py [--render] [cfg1] [cfg2]   (--render: only the renders)
 """
 from __future__ import annotations
 
 import gzip
+import json
 import os
+import re
 import shutil
 import subprocess
 import sys
@@ -31,12 +36,65 @@ from drmlt import scenegen  # noqa: E402
 
 REF_DIR = os.path.join(REPO, "oracle", "_ref", "single")
 HARNESS = os.path.join(REF_DIR, "ref_harness")
+DPT = os.path.join(REF_DIR, "dpt")
 
 CONFIGS = {
     # name: (scene writer, derivative depth, counts)
     "cfg1": (scenegen.config1, 5, dict(bidir=200, subpath=300, direct=200, tech=150, perturb=6)),
     "cfg2": (lambda d: scenegen.config2(d, "green"), 8, dict(bidir=100, subpath=200, direct=100, tech=100, perturb=6)),
 }
+
+# full renders: (output suffix, scene writer with the render's spp, derivative depth)
+RENDERS = {
+    "cfg1": [("render", lambda d: scenegen.config1(d, spp=16), 5)],
+    "cfg2": [("render_mira", lambda d: scenegen.config2(d, "mira", spp=1), 8),
+             ("render_green", lambda d: scenegen.config2(d, "green", spp=1), 8)],
+}
+
+
+def read_pfm(path):
+    import numpy as np
+    with open(path, "rb") as f:
+        magic = f.readline().strip()
+        w, h = map(int, f.readline().split())
+        scale = float(f.readline())
+        ch = 3 if magic == b"PF" else 1
+        data = np.frombuffer(f.read(), "<f4" if scale < 0 else ">f4").reshape(h, w, ch)
+    return data[::-1].astype(np.float64)
+
+
+def _stats(log: str) -> dict:
+    """The last 'Rendering Statistics' block. delayed.cpp:312-320 prints the
+    H2MC ratio under the 'isotropic' label and vice versa; undone here."""
+    block = log[log.rindex("Rendering Statistics"):]
+    vals = re.findall(r":\s*([-0-9.e]+)\s*\((\d+)\)", block)
+    (rl, nl), (r1, n1), (rh, nh), (ri, ni) = [(float(a), int(b)) for a, b in vals[:4]]
+    return dict(large=[rl, nl], stage1=[r1, n1], stage2_h2mc=[rh, nh], stage2_iso=[ri, ni])
+
+
+def render(cfg: str, blocks: int = 16):
+    import numpy as np
+    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
+    for name, writer, depth in RENDERS[cfg]:
+        tmp = tempfile.mkdtemp()
+        try:
+            xml = writer(os.path.join(tmp, "scene"))
+            wd = os.path.dirname(xml)
+            shutil.copy(os.path.join(REF_DIR, "lib_d%d" % depth, "pathlibbidir.so"), wd)
+            out = subprocess.run([DPT, os.path.basename(xml), "-d", "--z", "--p=8", "--max-derivatives-depth=%d" % depth],
+                                 cwd=wd, check=True, capture_output=True, text=True).stdout
+            img = read_pfm(os.path.join(wd, "image.pfm"))
+            H, W, _ = img.shape
+            blk = img.reshape(blocks, H // blocks, blocks, W // blocks, 3).mean(axis=(1, 3))
+            rec = dict(stats=_stats(out), mean=img.mean(axis=(0, 1)).tolist(), blocks=blk.round(8).tolist(),
+                       width=W, height=H)
+            dst = os.path.join(HERE, "%s_%s.json.gz" % (cfg, name))
+            with open(dst, "wb") as raw:
+                with gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as g:
+                    g.write(json.dumps(rec).encode())
+            print(dst, rec["stats"], rec["mean"])
+        finally:
+            shutil.rmtree(tmp)
 
 
 def run(cfg: str):
@@ -63,5 +121,9 @@ def run(cfg: str):
 
 
 if __name__ == "__main__":
-    for c in (sys.argv[1:] or ["cfg1"]):
-        run(c)
+    args = sys.argv[1:]
+    only_render = "--render" in args
+    for c in [a for a in args if not a.startswith("--")] or ["cfg1"]:
+        if not only_render:
+            run(c)
+        render(c)

@@ -1,0 +1,192 @@
+"""CUDA path vs the oracle (oracle/oracle.cpp, itself pinned to the reference by
+test_oracle.py) on seeded random inputs, at sizes beyond the golden fixtures.
+
+All CUDA calls go through libdrmlt.so's C ABI. Bars: contributions relative
+1e-4; log f relative 1e-4 of the FP64 oracle; gradient and Hessian 1e-3 of the
+largest entry against the oracle's FP64 forward-over-reverse derivatives;
+ComputeGaussian (FP64 on both sides) 1e-6; ray hits: same triangle on at least
+99.99% of rays. The CUDA side computes in FP32 with fused multiply-adds, so a
+path whose ray grazes a triangle edge can branch differently; each test bounds
+that fraction explicitly.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from helpers import REPO, scene_xml
+
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+pytestmark = pytest.mark.gpu
+
+CFGS = ["cfg1", "cfg2"]
+MAX_DEPTH = {"cfg1": 5, "cfg2": 8}
+
+
+@pytest.fixture(scope="module")
+def oracles(scene_root):
+    import oracle_dr
+    from drmlt import scene as dscene
+    cache = {}
+
+    def get(cfg):
+        if cfg not in cache:
+            cache[cfg] = oracle_dr.Oracle(dscene.load_scene(scene_xml(cfg, scene_root)))
+        return cache[cfg]
+
+    yield get
+    for o in cache.values():
+        o.close()
+
+
+def _random_large_steps(cfg, n, seed):
+    """n seeded uniform streams with techniques drawn like the multiplexed large step."""
+    rng = np.random.default_rng(seed)
+    L = rng.integers(3, MAX_DEPTH[cfg] + 1, n)
+    cam = np.array([rng.integers(1, l + 2) for l in L], np.int32)
+    lgt = (L + 1 - cam).astype(np.int32)
+    tapes = rng.random((n, 64), dtype=np.float32)
+    tapes = np.minimum(tapes, np.float32(1.0 - 2 ** -24))
+    return tapes, cam, lgt
+
+
+_CACHE = {}
+
+
+def _valid_paths(cfg, renderers, oracles, n=4096):
+    """Random large-step paths traced by both sides; returns the ones both found valid and equal."""
+    if cfg in _CACHE:
+        return _CACHE[cfg]
+    tapes, cam, lgt = _random_large_steps(cfg, n, 17)
+    r, o = renderers(cfg), oracles(cfg)
+    cg, tg, ctg, pg, sg = r.replay(1, list(tapes), cam, lgt)
+    co, to, cto, po, so = o.replay(1, list(tapes), cam, lgt)
+    same = (cg == co) & (sg == so)
+    keep = np.nonzero(same & (cg == 1))[0]
+    _CACHE[cfg] = (tapes, cam, lgt, (cg, ctg, pg, sg), (co, cto, po, so), keep)
+    return _CACHE[cfg]
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_random_large_steps_vs_oracle(renderers, oracles, cfg):
+    tapes, cam, lgt, g, o, keep = _valid_paths(cfg, renderers, oracles)
+    cg, ctg, pg, sg = g
+    co, cto, po, so = o
+    n = len(tapes)
+    bad = int(np.sum((cg != co) | (sg != so)))
+    assert len(keep) > n // 20
+    for i in keep:
+        d = 2 * (pg[i]["c"] + pg[i]["l"] - 1)
+        nv = pg[i]["c"] + pg[i]["l"] - 2
+        ok = (pg[i]["c"], pg[i]["l"], pg[i]["lgt_light"], pg[i]["lgt_prim"], pg[i]["dl_light"], pg[i]["dl_prim"],
+              pg[i]["use_abs"]) == (po[i]["c"], po[i]["l"], po[i]["lgt_light"], po[i]["lgt_prim"], po[i]["dl_light"],
+                                    po[i]["dl_prim"], po[i]["use_abs"])
+        ok &= np.array_equal(pg[i]["tri"][:nv], po[i]["tri"][:nv])
+        ok &= np.allclose(pg[i]["u"][:d], po[i]["u"][:d], atol=1e-5, rtol=0)
+        a, b = ctg[i, 0], cto[i, 0]
+        ok &= np.allclose(a["rgb"], b["rgb"], rtol=1e-4, atol=1e-12) and abs(a["ss"] - b["ss"]) <= 1e-4 * abs(b["ss"])
+        ok &= np.allclose(a["screen"], b["screen"], atol=2e-5, rtol=0)
+        bad += 0 if ok else 1
+    assert bad <= n // 200, "%d / %d large steps differ" % (bad, n)
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_random_perturbations_vs_oracle(renderers, oracles, cfg):
+    """PerturbPathBidir on random valid paths with N(0, sigma) offsets, sigma in {0.01, 0.0025, 0.05}."""
+    tapes, cam, lgt, g, o, keep = _valid_paths(cfg, renderers, oracles)
+    paths = g[2][keep]
+    rng = np.random.default_rng(23)
+    sig = rng.choice([0.01, 0.0025, 0.05], len(paths)).astype(np.float32)
+    off = (rng.standard_normal((len(paths), 24)) * sig[:, None]).astype(np.float32)
+    og, cg = renderers(cfg).perturb(paths, off)
+    oo, co = oracles(cfg).perturb(paths, off)
+    bad = 0
+    for i in range(len(paths)):
+        d = 2 * (paths[i]["c"] + paths[i]["l"] - 1)
+        ok = bool(cg[i]["valid"]) == bool(co[i]["valid"]) and np.allclose(og[i]["u"][:d], oo[i]["u"][:d], atol=1e-6)
+        if ok and co[i]["valid"]:
+            ok = abs(cg[i]["ss"] - co[i]["ss"]) <= 1e-4 * abs(co[i]["ss"]) and np.allclose(
+                cg[i]["rgb"], co[i]["rgb"], rtol=1e-4, atol=1e-12)
+        bad += 0 if ok else 1
+    assert bad <= max(2, len(paths) // 200), "%d / %d perturbations differ" % (bad, len(paths))
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_random_derivatives_vs_fp64_oracle(renderers, oracles, cfg):
+    """log f, gradient and Hessian (CUDA, FP32 hyper-dual) vs the oracle's FP64
+    forward-over-reverse derivatives of the same path function, every technique."""
+    tapes, cam, lgt, g, o, keep = _valid_paths(cfg, renderers, oracles)
+    paths = g[2][keep]
+    ss = g[1][keep, 0]["ss"]
+    sel = np.nonzero(ss > 1e-15)[0]
+    paths = paths[sel]
+    u = np.zeros((len(paths), 24), np.float32)
+    for i in range(len(paths)):
+        u[i] = paths[i]["u"]
+    r, ora = renderers(cfg), oracles(cfg)
+    logf = r.path_eval(paths, u)
+    gg, hg = r.path_grad_hess(paths, u)
+    f64, _, _ = ora.fd_derivs(paths, u.astype(np.float64), 1e-4)
+    go, ho = ora.tape_derivs(paths, u)
+    bad_f, bad_g, bad_h = [], [], []
+    for i in range(len(paths)):
+        d = 2 * (paths[i]["c"] + paths[i]["l"] - 1)
+        if not np.isfinite(f64[i]):
+            continue
+        if abs(logf[i] - f64[i]) > 1e-4 * max(1.0, abs(f64[i])):
+            bad_f.append(i)
+        if np.max(np.abs(gg[i, :d] - go[i, :d])) > 1e-3 * max(np.max(np.abs(go[i, :d])), 1e-6):
+            bad_g.append(i)
+        if np.max(np.abs(hg[i, :d * d] - ho[i, :d * d])) > 1e-3 * max(np.max(np.abs(ho[i, :d * d])), 1e-6):
+            bad_h.append(i)
+    n = len(paths)
+    assert n > 100
+    tol = max(2, n // 100)
+    assert len(bad_f) <= tol, "log f: %d / %d" % (len(bad_f), n)
+    assert len(bad_g) <= tol, "gradient: %d / %d" % (len(bad_g), n)
+    assert len(bad_h) <= tol, "Hessian: %d / %d" % (len(bad_h), n)
+
+
+@pytest.mark.parametrize("cfg", CFGS)
+def test_random_gaussians_vs_fp64_oracle(renderers, oracles, cfg):
+    """ComputeGaussian on the GPU (warp Jacobi, FP64) vs the oracle's sequential FP64 Jacobi."""
+    tapes, cam, lgt, g, o, keep = _valid_paths(cfg, renderers, oracles)
+    paths = g[2][keep]
+    ss = g[1][keep, 0]["ss"].astype(np.float32)
+    u = np.stack([p["u"] for p in paths]).astype(np.float32)
+    grad, hess = oracles(cfg).tape_derivs(paths, u)
+    dims = np.array([2 * (p["c"] + p["l"] - 1) for p in paths], np.int32)
+    mg, icg, cvg, ldg = renderers(cfg).compute_gaussian(dims, ss, grad, hess)
+    mo, ico, cvo, ldo = oracles(cfg).compute_gaussian(dims, ss, grad, hess)
+    worst = []
+    for i in range(len(paths)):
+        d = dims[i]
+        e = [np.max(np.abs(icg[i, :d * d] - ico[i, :d * d])) / max(np.max(np.abs(ico[i, :d * d])), 1e-300),
+             np.max(np.abs(cvg[i, :d * d] - cvo[i, :d * d])) / max(np.max(np.abs(cvo[i, :d * d])), 1e-300),
+             np.max(np.abs(mg[i, :d] - mo[i, :d])) / max(np.max(np.abs(mo[i, :d])), 1e-3),
+             abs(ldg[i] - ldo[i]) / max(1.0, abs(ldo[i]))]
+        worst.append(max(e))
+    worst = np.array(worst)
+    assert np.mean(worst < 1e-6) >= 0.995, "max %g" % worst.max()
+
+
+@pytest.mark.parametrize("cfg", ["cfg1"])
+def test_ray_hits_vs_oracle(renderers, oracles, cfg):
+    """Closest-hit and occlusion casts through the BVH vs brute force over all triangles."""
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    org = (rng.random((n, 3)) * 1.96 - 0.98).astype(np.float32)
+    d = rng.standard_normal((n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    r, o = renderers(cfg), oracles(cfg)
+    tg, thg = r.trace_rays(org, d)
+    to, tho = o.trace_rays(org, d)
+    agree = np.mean(tg == to)
+    assert agree >= 0.9999, agree
+    both = (tg == to) & (tg >= 0)
+    assert np.allclose(thg[both], tho[both], rtol=1e-5, atol=1e-6)
+    og, _ = r.trace_rays(org, d, tmax=1.0, any_hit=True)
+    oo, _ = o.trace_rays(org, d, tmax=1.0, any_hit=True)
+    assert np.mean((og >= 0) == (oo >= 0)) >= 0.9999

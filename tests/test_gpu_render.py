@@ -1,0 +1,65 @@
+"""Whole renders on the GPU vs full renders of the reference (`dpt -d`, fixtures
+<cfg>_render*.json.gz made by tests/golden/make_golden.py): same scene, same
+options, same number of mutations, different random streams, so the checks are
+statistical.
+
+Bars. Acceptance ratios: within 0.006 (large step, stage 1) and 0.012 (second
+stages) of the reference's -- two `dpt` runs of the 16-spp Cornell box with
+different seeds differ by up to 0.0035 on the second stages. The H2MC ratio of
+the mira run gets 0.015: the reference's chad Hessian is not the exact Hessian
+for light-tracing techniques (camDepth = 1), while this build's is. Image:
+per-channel mean within 2%, 8 x 8 block means within 6% on average."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+RENDERS = [("cfg1", "render", "green"), ("cfg2", "render_mira", "mira"), ("cfg2", "render_green", "green")]
+
+
+def _fixture(cfg, name):
+    import gzip
+    import json
+    p = os.path.join(GOLDEN, "%s_%s.json.gz" % (cfg, name))
+    with gzip.open(p, "rt") as f:
+        return json.load(f)
+
+
+def _scene(cfg, dr_type, root):
+    from drmlt import scenegen
+    d = os.path.join(root, "%s_%s_render" % (cfg, dr_type))
+    if cfg == "cfg1":
+        return scenegen.config1(d, spp=16)
+    return scenegen.config2(d, dr_type, spp=1)
+
+
+@pytest.mark.parametrize("cfg,name,dr_type", RENDERS)
+def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_type):
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    ref = _fixture(cfg, name)
+    sd = dscene.load_scene(_scene(cfg, dr_type, scene_root))
+    with Renderer(sd) as r:
+        r.render()
+        img = r.film().astype(np.float64)
+        st = r.stats()
+    assert st["mutations"] == sd.options.spp * sd.width * sd.height
+    mine = dict(large=st["large_step_accepted"] / st["large_step"],
+                stage1=st["stage1_accepted"] / st["stage1"],
+                stage2_iso=st["stage2_iso_accepted"] / st["stage2_iso"],
+                stage2_h2mc=st["stage2_h2mc_accepted"] / st["stage2_h2mc"])
+    tol = dict(large=0.006, stage1=0.006, stage2_iso=0.012, stage2_h2mc=0.015 if dr_type == "mira" else 0.012)
+    for k, t in tol.items():
+        assert abs(mine[k] - ref["stats"][k][0]) <= t, (k, mine[k], ref["stats"][k][0])
+    mean = img.mean(axis=(0, 1))
+    np.testing.assert_allclose(mean, ref["mean"], rtol=0.02)
+    blk = np.array(ref["blocks"])
+    rb = blk.reshape(8, 2, 8, 2, 3).mean(axis=(1, 3))
+    H, W, _ = img.shape
+    mb = img.reshape(8, H // 8, 8, W // 8, 3).mean(axis=(1, 3))
+    rel = np.abs(mb - rb) / np.maximum(rb, 1e-3)
+    assert rel.mean() < 0.06, rel.mean()
