@@ -214,6 +214,7 @@ def run_ours(args, world, rank, local):
             "wall_s_timed_region": wall,
             "acceptance": {k: stats[k + "_accepted"] / max(1, stats[k])
                            for k in ("large_step", "stage1", "stage2_iso", "stage2_h2mc")},
+            "gaussians": {"anisotropic": stats["gaussians"], "fp64_jacobi_fallback": stats["gaussians_fp64_fallback"]},
         }
     if world > 1:
         torch.distributed.destroy_process_group()

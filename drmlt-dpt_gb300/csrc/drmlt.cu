@@ -36,6 +36,10 @@ int dalloc(T **p, size_t n) {
     return DRMLT_OK;
 }
 
+// Lets the Gaussian kernels take their dynamic shared scratch (up to
+// gauss_smem_bytes(kMaxDim), above the 48 KB default) on the current device.
+int gauss_kernels_setup();
+
 template <class T>
 int upload(T **p, const T *src, size_t n) {
     int rc = dalloc(p, n);
@@ -113,6 +117,7 @@ struct Renderer {
         p.uniformMix = opt.uniform_mixing_prob;
         p.accMap = opt.acceptance_map;
         p.maxDerv = opt.max_derivative_depth;
+        p.gaussDim = std::min(2 * opt.max_depth, kMaxDim);
         p.seed = opt.seed;
         return p;
     }
@@ -128,6 +133,7 @@ struct Renderer {
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
             return fail(DRMLT_E_CUDA, "no CUDA device available");
         CK(cudaSetDevice(opt.device));
+        if (int rc = gauss_kernels_setup()) return rc;
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         CK(cudaEventCreate(&ev0));
         CK(cudaEventCreate(&ev1));
@@ -423,10 +429,11 @@ struct Renderer {
         k_reset_counters<<<1, 32, 0, stream>>>(cv.counters);
         k_stage1<<<nb, 128, 0, stream>>>(p, iter);
         k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
-        k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 0);
+        const size_t gsm = gauss_smem_bytes(p.gaussDim);
+        k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 0);
         k_stage2<<<nb, 128, 0, stream>>>(p, iter);
         k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
-        k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 2);
+        k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 2);
         k_finish<<<nb, 128, 0, stream>>>(p, iter);
     }
 
@@ -450,13 +457,14 @@ struct Renderer {
             cudaEventRecord(ev[1], stream);
             k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
             cudaEventRecord(ev[2], stream);
-            k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 0);
+            const size_t gsm = gauss_smem_bytes(p.gaussDim);
+            k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 0);
             cudaEventRecord(ev[3], stream);
             k_stage2<<<nb, 128, 0, stream>>>(p, iter);
             cudaEventRecord(ev[4], stream);
             k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
             cudaEventRecord(ev[5], stream);
-            k_gauss<<<nbG, 32 * kGaussWarps, 0, stream>>>(p, 2);
+            k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 2);
             cudaEventRecord(ev[6], stream);
             k_finish<<<nb, 128, 0, stream>>>(p, iter);
             cudaEventRecord(ev[7], stream);
@@ -610,6 +618,8 @@ int drmlt_get_stats(void *handle, drmlt_stats *st) {
     st->stage2_h2mc = h[kStatH2mc];
     st->stage2_h2mc_accepted = h[kStatH2mcAcc];
     st->mutations = h[kStatMutations];
+    st->gaussians = h[kStatGauss];
+    st->gaussians_fp64_fallback = h[kStatGaussFallback];
     return DRMLT_OK;
 }
 
@@ -636,6 +646,15 @@ int drmlt_last_run_ms(void *handle, float *ms) {
 }  // extern "C"
 
 #include "parity.cuh"
+
+namespace {
+int gauss_kernels_setup() {
+    const int bytes = int(gauss_smem_bytes(kMaxDim));
+    CK(cudaFuncSetAttribute(k_gauss, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    CK(cudaFuncSetAttribute(k_gauss_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return DRMLT_OK;
+}
+}  // namespace
 
 // ============================================================================ no-allocation entry point
 // Scratch for drmlt_compute_gaussian_noalloc: the FP64 eigen-basis store of up
@@ -669,6 +688,8 @@ extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const 
     if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(DRMLT_E_ARG, "device ordinal out of range");
     if (g_noallocStorePtr[dev] == nullptr) {
         // set-up on this device's first call (the device is current here)
+        int rc = gauss_kernels_setup();
+        if (rc) return rc;
         double *p = nullptr;
         CK(cudaGetSymbolAddress((void **)&p, g_noallocGaussStore));
         g_noallocStorePtr[dev] = p;
@@ -678,8 +699,10 @@ extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const 
     CK(cudaMemsetAsync(mean, 0, size_t(n) * kMaxDim * sizeof(double), st));
     CK(cudaMemsetAsync(inv_cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
     CK(cudaMemsetAsync(cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
-    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps, 0, st>>>(dims, ss, grad, hess, n, sigma, g_noallocStorePtr[dev], mean, inv_cov,
-                                                cov, log_det);
+    // dims are device data here: scratch is sized for kMaxDim, and an odd or
+    // out-of-range dimension yields zero outputs and a NaN log-determinant
+    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps, gauss_smem_bytes(kMaxDim), st>>>(
+        dims, ss, grad, hess, n, sigma, kMaxDim, g_noallocStorePtr[dev], mean, inv_cov, cov, log_det);
     CK(cudaGetLastError());
     return DRMLT_OK;
 }

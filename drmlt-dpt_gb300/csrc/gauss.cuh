@@ -7,10 +7,10 @@
 // GenerateSample (src/gaussian.cpp:4-47).
 //
 // A Gaussian is stored as its precision eigen-basis: invCov = V diag(p) V^T,
-// covL = V diag(p^-1/2), mean, logDet = sum log p. The eigen-decomposition is a
-// cyclic Jacobi sweep in FP64 (any symmetric eigensolver gives the same
-// invCov, mean and covariance; only the column order/sign of covL differ,
-// which leaves the sampled distribution unchanged).
+// covL = V diag(p^-1/2), mean, logDet = sum log p. The eigen-decomposition is
+// FP32 cyclic Jacobi refined to FP64 accuracy (any symmetric eigensolver gives
+// the same invCov, mean and covariance; only the column order/sign of covL
+// differ, which leaves the sampled distribution unchanged).
 #pragma once
 #include "common.cuh"
 
@@ -59,89 +59,258 @@ DEV void gauss_isotropic(int dim, double sigma, GaussView g) {
     *g.dimv = double(dim);
 }
 
-// Warp-cooperative two-sided Jacobi with round-robin (Brent-Luk) ordering:
-// each round rotates n/2 disjoint index pairs at once, so the 32 lanes of a
-// warp share the row and column updates of one matrix held in shared memory.
-// A (n x n, row-major, symmetric, n even) is destroyed: on return its diagonal
-// holds the eigenvalues and V (row-major) the eigenvectors as columns.
-// cs: 2 * kMaxDim doubles of shared scratch for the rotations of a round.
-DEV int rr_partner(int k, int round, int n, bool second) {
-    // circle method: position 0 is fixed, positions 1..n-1 rotate by `round`
-    const int m = n - 1;
-    auto player = [&](int pos) { return pos == 0 ? 0 : 1 + (pos - 1 + round) % m; };
-    return second ? player(n - 1 - k) : player(k);
+// Shared-memory scratch of one warp for a Gaussian of dimension <= m. Matrices
+// are row-major with a padded row stride ld = m + 1, so a warp walking down a
+// column hits distinct banks.
+struct GaussSmem {
+    int m, ld;
+    double *A64;   // m x ld: the symmetrised Hessian (destroyed by the FP64 fallback)
+    double *X;     // m x ld: eigenvectors (columns) in FP64
+    double *lam;   // m: eigenvalues in FP64
+    double *cs64;  // 2m: rotations of the FP64 fallback
+    float *A32;    // m x ld: FP32 Jacobi working matrix, then the residual Z, then X E
+    float *V32;    // m x ld: FP32 eigenvectors
+    float *R32;    // m x ld: I - X^T X
+    float *T32;    // m x ld: X^T Z, then the correction E
+    float *l32;    // m: FP32 eigenvalues
+    float *cs32;   // 2m
+    int *pq;       // 2m
+    DEV GaussSmem(double *base, int maxDim) {
+        m = maxDim;
+        ld = maxDim + 1;
+        A64 = base;
+        X = A64 + m * ld;
+        lam = X + m * ld;
+        cs64 = lam + m;
+        A32 = reinterpret_cast<float *>(cs64 + 2 * m);
+        V32 = A32 + m * ld;
+        R32 = V32 + m * ld;
+        T32 = R32 + m * ld;
+        l32 = T32 + m * ld;
+        cs32 = l32 + m;
+        pq = reinterpret_cast<int *>(cs32 + 2 * m);
+    }
+};
+
+// doubles of scratch per warp (kept a multiple of 2 for 16-byte alignment)
+HD constexpr int gauss_smem_doubles(int m) {
+    return ((2 * m * (m + 1) + 3 * m) + (4 * m * (m + 1) + 3 * m + 2 * m + 1) / 2 + 1) & ~1;
 }
 
-DEV void jacobi_eigen_warp(double *A, double *V, double *cs, int n) {
+// Lane layout for an n x n elementwise pass: lane = h * np2 + j, column j,
+// rows h, h + G, ... (np2 = next power of two >= n, G = 32 / np2 row groups).
+struct LaneGrid {
+    int j, h, G;
+    DEV explicit LaneGrid(int n) {
+        const int lane = threadIdx.x & 31;
+        const int lg = n <= 8 ? 3 : (n <= 16 ? 4 : 5);
+        j = lane & ((1 << lg) - 1);
+        h = lane >> lg;
+        G = 32 >> lg;
+    }
+};
+
+DEV float jsqrt(float x) { return sqrtf(x); }
+DEV double jsqrt(double x) { return ::sqrt(x); }
+
+// Round-robin (Brent-Luk circle method) partner of slot k in `round`: slot 0 is
+// fixed, slots 1..n-1 rotate.
+DEV int rr_player(int pos, int round, int m) {
+    if (pos == 0) return 0;
+    int t = pos - 1 + round;
+    if (t >= m) t -= m;
+    return 1 + t;
+}
+
+// Two-sided cyclic Jacobi, one warp, round-robin ordering: each round rotates
+// n/2 disjoint index pairs at once. A (n x ld, symmetric, n even) is destroyed:
+// its diagonal ends up holding the eigenvalues and V the eigenvectors as
+// columns. T = float for the fast first pass, double for the fallback.
+template <class T>
+DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int maxSweeps) {
     const int lane = threadIdx.x & 31;
-    for (int e = lane; e < n * n; e += 32) V[e] = (e / n == e % n) ? 1.0 : 0.0;
+    const LaneGrid g(n);
+    for (int i = g.h; i < n; i += g.G)
+        if (g.j < n) V[i * ld + g.j] = i == g.j ? T(1) : T(0);
     __syncwarp();
-    const int half = n / 2;
-    for (int sweep = 0; sweep < 30; sweep++) {
-        double off = 0.0, diag = 0.0;
-        for (int e = lane; e < n * n; e += 32) {
-            const int i = e / n, k = e % n;
-            if (i == k) diag += A[e] * A[e];
-            else if (k > i) off += A[e] * A[e];
+    const int half = n / 2, m = n - 1;
+    T prevOff = T(0);
+    for (int sweep = 0; sweep < maxSweeps; sweep++) {
+        T off = T(0), diag = T(0);
+        for (int i = g.h; i < n; i += g.G) {
+            if (g.j >= n) continue;
+            const T a = A[i * ld + g.j];
+            if (i == g.j) diag += a * a;
+            else if (g.j > i) off += a * a;
         }
         for (int o = 16; o > 0; o >>= 1) {
             off += __shfl_xor_sync(0xffffffffu, off, o);
             diag += __shfl_xor_sync(0xffffffffu, diag, o);
         }
-        // stop once the off-diagonal mass is at FP64 round-off of the diagonal
-        if (off <= 1e-26 * diag || off == 0.0) break;
-        for (int round = 0; round < n - 1; round++) {
+        // converged, or (single precision) stalled at round-off
+        if (off <= offTol * diag || off == T(0) || (sweep >= 4 && off > T(0.25) * prevOff)) break;
+        prevOff = off;
+        for (int round = 0; round < m; round++) {
             if (lane < half) {
-                int p = rr_partner(lane, round, n, false), q = rr_partner(lane, round, n, true);
+                int p = rr_player(lane, round, m), q = rr_player(n - 1 - lane, round, m);
                 if (p > q) { const int t = p; p = q; q = t; }
-                const double apq = A[p * n + q];
-                double c = 1.0, s = 0.0;
-                if (apq != 0.0) {
-                    const double theta = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
-                    const double t = (theta >= 0.0 ? 1.0 : -1.0) / (::fabs(theta) + ::sqrt(theta * theta + 1.0));
-                    c = 1.0 / ::sqrt(t * t + 1.0);
+                const T apq = A[p * ld + q];
+                T c = T(1), s = T(0);
+                if (apq != T(0)) {
+                    const T theta = (A[q * ld + q] - A[p * ld + p]) / (T(2) * apq);
+                    const T at = theta < T(0) ? -theta : theta;
+                    const T t = at > T(1e18) ? T(0.5) / theta
+                                             : (theta >= T(0) ? T(1) : T(-1)) / (at + jsqrt(theta * theta + T(1)));
+                    c = T(1) / jsqrt(t * t + T(1));
                     s = t * c;
                 }
+                pq[2 * lane] = p;
+                pq[2 * lane + 1] = q;
                 cs[2 * lane] = c;
                 cs[2 * lane + 1] = s;
             }
             __syncwarp();
-            // rows p, q of every pair
-            for (int task = lane; task < half * n; task += 32) {
-                const int k = task / n, j = task % n;
-                int p = rr_partner(k, round, n, false), q = rr_partner(k, round, n, true);
-                if (p > q) { const int t = p; p = q; q = t; }
-                const double c = cs[2 * k], s = cs[2 * k + 1];
-                const double apj = A[p * n + j], aqj = A[q * n + j];
-                A[p * n + j] = c * apj - s * aqj;
-                A[q * n + j] = s * apj + c * aqj;
+            if (g.j < n) {
+                for (int k = g.h; k < half; k += g.G) {  // rows p, q
+                    const int p = pq[2 * k], q = pq[2 * k + 1];
+                    const T c = cs[2 * k], s = cs[2 * k + 1];
+                    const T a = A[p * ld + g.j], b = A[q * ld + g.j];
+                    A[p * ld + g.j] = c * a - s * b;
+                    A[q * ld + g.j] = s * a + c * b;
+                }
             }
             __syncwarp();
-            // columns p, q of every pair, and the eigenvector columns
-            for (int task = lane; task < half * n; task += 32) {
-                const int k = task / n, i = task % n;
-                int p = rr_partner(k, round, n, false), q = rr_partner(k, round, n, true);
-                if (p > q) { const int t = p; p = q; q = t; }
-                const double c = cs[2 * k], s = cs[2 * k + 1];
-                const double aip = A[i * n + p], aiq = A[i * n + q];
-                A[i * n + p] = c * aip - s * aiq;
-                A[i * n + q] = s * aip + c * aiq;
-                const double vip = V[i * n + p], viq = V[i * n + q];
-                V[i * n + p] = c * vip - s * viq;
-                V[i * n + q] = s * vip + c * viq;
+            if (g.j < n) {
+                for (int k = g.h; k < half; k += g.G) {  // columns p, q and the eigenvector columns
+                    const int p = pq[2 * k], q = pq[2 * k + 1];
+                    const T c = cs[2 * k], s = cs[2 * k + 1];
+                    const int r = g.j * ld;
+                    const T a = A[r + p], b = A[r + q];
+                    A[r + p] = c * a - s * b;
+                    A[r + q] = s * a + c * b;
+                    const T va = V[r + p], vb = V[r + q];
+                    V[r + p] = c * va - s * vb;
+                    V[r + q] = s * va + c * vb;
+                }
             }
             __syncwarp();
         }
     }
 }
 
-// ComputeGaussian with one warp: grad (D floats), hess (D x D floats,
-// row-major) in global memory; A, V (kMaxDim^2 doubles each) and cs (2 kMaxDim)
-// in this warp's shared memory. Non-finite derivatives are scrubbed to zero
-// first (drsmallstep.cpp:149-154). All 32 lanes must call it.
-DEV void compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const float *grad, const float *hess,
-                               double *A, double *V, double *cs, GaussView g) {
+// One refinement step of the symmetric eigen-decomposition (Ogita & Aishima,
+// "Iterative refinement for symmetric eigenvalue decomposition", 2018) from the
+// FP32 Jacobi result (X = V32, lambda = l32) to FP64 accuracy. Only the
+// cancelling sums run in FP64 (the residual Z = A X - X diag(lambda) and
+// R = I - X^T X); the corrections built from them are ~1e-7 and are formed in
+// FP32:
+//   T = X^T Z,  lambda~_i = lambda_i + T_ii / (1 - R_ii),
+//   E_ij = (T_ij + R_ij (lambda~_j - lambda_j)) / (lambda~_j - lambda~_i)  if the gap exceeds delta,
+//   E_ij = R_ij / 2  otherwise (clusters; and i = j),
+//   X' = X + X E,  delta = 2 (|offdiag(X^T A X)|_F + |A|_F |R|_F).
+// The step is accepted when the FP64 residual |A X' - X' diag(lambda~)|_F is
+// below 1e-12 |A|_F; otherwise (eigenvalue clusters the FP32 pass could not
+// separate) the caller falls back to FP64 Jacobi. Writes X and lam in sm.
+DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
     const int lane = threadIdx.x & 31;
+    const LaneGrid g(n);
+    const int ld = sm.ld;
+    const double *A = sm.A64;
+    const float *X32 = sm.V32;
+    float *Z = sm.A32;
+    // Z = A X - X diag(l32) and R = I - X^T X, FP64 accumulation of exact FP32 products
+    if (g.j < n) {
+        const double lj = double(sm.l32[g.j]);
+        for (int i = g.h; i < n; i += g.G) {
+            double z = -double(X32[i * ld + g.j]) * lj;
+            double r = i == g.j ? 1.0 : 0.0;
+            for (int k = 0; k < n; k++) {
+                const double xkj = double(X32[k * ld + g.j]);
+                z = ::fma(A[i * ld + k], xkj, z);
+                r = ::fma(-double(X32[k * ld + i]), xkj, r);
+            }
+            Z[i * ld + g.j] = float(z);
+            sm.R32[i * ld + g.j] = float(r);
+        }
+    }
+    __syncwarp();
+    // T = X^T Z (FP32)
+    if (g.j < n) {
+        for (int i = g.h; i < n; i += g.G) {
+            float t = 0.0f;
+            for (int k = 0; k < n; k++) t = fmaf(X32[k * ld + i], Z[k * ld + g.j], t);
+            sm.T32[i * ld + g.j] = t;
+        }
+    }
+    __syncwarp();
+    if (lane < n) sm.lam[lane] = double(sm.l32[lane]) + double(sm.T32[lane * ld + lane]) / (1.0 - double(sm.R32[lane * ld + lane]));
+    __syncwarp();
+    float offS = 0.0f, nR = 0.0f;
+    if (g.j < n) {
+        for (int i = g.h; i < n; i += g.G) {
+            const float r = sm.R32[i * ld + g.j];
+            nR += r * r;
+            if (i != g.j) {
+                const float sij = sm.T32[i * ld + g.j] - r * sm.l32[g.j];
+                offS += sij * sij;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        offS += __shfl_xor_sync(0xffffffffu, offS, o);
+        nR += __shfl_xor_sync(0xffffffffu, nR, o);
+    }
+    const float delta = 2.0f * (sqrtf(offS) + float(froA) * sqrtf(nR));
+    // E in place of T
+    if (g.j < n) {
+        const double ltj = sm.lam[g.j];
+        const float dj = float(ltj - double(sm.l32[g.j]));
+        for (int i = g.h; i < n; i += g.G) {
+            const float r = sm.R32[i * ld + g.j];
+            float e;
+            const float gap = float(ltj - sm.lam[i]);
+            if (i == g.j || !(fabsf(gap) > delta)) e = 0.5f * r;
+            else e = (sm.T32[i * ld + g.j] + r * dj) / gap;
+            sm.T32[i * ld + g.j] = e;
+        }
+    }
+    __syncwarp();
+    // X' = X + X E: the product in FP32 (it is ~1e-7), the sum in FP64
+    if (g.j < n) {
+        for (int i = g.h; i < n; i += g.G) {
+            float c = 0.0f;
+            for (int k = 0; k < n; k++) c = fmaf(X32[i * ld + k], sm.T32[k * ld + g.j], c);
+            sm.X[i * ld + g.j] = double(X32[i * ld + g.j]) + double(c);
+        }
+    }
+    __syncwarp();
+    // certificate: FP64 residual of the refined pairs
+    double res = 0.0;
+    if (g.j < n) {
+        const double lj = sm.lam[g.j];
+        for (int i = g.h; i < n; i += g.G) {
+            double z = -sm.X[i * ld + g.j] * lj;
+            for (int k = 0; k < n; k++) z = ::fma(A[i * ld + k], sm.X[k * ld + g.j], z);
+            res += z * z;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) res += __shfl_xor_sync(0xffffffffu, res, o);
+    return res <= 1e-24 * froA * froA;  // false for NaN
+}
+
+enum : int { kGaussIsotropic = 0, kGaussRefined = 1, kGaussFp64Jacobi = 2 };
+
+// ComputeGaussian with one warp: grad (D floats), hess (D x D floats,
+// row-major) in global memory; scratch in this warp's shared memory (GaussSmem
+// sized for the launch's largest dimension). Non-finite derivatives are
+// scrubbed to zero first (drsmallstep.cpp:149-154). All 32 lanes must call it.
+// The eigen-decomposition is FP32 Jacobi refined to FP64 (refine_eigen_warp),
+// or FP64 Jacobi when the refinement's certificate fails. Returns which of the
+// three (isotropic fallback, refined, FP64 Jacobi) produced the Gaussian.
+DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const float *grad, const float *hess,
+                               GaussSmem &sm, GaussView g) {
+    const int lane = threadIdx.x & 31;
+    const int ld = sm.ld;
     bool finite = true;
     for (int i = lane; i < dim; i += 32) finite = finite && isfinite(grad[i]);
     for (int i = lane; i < dim * dim; i += 32) finite = finite && isfinite(hess[i]);
@@ -165,24 +334,40 @@ DEV void compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const fl
             *g.dimv = double(dim);
         }
         __syncwarp();
-        return;
+        return kGaussIsotropic;
     }
     // symmetrise: the reference maps the row-major Hessian as a column-major
     // matrix and SelfAdjointEigenSolver reads its lower triangle, i.e. the
     // row-major upper triangle
-    for (int e = lane; e < dim * dim; e += 32) {
-        const int i = e / dim, k = e % dim;
-        A[e] = finite ? double(hess[i <= k ? e : k * dim + i]) : 0.0;
+    {
+        const LaneGrid lg(dim);
+        if (lg.j < dim) {
+            for (int i = lg.h; i < dim; i += lg.G) {
+                const int k = lg.j;
+                const float h = finite ? hess[i <= k ? i * dim + k : k * dim + i] : 0.0f;
+                sm.A64[i * ld + k] = double(h);
+                sm.A32[i * ld + k] = h;
+            }
+        }
     }
     __syncwarp();
-    jacobi_eigen_warp(A, V, cs, dim);
+    jacobi_warp<float>(sm.A32, sm.V32, sm.cs32, sm.pq, dim, ld, 1e-13f, 16);
+    if (lane < dim) sm.l32[lane] = sm.A32[lane * ld + lane];
+    __syncwarp();
+    int kind = kGaussRefined;
+    if (!refine_eigen_warp(sm, dim, ::sqrt(fro))) {
+        kind = kGaussFp64Jacobi;
+        jacobi_warp<double>(sm.A64, sm.X, sm.cs64, sm.pq, dim, ld, 1e-26, 30);
+        if (lane < dim) sm.lam[lane] = sm.A64[lane * ld + lane];
+        __syncwarp();
+    }
     // per eigenvalue (lane k): H2MC bounding and the drifted mean's eigen-coordinates
     double mt = 0.0, logp = 0.0;
     if (lane < dim) {
         const int k = lane;
-        const double lam = A[k * dim + k];
+        const double lam = sm.lam[k];
         double vg = 0.0;
-        for (int i = 0; i < dim; i++) vg += V[i * dim + k] * (finite ? double(grad[i]) : 0.0);
+        for (int i = 0; i < dim; i++) vg += sm.X[i * ld + k] * (finite ? double(grad[i]) : 0.0);
         double eb = ::fabs(lam) > 1e-10 ? 1.0 / ::fabs(lam) : 0.0;
         const double ob = eb * vg;
         double s2, o;
@@ -205,21 +390,22 @@ DEV void compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const fl
         g.p[k] = post;
         mt = eb / post * o;
         logp = ::log(post);
-        cs[k] = mt;
+        sm.cs64[k] = mt;
     }
     for (int o = 16; o > 0; o >>= 1) logp += __shfl_xor_sync(0xffffffffu, logp, o);
     __syncwarp();
-    for (int e = lane; e < dim * dim; e += 32) g.V[e] = V[e];
+    for (int e = lane; e < dim * dim; e += 32) g.V[e] = sm.X[(e / dim) * ld + e % dim];
     for (int i = lane; i < dim; i += 32) {
-        double m = 0.0;
-        for (int k = 0; k < dim; k++) m += V[i * dim + k] * cs[k];
-        g.mean[i] = m;
+        double mu = 0.0;
+        for (int k = 0; k < dim; k++) mu += sm.X[i * ld + k] * sm.cs64[k];
+        g.mean[i] = mu;
     }
     if (lane == 0) {
         *g.logDet = logp;
         *g.dimv = double(dim);
     }
     __syncwarp();
+    return kind;
 }
 
 // GaussianLogPdf (src/gaussian.cpp:18-26) in FP64.

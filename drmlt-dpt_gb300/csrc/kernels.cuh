@@ -43,7 +43,7 @@ struct Scratch {
 
 enum : int {
     kStatLarge = 0, kStatLargeAcc, kStatStage1, kStatStage1Acc, kStatIso, kStatIsoAcc, kStatH2mc,
-    kStatH2mcAcc, kStatMutations, kNumStats
+    kStatH2mcAcc, kStatMutations, kStatGauss, kStatGaussFallback, kNumStats
 };
 
 struct ChainView {
@@ -79,6 +79,7 @@ struct RunParams {
     float uniformMix;
     int accMap;
     int maxDerv;
+    int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch
     unsigned long long seed;
 };
 
@@ -274,12 +275,13 @@ __global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
                     p.d.hess + size_t(w) * kMaxDim * kMaxDim);
 }
 
-// One warp per listed chain; 4 warps per block share nothing but the block.
+// One warp per listed chain; 4 warps per block, each with its own slice of
+// dynamic shared memory (gauss_smem_doubles(maxDim) doubles).
 constexpr int kGaussWarps = 4;
-constexpr int kGaussSmem = 2 * kMaxDim * kMaxDim + 2 * kMaxDim;  // doubles per warp
+inline size_t gauss_smem_bytes(int maxDim) { return size_t(kGaussWarps) * gauss_smem_doubles(maxDim) * sizeof(double); }
 
 __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int which) {
-    __shared__ double sm[kGaussWarps][kGaussSmem];
+    extern __shared__ double gsm[];
     const int wib = threadIdx.x >> 5;
     const int w = blockIdx.x * kGaussWarps + wib;
     const int n = p.d.counters[which == 0 ? 0 : 1];
@@ -287,11 +289,17 @@ __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int whi
     const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
     Slot &st = slot_of(p.d, chain, which);
     const int dim = path_dim(st.rec.c, st.rec.l);
-    double *A = sm[wib];
-    compute_gaussian_warp(dim, H2mcParam(p.sigma1), st.ss, p.d.grad + size_t(w) * kMaxDim,
-                          p.d.hess + size_t(w) * kMaxDim * kMaxDim, A, A + kMaxDim * kMaxDim,
-                          A + 2 * kMaxDim * kMaxDim, GaussView(gauss_of(p.d, chain, which)));
-    if ((threadIdx.x & 31) == 0) st.gaussInit = 1;
+    GaussSmem sm(gsm + size_t(wib) * gauss_smem_doubles(p.gaussDim), p.gaussDim);
+    // dim <= gaussDim holds by construction (max_depth bounds every path); the
+    // isotropic branch needs no scratch, so an impossible larger dim stays in bounds
+    const int kind = compute_gaussian_warp(dim, H2mcParam(p.sigma1), dim <= sm.m ? st.ss : 0.0f,
+                                           p.d.grad + size_t(w) * kMaxDim, p.d.hess + size_t(w) * kMaxDim * kMaxDim, sm,
+                                           GaussView(gauss_of(p.d, chain, which)));
+    if ((threadIdx.x & 31) == 0) {
+        st.gaussInit = 1;
+        if (kind != kGaussIsotropic) atomicAdd(&p.d.stats[kStatGauss], 1ull);
+        if (kind == kGaussFp64Jacobi) atomicAdd(&p.d.stats[kStatGaussFallback], 1ull);
+    }
 }
 
 // ------------------------------------------------------------- stage 2 proposal

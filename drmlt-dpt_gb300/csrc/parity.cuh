@@ -130,20 +130,26 @@ __global__ void k_replay(SceneView s, int mode, const float *tapes, const int *t
     outConsumed[i] = rng.pos;
 }
 
+// dims[i] must be even and <= maxDim (checked by the callers); dynamic shared
+// memory gauss_smem_bytes(maxDim).
 __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss_batch(const int *dims, const float *ss, const float *grad,
-                                                                 const float *hess, int n, float sigma, double *store,
-                                                                 double *mean, double *invCov, double *cov,
-                                                                 double *logDet) {
-    __shared__ double sm[kGaussWarps][kGaussSmem];
+                                                                 const float *hess, int n, float sigma, int maxDim,
+                                                                 double *store, double *mean, double *invCov,
+                                                                 double *cov, double *logDet) {
+    extern __shared__ double gsm[];
     const int wib = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * kGaussWarps + wib;
     if (i >= n) return;
     const int dim = dims[i];
+    if (dim <= 0 || dim > maxDim || (dim & 1)) {
+        if (lane == 0) logDet[i] = __longlong_as_double(0x7ff8000000000000ll);
+        return;
+    }
     GaussView g(store + size_t(i) * kGaussStride);
-    double *A = sm[wib];
+    GaussSmem sm(gsm + size_t(wib) * gauss_smem_doubles(maxDim), maxDim);
     compute_gaussian_warp(dim, H2mcParam(sigma), ss[i], grad + size_t(i) * kMaxDim, hess + size_t(i) * kMaxDim * kMaxDim,
-                          A, A + kMaxDim * kMaxDim, A + 2 * kMaxDim * kMaxDim, g);
+                          sm, g);
     for (int r = lane; r < dim; r += 32) mean[size_t(i) * kMaxDim + r] = g.mean[r];
     for (int e = lane; e < dim * dim; e += 32) {
         const int r = e / dim, c = e % dim;
@@ -322,8 +328,12 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
                            int n, double *mean, double *inv_cov, double *cov, double *log_det) {
     if (!handle || n < 0) return fail(DRMLT_E_ARG, "bad argument");
     if (n == 0) return DRMLT_OK;
-    for (int i = 0; i < n; i++)
-        if (dims[i] < 1 || dims[i] > kMaxDim) return fail(DRMLT_E_ARG, "dimension out of range");
+    int maxDim = 2;
+    for (int i = 0; i < n; i++) {
+        if (dims[i] < 2 || dims[i] > kMaxDim || (dims[i] & 1))
+            return fail(DRMLT_E_ARG, "dimension must be even and in [2, 24]");
+        maxDim = std::max(maxDim, int(dims[i]));
+    }
     Renderer *r = static_cast<Renderer *>(handle);
     int rc;
     DevBuf<int> dd;
@@ -337,8 +347,8 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
     CK(cudaMemset(dm.p, 0, size_t(n) * kMaxDim * sizeof(double)));
     CK(cudaMemset(dic.p, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double)));
     CK(cudaMemset(dc.p, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double)));
-    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps>>>(dd.p, dss.p, dg.p, dh.p, n, r->opt.perturb_stddev, dstore.p, dm.p, dic.p, dc.p,
-                                         dl.p);
+    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps, gauss_smem_bytes(maxDim)>>>(
+        dd.p, dss.p, dg.p, dh.p, n, r->opt.perturb_stddev, maxDim, dstore.p, dm.p, dic.p, dc.p, dl.p);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
     if ((rc = dm.get(mean, size_t(n) * kMaxDim)) || (rc = dic.get(inv_cov, size_t(n) * kMaxDim * kMaxDim)) ||

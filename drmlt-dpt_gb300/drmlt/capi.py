@@ -64,7 +64,8 @@ class Options(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "large_step", "large_step_accepted", "stage1", "stage1_accepted", "stage2_iso",
-        "stage2_iso_accepted", "stage2_h2mc", "stage2_h2mc_accepted", "mutations")]
+        "stage2_iso_accepted", "stage2_h2mc", "stage2_h2mc_accepted", "mutations", "gaussians",
+        "gaussians_fp64_fallback")]
 
 
 class Path(C.Structure):

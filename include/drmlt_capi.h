@@ -112,13 +112,17 @@ typedef struct drmlt_options {
     int32_t use_graph;            /* capture each iteration as a CUDA graph */
 } drmlt_options;
 
-/* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels). */
+/* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
+ * two counters of this implementation: anisotropic Gaussians computed, and how
+ * many of them needed the FP64 Jacobi fallback (eigenvalue clusters the
+ * FP32-then-refined eigensolver could not certify). */
 typedef struct drmlt_stats {
     uint64_t large_step, large_step_accepted;
     uint64_t stage1, stage1_accepted;
     uint64_t stage2_iso, stage2_iso_accepted;
     uint64_t stage2_h2mc, stage2_h2mc_accepted;
     uint64_t mutations;
+    uint64_t gaussians, gaussians_fp64_fallback;
 } drmlt_stats;
 
 /* A technique path (one Markov state): SubpathContrib camDepth c / lightDepth l,

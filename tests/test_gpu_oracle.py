@@ -151,7 +151,7 @@ def test_random_derivatives_vs_fp64_oracle(renderers, oracles, cfg):
 
 @pytest.mark.parametrize("cfg", CFGS)
 def test_random_gaussians_vs_fp64_oracle(renderers, oracles, cfg):
-    """ComputeGaussian on the GPU (warp Jacobi, FP64) vs the oracle's sequential FP64 Jacobi."""
+    """ComputeGaussian on the GPU (FP32 Jacobi refined to FP64) vs the oracle's sequential FP64 Jacobi."""
     tapes, cam, lgt, g, o, keep = _valid_paths(cfg, renderers, oracles)
     paths = g[2][keep]
     ss = g[1][keep, 0]["ss"].astype(np.float32)
@@ -170,6 +170,7 @@ def test_random_gaussians_vs_fp64_oracle(renderers, oracles, cfg):
         worst.append(max(e))
     worst = np.array(worst)
     assert np.mean(worst < 1e-6) >= 0.995, "max %g" % worst.max()
+    assert np.median(worst) < 1e-10, np.median(worst)
 
 
 @pytest.mark.parametrize("cfg", ["cfg1"])
@@ -183,8 +184,11 @@ def test_ray_hits_vs_oracle(renderers, oracles, cfg):
     r, o = renderers(cfg), oracles(cfg)
     tg, thg = r.trace_rays(org, d)
     to, tho = o.trace_rays(org, d)
-    agree = np.mean(tg == to)
-    assert agree >= 0.9999, agree
+    # a different triangle at the same distance is a tie between coplanar
+    # triangles (a box's bottom face lies on the floor), not a miss
+    tie = (tg != to) & (tg >= 0) & (to >= 0) & (np.abs(thg - tho) <= 1e-5 * np.abs(tho))
+    agree = np.mean((tg == to) | tie)
+    assert agree >= 0.9999, (agree, np.mean(tie))
     both = (tg == to) & (tg >= 0)
     assert np.allclose(thg[both], tho[both], rtol=1e-5, atol=1e-6)
     og, _ = r.trace_rays(org, d, tmax=1.0, any_hit=True)

@@ -47,7 +47,10 @@ def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_
         r.render()
         img = r.film().astype(np.float64)
         st = r.stats()
-    assert st["mutations"] == sd.options.spp * sd.width * sd.height
+    # the reference's loop runs numSamplesPerChain % numChains extra samples
+    # (chainsNeedExtraSamples, delayed.cpp:209-210,339), so the total is within one
+    # sample per chain of spp * W * H
+    assert abs(st["mutations"] - sd.options.spp * sd.width * sd.height) <= sd.options.numChains
     mine = dict(large=st["large_step_accepted"] / st["large_step"],
                 stage1=st["stage1_accepted"] / st["stage1"],
                 stage2_iso=st["stage2_iso_accepted"] / st["stage2_iso"],
