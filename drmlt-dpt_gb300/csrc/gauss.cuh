@@ -148,7 +148,7 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
             diag += __shfl_xor_sync(0xffffffffu, diag, o);
         }
         // converged, or (single precision) stalled at round-off
-        if (off <= offTol * diag || off == T(0) || (sweep >= 4 && off > T(0.25) * prevOff)) break;
+        if (off <= offTol * diag || off == T(0) || (sweep >= 6 && off > T(0.5) * prevOff)) break;
         prevOff = off;
         for (int round = 0; round < m; round++) {
             if (lane < half) {
@@ -198,104 +198,137 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
     }
 }
 
-// One refinement step of the symmetric eigen-decomposition (Ogita & Aishima,
-// "Iterative refinement for symmetric eigenvalue decomposition", 2018) from the
-// FP32 Jacobi result (X = V32, lambda = l32) to FP64 accuracy. Only the
-// cancelling sums run in FP64 (the residual Z = A X - X diag(lambda) and
-// R = I - X^T X); the corrections built from them are ~1e-7 and are formed in
-// FP32:
-//   T = X^T Z,  lambda~_i = lambda_i + T_ii / (1 - R_ii),
-//   E_ij = (T_ij + R_ij (lambda~_j - lambda_j)) / (lambda~_j - lambda~_i)  if the gap exceeds delta,
-//   E_ij = R_ij / 2  otherwise (clusters; and i = j),
-//   X' = X + X E,  delta = 2 (|offdiag(X^T A X)|_F + |A|_F |R|_F).
-// The step is accepted when the FP64 residual |A X' - X' diag(lambda~)|_F is
-// below 1e-12 |A|_F; otherwise (eigenvalue clusters the FP32 pass could not
-// separate) the caller falls back to FP64 Jacobi. Writes X and lam in sm.
-DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
-    const int lane = threadIdx.x & 31;
+// FP64-accumulated residuals of an approximate eigen-decomposition (X, lam):
+// Z = A X - X diag(lam) into sm.A32 and, unless skipR, R = I - X^T X into
+// sm.R32. Both are ~1e-7 or smaller, so FP32 storage keeps their accuracy; the
+// sums cancel and run in FP64. Returns |Z|_F^2. fromFloat: X is sm.V32 (then
+// every product is exact in FP64), else sm.X.
+DEV double eigen_residuals(GaussSmem &sm, int n, bool fromFloat, bool skipR) {
     const LaneGrid g(n);
     const int ld = sm.ld;
     const double *A = sm.A64;
-    const float *X32 = sm.V32;
-    float *Z = sm.A32;
-    // Z = A X - X diag(l32) and R = I - X^T X, FP64 accumulation of exact FP32 products
-    if (g.j < n) {
-        const double lj = double(sm.l32[g.j]);
-        for (int i = g.h; i < n; i += g.G) {
-            double z = -double(X32[i * ld + g.j]) * lj;
-            double r = i == g.j ? 1.0 : 0.0;
-            for (int k = 0; k < n; k++) {
-                const double xkj = double(X32[k * ld + g.j]);
-                z = ::fma(A[i * ld + k], xkj, z);
-                r = ::fma(-double(X32[k * ld + i]), xkj, r);
-            }
-            Z[i * ld + g.j] = float(z);
-            sm.R32[i * ld + g.j] = float(r);
-        }
-    }
-    __syncwarp();
-    // T = X^T Z (FP32)
-    if (g.j < n) {
-        for (int i = g.h; i < n; i += g.G) {
-            float t = 0.0f;
-            for (int k = 0; k < n; k++) t = fmaf(X32[k * ld + i], Z[k * ld + g.j], t);
-            sm.T32[i * ld + g.j] = t;
-        }
-    }
-    __syncwarp();
-    if (lane < n) sm.lam[lane] = double(sm.l32[lane]) + double(sm.T32[lane * ld + lane]) / (1.0 - double(sm.R32[lane * ld + lane]));
-    __syncwarp();
-    float offS = 0.0f, nR = 0.0f;
-    if (g.j < n) {
-        for (int i = g.h; i < n; i += g.G) {
-            const float r = sm.R32[i * ld + g.j];
-            nR += r * r;
-            if (i != g.j) {
-                const float sij = sm.T32[i * ld + g.j] - r * sm.l32[g.j];
-                offS += sij * sij;
-            }
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        offS += __shfl_xor_sync(0xffffffffu, offS, o);
-        nR += __shfl_xor_sync(0xffffffffu, nR, o);
-    }
-    const float delta = 2.0f * (sqrtf(offS) + float(froA) * sqrtf(nR));
-    // E in place of T
-    if (g.j < n) {
-        const double ltj = sm.lam[g.j];
-        const float dj = float(ltj - double(sm.l32[g.j]));
-        for (int i = g.h; i < n; i += g.G) {
-            const float r = sm.R32[i * ld + g.j];
-            float e;
-            const float gap = float(ltj - sm.lam[i]);
-            if (i == g.j || !(fabsf(gap) > delta)) e = 0.5f * r;
-            else e = (sm.T32[i * ld + g.j] + r * dj) / gap;
-            sm.T32[i * ld + g.j] = e;
-        }
-    }
-    __syncwarp();
-    // X' = X + X E: the product in FP32 (it is ~1e-7), the sum in FP64
-    if (g.j < n) {
-        for (int i = g.h; i < n; i += g.G) {
-            float c = 0.0f;
-            for (int k = 0; k < n; k++) c = fmaf(X32[i * ld + k], sm.T32[k * ld + g.j], c);
-            sm.X[i * ld + g.j] = double(X32[i * ld + g.j]) + double(c);
-        }
-    }
-    __syncwarp();
-    // certificate: FP64 residual of the refined pairs
     double res = 0.0;
     if (g.j < n) {
         const double lj = sm.lam[g.j];
         for (int i = g.h; i < n; i += g.G) {
-            double z = -sm.X[i * ld + g.j] * lj;
-            for (int k = 0; k < n; k++) z = ::fma(A[i * ld + k], sm.X[k * ld + g.j], z);
+            const double xij = fromFloat ? double(sm.V32[i * ld + g.j]) : sm.X[i * ld + g.j];
+            double z = -xij * lj;
+            double r = i == g.j ? 1.0 : 0.0;
+            for (int k = 0; k < n; k++) {
+                const double xkj = fromFloat ? double(sm.V32[k * ld + g.j]) : sm.X[k * ld + g.j];
+                z = ::fma(A[i * ld + k], xkj, z);
+                if (!skipR) {
+                    const double xki = fromFloat ? double(sm.V32[k * ld + i]) : sm.X[k * ld + i];
+                    r = ::fma(-xki, xkj, r);
+                }
+            }
+            sm.A32[i * ld + g.j] = float(z);
+            if (!skipR) sm.R32[i * ld + g.j] = float(r);
             res += z * z;
         }
     }
     for (int o = 16; o > 0; o >>= 1) res += __shfl_xor_sync(0xffffffffu, res, o);
-    return res <= 1e-24 * froA * froA;  // false for NaN
+    __syncwarp();
+    return res;
+}
+
+// Iterative refinement of the symmetric eigen-decomposition (Ogita & Aishima,
+// "Iterative refinement for symmetric eigenvalue decomposition", 2018), from
+// the FP32 Jacobi result (sm.V32, sm.l32) towards FP64 accuracy. Per step, with
+// Z = A X - X diag(lam) and R = I - X^T X from eigen_residuals:
+//   T = X^T Z,  lam~_i = lam_i + T_ii / (1 - R_ii),
+//   E_ij = (T_ij + R_ij (lam~_j - lam_j)) / (lam~_j - lam~_i)  if |lam~_j - lam~_i| > delta,
+//   E_ij = R_ij / 2  otherwise (clusters, and i = j),
+//   X' = X + X E,  delta = 2 (|offdiag(X^T A X)|_F + |A|_F |R|_F).
+// T, E and X E are ~1e-7 and are formed in FP32 from a float copy of X; only
+// the residual sums and X + X E are FP64. A step is accepted when the FP64
+// residual of (X', lam~) is below 1e-11 |A|_F; at most two steps, then the
+// caller falls back to FP64 Jacobi. Leaves X and lam in sm.
+DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
+    const int lane = threadIdx.x & 31;
+    const LaneGrid g(n);
+    const int ld = sm.ld;
+    const double tol2 = 1e-22 * froA * froA;
+    if (lane < n) sm.lam[lane] = double(sm.l32[lane]);
+    __syncwarp();
+    eigen_residuals(sm, n, true, false);
+    if (g.j < n)
+        for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = double(sm.V32[i * ld + g.j]);
+    double *lamNew = sm.cs64;
+    for (int step = 0; step < 2; step++) {
+        const float *X32 = sm.V32;
+        const float *Z = sm.A32;
+        // T = X^T Z
+        if (g.j < n) {
+            for (int i = g.h; i < n; i += g.G) {
+                float t = 0.0f;
+                for (int k = 0; k < n; k++) t = fmaf(X32[k * ld + i], Z[k * ld + g.j], t);
+                sm.T32[i * ld + g.j] = t;
+            }
+        }
+        __syncwarp();
+        if (lane < n)
+            lamNew[lane] = sm.lam[lane] + double(sm.T32[lane * ld + lane]) / (1.0 - double(sm.R32[lane * ld + lane]));
+        float offS = 0.0f, nR = 0.0f;
+        if (g.j < n) {
+            const float lj = float(sm.lam[g.j]);
+            for (int i = g.h; i < n; i += g.G) {
+                const float r = sm.R32[i * ld + g.j];
+                nR += r * r;
+                if (i != g.j) {
+                    const float sij = sm.T32[i * ld + g.j] - r * lj;
+                    offS += sij * sij;
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            offS += __shfl_xor_sync(0xffffffffu, offS, o);
+            nR += __shfl_xor_sync(0xffffffffu, nR, o);
+        }
+        const float delta = 2.0f * (sqrtf(offS) + float(froA) * sqrtf(nR));
+        __syncwarp();
+        // E in place of T
+        if (g.j < n) {
+            const double ltj = lamNew[g.j];
+            const float dj = float(ltj - sm.lam[g.j]);
+            for (int i = g.h; i < n; i += g.G) {
+                const float r = sm.R32[i * ld + g.j];
+                const float gap = float(ltj - lamNew[i]);
+                float e;
+                if (i == g.j || !(fabsf(gap) > delta)) e = 0.5f * r;
+                else e = (sm.T32[i * ld + g.j] + r * dj) / gap;
+                sm.T32[i * ld + g.j] = e;
+            }
+        }
+        __syncwarp();
+        // X' = X + X E: the product in FP32 (it is ~1e-7), the sum in FP64
+        if (g.j < n) {
+            for (int i = g.h; i < n; i += g.G) {
+                float c = 0.0f;
+                for (int k = 0; k < n; k++) c = fmaf(X32[i * ld + k], sm.T32[k * ld + g.j], c);
+                sm.X[i * ld + g.j] += double(c);
+            }
+        }
+        if (lane < n) sm.lam[lane] = lamNew[lane];
+        __syncwarp();
+        // certificate: FP64 residual of the refined pairs (also the next step's Z)
+        const double res = eigen_residuals(sm, n, false, true);
+        if (res <= tol2) return true;  // false for NaN
+        if (step == 1) break;
+        if (g.j < n)
+            for (int i = g.h; i < n; i += g.G) sm.V32[i * ld + g.j] = float(sm.X[i * ld + g.j]);
+        __syncwarp();
+        // R for the refined X (FP64; Z is already in place)
+        if (g.j < n) {
+            for (int i = g.h; i < n; i += g.G) {
+                double r = i == g.j ? 1.0 : 0.0;
+                for (int k = 0; k < n; k++) r = ::fma(-sm.X[k * ld + i], sm.X[k * ld + g.j], r);
+                sm.R32[i * ld + g.j] = float(r);
+            }
+        }
+        __syncwarp();
+    }
+    return false;
 }
 
 enum : int { kGaussIsotropic = 0, kGaussRefined = 1, kGaussFp64Jacobi = 2 };
@@ -351,7 +384,7 @@ DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const flo
         }
     }
     __syncwarp();
-    jacobi_warp<float>(sm.A32, sm.V32, sm.cs32, sm.pq, dim, ld, 1e-13f, 16);
+    jacobi_warp<float>(sm.A32, sm.V32, sm.cs32, sm.pq, dim, ld, 1e-14f, 12);
     if (lane < dim) sm.l32[lane] = sm.A32[lane * ld + lane];
     __syncwarp();
     int kind = kGaussRefined;
