@@ -76,8 +76,13 @@ struct Renderer {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float lastRunMs = 0.0f;
+    long long launches = 0;  // kernels launched by run() so far
     cudaGraphExec_t graph = nullptr;
     int *dIter = nullptr;
+    // chain groups, each stepped on its own stream
+    int G = 1, chunk = 0;
+    std::vector<cudaStream_t> gstreams;
+    std::vector<cudaEvent_t> gevents;
     unsigned long long bootSeed = 0;
 
     template <class T>
@@ -94,17 +99,21 @@ struct Renderer {
     }
     ~Renderer() {
         if (graph) cudaGraphExecDestroy(graph);
+        for (cudaStream_t s : gstreams) cudaStreamDestroy(s);
+        for (cudaEvent_t e : gevents) cudaEventDestroy(e);
         for (void *p : owned) cudaFree(p);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
     }
 
+    // all chains at once (prepass seeding)
     RunParams params() const {
         RunParams p;
         p.s = sv;
         p.d = cv;
         p.N = N;
+        p.c0 = 0;
         p.samplesPerChain = samplesPerChain;
         p.extraChains = extraChains;
         p.b = b;
@@ -119,6 +128,22 @@ struct Renderer {
         p.maxDerv = opt.max_derivative_depth;
         p.gaussDim = std::min(2 * opt.max_depth, kMaxDim);
         p.seed = opt.seed;
+        return p;
+    }
+
+    // chain group g: its chain range and its slices of the lists, counters and derivative rows
+    RunParams params(int g) const {
+        RunParams p = params();
+        p.c0 = g * chunk;
+        p.N = std::min(chunk, N - p.c0);
+        p.d.listX += p.c0;
+        p.d.listZ += p.c0;
+        p.d.listS += p.c0;
+        p.d.counters += 4 * g;
+        p.d.hist += size_t(kPlanBins) * g;
+        p.d.order += p.c0;
+        p.d.grad += size_t(p.c0) * kMaxDim;
+        p.d.hess += size_t(p.c0) * kMaxDim * kMaxDim;
         return p;
     }
 
@@ -297,7 +322,22 @@ struct Renderer {
         if ((rc = alloc(&cv.scr, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listX, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
-        if ((rc = alloc(&cv.counters, 4))) return rc;
+        if ((rc = alloc(&cv.listS, size_t(N)))) return rc;
+        G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 4;
+        G = std::min(G, N);
+        chunk = (N + G - 1) / G;
+        G = (N + chunk - 1) / chunk;
+        for (int g = 0; g < G; g++) {
+            cudaStream_t s;
+            cudaEvent_t e;
+            CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            gstreams.push_back(s);
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            gevents.push_back(e);
+        }
+        if ((rc = alloc(&cv.counters, 4 * size_t(G)))) return rc;
+        if ((rc = alloc(&cv.hist, size_t(kPlanBins) * G))) return rc;
+        if ((rc = alloc(&cv.order, size_t(N)))) return rc;
         if ((rc = alloc(&cv.grad, size_t(N) * kMaxDim))) return rc;
         if ((rc = alloc(&cv.hess, size_t(N) * kMaxDim * kMaxDim))) return rc;
         if ((rc = alloc(&cv.stats, kNumStats))) return rc;
@@ -306,7 +346,7 @@ struct Renderer {
         CK(cudaMemset(cv.stats, 0, kNumStats * sizeof(unsigned long long)));
         CK(cudaMemset(cv.film, 0, size_t(W) * H * 3 * sizeof(float)));
         CK(cudaMemset(cv.direct, 0, size_t(W) * H * 3 * sizeof(float)));
-        CK(cudaMemset(cv.counters, 0, 4 * sizeof(int)));
+        CK(cudaMemset(cv.counters, 0, 4 * size_t(G) * sizeof(int)));
         // sample split of delayed.cpp:205-210, including its extra-sample rule
         const long long totalSamples = (long long)opt.spp * W * H;
         samplesPerChain = totalSamples / N;
@@ -420,26 +460,47 @@ struct Renderer {
         return DRMLT_OK;
     }
 
-    // One Markov-chain iteration: the per-stage launches.
-    void launch_iteration(int iter) {
-        const RunParams p = params();
-        const int nb = (N + 127) / 128;
-        const int nbWarp = (N * 32 + 127) / 128;
-        const int nbG = (N + kGaussWarps - 1) / kGaussWarps;
-        k_reset_counters<<<1, 32, 0, stream>>>(cv.counters);
-        k_stage1<<<nb, 128, 0, stream>>>(p, iter);
-        k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
+    // Stage k of iteration `iter` for chain group g on stream s:
+    //   0 stage1 (counter reset, plan, order, stage-1 kernel), 1 derivatives at x,
+    //   2 Gaussians at x, 3 stage2, 4 derivatives at z, 5 Gaussians at z,
+    //   6 finish (Green's y* trace, acceptance, splats, swap).
+    // The list-driven kernels are sized for the whole group and exit past the
+    // list's device-side length.
+    static constexpr int kNumStagesRun = 7;
+    int launch_stage(int k, int g, int iter, cudaStream_t s) const {
+        const RunParams p = params(g);
+        const int nb = (p.N + kStageBlock - 1) / kStageBlock;
+        const int nbWarp = (p.N * 32 + 127) / 128;
+        const int nbG = (p.N + kGaussWarps - 1) / kGaussWarps;
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
-        k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 0);
-        k_stage2<<<nb, 128, 0, stream>>>(p, iter);
-        k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
-        k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 2);
-        k_finish<<<nb, 128, 0, stream>>>(p, iter);
+        switch (k) {
+            case 0:
+                k_reset_counters<<<1, 128, 0, s>>>(p.d.counters, p.d.hist);
+                k_plan<<<nb, kStageBlock, 0, s>>>(p, iter);
+                k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
+                k_stage1<<<nb, kStageBlock, 0, s>>>(p, iter);
+                return 4;
+            case 1: k_derivs<<<nbWarp, 128, 0, s>>>(p, 0); return 1;
+            case 2: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 0); return 1;
+            case 3: k_stage2<<<nb, kStageBlock, 0, s>>>(p, iter); return 1;
+            case 4: k_derivs<<<nbWarp, 128, 0, s>>>(p, 2); return 1;
+            case 5: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 2); return 1;
+            default:
+                if (p.drType == 0) k_ystar<<<nb, kStageBlock, 0, s>>>(p, iter);
+                k_finish<<<nb, kStageBlock, 0, s>>>(p, iter);
+                return p.drType == 0 ? 2 : 1;
+        }
+    }
+    // returns the number of kernels launched
+    int launch_iteration(int g, int iter, cudaStream_t s) const {
+        int n = 0;
+        for (int k = 0; k < kNumStagesRun; k++) n += launch_stage(k, g, iter, s);
+        return n;
     }
 
     // The same iterations with CUDA events around each stage (on the launching
     // stream); accumulates per-stage milliseconds into ms[kNumStages].
-    static constexpr int kNumStages = 7;
+    static constexpr int kNumStages = kNumStagesRun;
     int profile(long long iterations, float *ms, long long *done) {
         if (!prepassDone) return fail(DRMLT_E_STATE, "profile before prepass");
         const long long end = std::min(iterDone + iterations, total_iterations());
@@ -447,28 +508,16 @@ struct Renderer {
         for (int k = 0; k <= kNumStages; k++) CK(cudaEventCreate(&ev[k]));
         for (int k = 0; k < kNumStages; k++) ms[k] = 0.0f;
         long long mutations = 0;
-        const int nb = (N + 127) / 128, nbWarp = (N * 32 + 127) / 128, nbG = (N + kGaussWarps - 1) / kGaussWarps;
         for (long long it = iterDone; it < end; it++) {
-            const RunParams p = params();
             const int iter = int(it);
+            // stage by stage over all groups on one stream, so each stage's
+            // events bracket that stage for every chain
             cudaEventRecord(ev[0], stream);
-            k_reset_counters<<<1, 32, 0, stream>>>(cv.counters);
-            k_stage1<<<nb, 128, 0, stream>>>(p, iter);
-            cudaEventRecord(ev[1], stream);
-            k_derivs<<<nbWarp, 128, 0, stream>>>(p, 0);
-            cudaEventRecord(ev[2], stream);
-            const size_t gsm = gauss_smem_bytes(p.gaussDim);
-            k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 0);
-            cudaEventRecord(ev[3], stream);
-            k_stage2<<<nb, 128, 0, stream>>>(p, iter);
-            cudaEventRecord(ev[4], stream);
-            k_derivs<<<nbWarp, 128, 0, stream>>>(p, 2);
-            cudaEventRecord(ev[5], stream);
-            k_gauss<<<nbG, 32 * kGaussWarps, gsm, stream>>>(p, 2);
-            cudaEventRecord(ev[6], stream);
-            k_finish<<<nb, 128, 0, stream>>>(p, iter);
-            cudaEventRecord(ev[7], stream);
-            CK(cudaEventSynchronize(ev[7]));
+            for (int k = 0; k < kNumStagesRun; k++) {
+                for (int g = 0; g < G; g++) launch_stage(k, g, iter, stream);
+                cudaEventRecord(ev[k + 1], stream);
+            }
+            CK(cudaEventSynchronize(ev[kNumStages]));
             for (int k = 0; k < kNumStages; k++) {
                 float t;
                 cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
@@ -490,9 +539,14 @@ struct Renderer {
         const long long end = std::min(iterDone + iterations, total_iterations());
         long long mutations = 0;
         CK(cudaEventRecord(ev0, stream));
+        for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(gstreams[g], ev0, 0));
         for (long long it = iterDone; it < end; it++) {
-            launch_iteration(int(it));
+            for (int g = 0; g < G; g++) launches += launch_iteration(g, int(it), gstreams[g]);
             mutations += (it < samplesPerChain) ? N : extraChains;
+        }
+        for (int g = 0; g < G; g++) {
+            CK(cudaEventRecord(gevents[g], gstreams[g]));
+            CK(cudaStreamWaitEvent(stream, gevents[g], 0));
         }
         CK(cudaEventRecord(ev1, stream));
         CK(cudaGetLastError());
@@ -550,6 +604,7 @@ void drmlt_default_options(drmlt_options *o) {
     o->seed = 0x1234ABCDull;
     o->device = 0;
     o->use_graph = 0;
+    o->chain_groups = 0;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }
@@ -634,6 +689,12 @@ int drmlt_profile(void *handle, int64_t iterations, float *stage_ms, int64_t *do
 int drmlt_total_iterations(void *handle, int64_t *iterations) {
     if (!handle || !iterations) return fail(DRMLT_E_ARG, "null argument");
     *iterations = static_cast<Renderer *>(handle)->total_iterations();
+    return DRMLT_OK;
+}
+
+int drmlt_kernel_launches(void *handle, int64_t *n) {
+    if (!handle || !n) return fail(DRMLT_E_ARG, "null argument");
+    *n = static_cast<Renderer *>(handle)->launches;
     return DRMLT_OK;
 }
 

@@ -38,8 +38,14 @@ enum : int {
 struct Scratch {
     float a1, a2;
     int flags;
+    int key, rank;      // stage-1 work class and rank within it (k_plan)
+    float aStar;        // Green's reverse first-stage acceptance (k_ystar)
     float offset[kMaxDim];
 };
+
+// Stage-1 work classes: 0 idle chain; 1 + 14 c + l small step of technique
+// (c, l); 200 + 14 L + lgtLength large step of sampled length L.
+constexpr int kPlanBins = 512;
 
 enum : int {
     kStatLarge = 0, kStatLargeAcc, kStatStage1, kStatStage1Acc, kStatIso, kStatIsoAcc, kStatH2mc,
@@ -53,7 +59,10 @@ struct ChainView {
     Scratch *scr;       // N
     int *listX;         // chains needing a Gaussian at the current state
     int *listZ;         // chains needing a Gaussian at the second proposal
-    int *counters;      // [0] = |listX|, [1] = |listZ|
+    int *listS;         // chains taking a second stage this iteration
+    int *order;         // stage-1 processing order (chains grouped by work class)
+    int *hist;          // kPlanBins counters of the work classes
+    int *counters;      // [0] = |listX|, [1] = |listZ|, [2] = |listS|
     float *grad;        // N x kMaxDim (indexed by list position)
     float *hess;        // N x kMaxDim^2
     unsigned long long *stats;
@@ -65,10 +74,13 @@ struct ChainView {
     float lengthFuncInt;
 };
 
+// One launch covers one chain group: chains c0 .. c0 + N - 1. The lists,
+// counters and gradient/Hessian rows in `d` are the group's own slices.
 struct RunParams {
     SceneView s;
     ChainView d;
     int N;
+    int c0;
     long long samplesPerChain;
     long long extraChains;
     float b;
@@ -82,6 +94,8 @@ struct RunParams {
     int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch
     unsigned long long seed;
 };
+
+constexpr int kStageBlock = 64;  // threads per block of the per-chain stage kernels
 
 // ------------------------------------------------------------- reference lambdas
 DEV bool flip_coin(float x, float d) { return (x == 1.0f) || (d < x); }      // delayed.cpp:250
@@ -151,11 +165,70 @@ DEV float length_pmf(const ChainView &d, int len) {
     return d.lengthFunc[len] / (d.lengthFuncInt * float(d.lengthCount));
 }
 
+// ------------------------------------------------------------- stage-1 plan
+// Draws each chain's stage-1 coin and, for a large step, its length and light
+// subpath length exactly as k_stage1 will (same stream, same order), and bins
+// the chain by the resulting work class. k_scatter then orders the chains by
+// class so that the lanes of a warp trace the same technique.
+DEV int plan_key(const RunParams &p, int i, int iter) {
+    if (iter >= samples_of(p, i)) return 0;
+    Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 0ull);
+    const Slot &cur = slot_of(p.d, i, 0);
+    const bool isLarge = flip_coin(p.largeProb, rng.uniform());
+    if (!cur.valid || isLarge) {
+        const int length = sample_discrete(p.d.lengthCdf, p.d.lengthCount, rng.uniform());
+        int lgtLength = int(rng.uniform() * float(length + 1));
+        lgtLength = lgtLength < 0 ? 0 : (lgtLength > length ? length : lgtLength);
+        return 200 + 14 * length + lgtLength;
+    }
+    return 1 + 14 * cur.rec.c + cur.rec.l;
+}
+
+__global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p, int iter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.N) return;
+    const int i = p.c0 + t;
+    int key = plan_key(p, i, iter);
+    key = key < 0 ? 0 : (key >= kPlanBins ? kPlanBins - 1 : key);
+    Scratch &sc = p.d.scr[i];
+    sc.key = key;
+    sc.rank = atomicAdd(&p.d.hist[key], 1);
+}
+
+constexpr int kScatterBlock = 256;
+__global__ void __launch_bounds__(kScatterBlock) k_scatter(RunParams p) {
+    __shared__ int start[kPlanBins];
+    __shared__ int warpSum[kScatterBlock / 32];
+    // exclusive scan of the class counts (two bins per thread)
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int h0 = p.d.hist[2 * tid], h1 = p.d.hist[2 * tid + 1];
+    int v = h0 + h1, incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    if (lane == 31) warpSum[wid] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < wid; w++) base += warpSum[w];
+    const int excl = base + incl - v;
+    start[2 * tid] = excl;
+    start[2 * tid + 1] = excl + h0;
+    __syncthreads();
+    for (int t = blockIdx.x * blockDim.x + tid; t < p.N; t += gridDim.x * blockDim.x) {
+        const int i = p.c0 + t;
+        const Scratch &sc = p.d.scr[i];
+        p.d.order[start[sc.key] + sc.rank] = i;
+    }
+}
+static_assert(2 * kScatterBlock == kPlanBins, "k_scatter scans two bins per thread");
+
 // ------------------------------------------------------------- stage 1
-__global__ void __launch_bounds__(128) k_stage1(RunParams p, int iter) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     StatAcc acc;
-    if (i < p.N) {
+    if (t < p.N) {
+        const int i = p.d.order[t];
         Scratch &sc = p.d.scr[i];
         int flags = 0;
         float a1 = 0.0f;
@@ -218,6 +291,7 @@ __global__ void __launch_bounds__(128) k_stage1(RunParams p, int iter) {
             const bool doSecond = !accept1 && !isLarge && cur.valid && p.integrator == 0;
             if (doSecond) {
                 flags |= kSecond;
+                p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
                 if (flip_coin(p.anisoProb, rng.uniform())) {
                     flags |= kAniso;
                     acc.c[kStatH2mc]++;
@@ -303,11 +377,12 @@ __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int whi
 }
 
 // ------------------------------------------------------------- stage 2 proposal
-__global__ void __launch_bounds__(128) k_stage2(RunParams p, int iter) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.N) return;
+// Over the group's second-stage list only (compacted by k_stage1).
+__global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.d.counters[2]) return;
+    const int i = p.d.listS[t];
     Scratch &sc = p.d.scr[i];
-    if (!(sc.flags & kSecond)) return;
     Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
     Slot &cur = slot_of(p.d, i, 0);
     Slot &S = slot_of(p.d, i, 2);
@@ -349,6 +424,29 @@ __global__ void __launch_bounds__(128) k_stage2(RunParams p, int iter) {
     sc.a2 = a2;
 }
 
+// Green's reverse path y* = z + (x - y) and its first-stage acceptance from z
+// (SmallStep::Trace, mutation.cpp:210-238), over the second-stage list only.
+__global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p, int iter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.d.counters[2]) return;
+    const int i = p.d.listS[t];
+    Scratch &sc = p.d.scr[i];
+    const Slot &cur = slot_of(p.d, i, 0);
+    const Slot &F = slot_of(p.d, i, 1);
+    const Slot &S = slot_of(p.d, i, 2);
+    float aStar = 0.0f;
+    if (S.valid) {
+        const int dim = path_dim(cur.rec.c, cur.rec.l);
+        float off[kMaxDim];
+        for (int k = 0; k < dim; k++) off[k] = cur.rec.u[k] - F.rec.u[k];
+        Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 3ull);
+        PathRec ystar;
+        Emit e;
+        if (perturb_path(p.s, S.rec, off, rng, ystar, e)) aStar = clamp01(e.ss / S.ss);
+    }
+    sc.aStar = aStar;
+}
+
 // log N(d | 0, sigma^2 I) differences for Mira's Q1 ratio (delayed.cpp:512-523), FP64.
 DEV double iso_quad(int dim, const float *a, const float *b) {
     double q = 0.0;
@@ -360,10 +458,11 @@ DEV double iso_quad(int dim, const float *a, const float *b) {
 }
 
 // ------------------------------------------------------------- finish
-__global__ void __launch_bounds__(128) k_finish(RunParams p, int iter) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p, int iter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = p.c0 + t;
     StatAcc acc;
-    if (i < p.N && (p.d.scr[i].flags & kActive)) {
+    if (t < p.N && (p.d.scr[i].flags & kActive)) {
         Scratch &sc = p.d.scr[i];
         const int flags = sc.flags;
         const float a1 = sc.a1;
@@ -393,15 +492,8 @@ __global__ void __launch_bounds__(128) k_finish(RunParams p, int iter) {
             if (is_invalid(a2)) {
                 a2 = 0.0f;
             } else if (p.drType == 0) {
-                // Green & Mira (2001): y* = z + (x - y) (delayed.cpp:473-500)
-                float aStar = 0.0f;
-                if (S.valid) {
-                    float off[kMaxDim];
-                    for (int k = 0; k < dim; k++) off[k] = cur.rec.u[k] - F.rec.u[k];
-                    PathRec ystar;
-                    Emit e;
-                    if (perturb_path(p.s, S.rec, off, rng, ystar, e)) aStar = clamp01(e.ss / S.ss);
-                }
+                // Green & Mira (2001) (delayed.cpp:473-500); y* traced by k_ystar
+                float aStar = sc.aStar;
                 if (is_invalid(aStar)) aStar = 0.0f;
                 if (aStar == 1.0f) {
                     a2 = 0.0f;
@@ -469,8 +561,9 @@ __global__ void __launch_bounds__(128) k_finish(RunParams p, int iter) {
     flush_stats(acc, p.d.stats);
 }
 
-__global__ void k_reset_counters(int *counters) {
-    if (threadIdx.x < 2) counters[threadIdx.x] = 0;
+__global__ void k_reset_counters(int *counters, int *hist) {
+    if (threadIdx.x < 4) counters[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < kPlanBins; k += blockDim.x) hist[k] = 0;
 }
 
 // ------------------------------------------------------------- prepass

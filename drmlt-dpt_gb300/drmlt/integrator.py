@@ -102,6 +102,11 @@ class Renderer:
         capi.check(capi.lib().drmlt_last_run_ms(self.handle, C.byref(ms)))
         return ms.value
 
+    def kernel_launches(self) -> int:
+        n = C.c_int64()
+        capi.check(capi.lib().drmlt_kernel_launches(self.handle, C.byref(n)))
+        return n.value
+
     STAGES = ("stage1", "derivs_x", "gauss_x", "stage2", "derivs_z", "gauss_z", "finish")
 
     def profile(self, iterations: int):

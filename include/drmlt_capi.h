@@ -110,6 +110,8 @@ typedef struct drmlt_options {
     uint64_t seed;                /* GPU random-stream key */
     int32_t device;               /* CUDA device ordinal */
     int32_t use_graph;            /* capture each iteration as a CUDA graph */
+    int32_t chain_groups;         /* chains are split into this many groups, each stepped on its own
+                                     CUDA stream so the groups' kernels overlap (0 = default, 4) */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
@@ -179,6 +181,8 @@ int drmlt_get_film(void *handle, float *rgb);
 int drmlt_get_stats(void *handle, drmlt_stats *stats);
 /* Device time of the last drmlt_run in milliseconds (CUDA events). */
 int drmlt_last_run_ms(void *handle, float *ms);
+/* Kernels launched by drmlt_run on this handle so far (all chain groups). */
+int drmlt_kernel_launches(void *handle, int64_t *n);
 
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
  * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,
