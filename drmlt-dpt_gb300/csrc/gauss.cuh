@@ -110,8 +110,40 @@ struct LaneGrid {
     }
 };
 
-DEV float jsqrt(float x) { return sqrtf(x); }
-DEV double jsqrt(double x) { return ::sqrt(x); }
+
+// Jacobi rotation (c, s) that annihilates a_pq. FP32: the classic formula.
+// FP64 (used only to polish an almost diagonal matrix): the tangent comes from
+// the FP32 formula, which leaves ~1e-7 a_pq behind and keeps the sweeps
+// converging, and c = (1 + t^2)^-1/2 is brought to FP64 accuracy by two steps of
+// Newton's iteration for the reciprocal square root
+// from the FP32 estimate, so the rotation is orthogonal in
+// FP64 without FP64 division or square-root sequences.
+DEV void rot_params(float app, float aqq, float apq, float &c, float &s) {
+    c = 1.0f;
+    s = 0.0f;
+    if (apq == 0.0f) return;
+    const float theta = (aqq - app) / (2.0f * apq);
+    const float at = fabsf(theta);
+    const float t = at > 1e18f ? 0.5f / theta : (theta >= 0.0f ? 1.0f : -1.0f) / (at + sqrtf(theta * theta + 1.0f));
+    c = 1.0f / sqrtf(t * t + 1.0f);
+    s = t * c;
+}
+DEV void rot_params(double app, double aqq, double apq, double &c, double &s) {
+    c = 1.0;
+    s = 0.0;
+    const float fpq = float(apq);
+    if (fpq == 0.0f || !isfinite(fpq)) return;
+    const float theta = float(aqq - app) / (2.0f * fpq);
+    const float at = fabsf(theta);
+    const float tf = at > 1e18f ? 0.5f / theta : (theta >= 0.0f ? 1.0f : -1.0f) / (at + sqrtf(theta * theta + 1.0f));
+    const double t = double(tf);
+    const double q = ::fma(t, t, 1.0);
+    double r = double(rsqrtf(float(q)));
+    r = r * ::fma(-0.5 * q, r * r, 1.5);
+    r = r * ::fma(-0.5 * q, r * r, 1.5);
+    c = r;
+    s = t * r;
+}
 
 // Round-robin (Brent-Luk circle method) partner of slot k in `round`: slot 0 is
 // fixed, slots 1..n-1 rotate.
@@ -154,16 +186,8 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
             if (lane < half) {
                 int p = rr_player(lane, round, m), q = rr_player(n - 1 - lane, round, m);
                 if (p > q) { const int t = p; p = q; q = t; }
-                const T apq = A[p * ld + q];
-                T c = T(1), s = T(0);
-                if (apq != T(0)) {
-                    const T theta = (A[q * ld + q] - A[p * ld + p]) / (T(2) * apq);
-                    const T at = theta < T(0) ? -theta : theta;
-                    const T t = at > T(1e18) ? T(0.5) / theta
-                                             : (theta >= T(0) ? T(1) : T(-1)) / (at + jsqrt(theta * theta + T(1)));
-                    c = T(1) / jsqrt(t * t + T(1));
-                    s = t * c;
-                }
+                T c, s;
+                rot_params(A[p * ld + p], A[q * ld + q], A[p * ld + q], c, s);
                 pq[2 * lane] = p;
                 pq[2 * lane + 1] = q;
                 cs[2 * lane] = c;
@@ -331,6 +355,58 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
     return false;
 }
 
+// Fallback when the refinement cannot certify (eigenvalue clusters it could not
+// separate): FP64 Jacobi on S = X^T A X in the refined basis X, which is
+// diagonal up to the clusters, then X <- X W. Scratch: Y = A X and the
+// rotations W use the FP32 matrices' storage as FP64 matrices (A32+V32 and
+// R32+T32 are each m x ld doubles of contiguous space).
+DEV void polish_eigen_warp(GaussSmem &sm, int n) {
+    const int lane = threadIdx.x & 31;
+    const LaneGrid g(n);
+    const int ld = sm.ld;
+    double *Y = reinterpret_cast<double *>(sm.A32);
+    double *Wm = reinterpret_cast<double *>(sm.R32);
+    if (g.j < n) {
+        for (int i = g.h; i < n; i += g.G) {
+            double y = 0.0;
+            for (int k = 0; k < n; k++) y = ::fma(sm.A64[i * ld + k], sm.X[k * ld + g.j], y);
+            Y[i * ld + g.j] = y;
+        }
+    }
+    __syncwarp();
+    if (g.j < n) {  // S = X^T Y over A64 (A is no longer needed)
+        for (int i = g.h; i < n; i += g.G) {
+            double v = 0.0;
+            for (int k = 0; k < n; k++) v = ::fma(sm.X[k * ld + i], Y[k * ld + g.j], v);
+            sm.A64[i * ld + g.j] = v;
+        }
+    }
+    __syncwarp();
+    if (g.j < n) {  // symmetrise S against round-off
+        for (int i = g.h; i < n; i += g.G) {
+            if (i < g.j) {
+                const double v = 0.5 * (sm.A64[i * ld + g.j] + sm.A64[g.j * ld + i]);
+                sm.A64[i * ld + g.j] = v;
+                sm.A64[g.j * ld + i] = v;
+            }
+        }
+    }
+    __syncwarp();
+    jacobi_warp<double>(sm.A64, Wm, sm.cs64, sm.pq, n, ld, 1e-28, 8);
+    if (g.j < n) {  // X <- X W (through Y)
+        for (int i = g.h; i < n; i += g.G) {
+            double v = 0.0;
+            for (int k = 0; k < n; k++) v = ::fma(sm.X[i * ld + k], Wm[k * ld + g.j], v);
+            Y[i * ld + g.j] = v;
+        }
+    }
+    __syncwarp();
+    if (g.j < n)
+        for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = Y[i * ld + g.j];
+    if (lane < n) sm.lam[lane] = sm.A64[lane * ld + lane];
+    __syncwarp();
+}
+
 enum : int { kGaussIsotropic = 0, kGaussRefined = 1, kGaussFp64Jacobi = 2 };
 
 // ComputeGaussian with one warp: grad (D floats), hess (D x D floats,
@@ -390,9 +466,7 @@ DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const flo
     int kind = kGaussRefined;
     if (!refine_eigen_warp(sm, dim, ::sqrt(fro))) {
         kind = kGaussFp64Jacobi;
-        jacobi_warp<double>(sm.A64, sm.X, sm.cs64, sm.pq, dim, ld, 1e-26, 30);
-        if (lane < dim) sm.lam[lane] = sm.A64[lane * ld + lane];
-        __syncwarp();
+        polish_eigen_warp(sm, dim);
     }
     // per eigenvalue (lane k): H2MC bounding and the drifted mean's eigen-coordinates
     double mt = 0.0, logp = 0.0;
