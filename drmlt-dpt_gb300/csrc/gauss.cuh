@@ -131,6 +131,8 @@ DEV void rot_params(float app, float aqq, float apq, float &c, float &s) {
 DEV void rot_params(double app, double aqq, double apq, double &c, double &s) {
     c = 1.0;
     s = 0.0;
+    // below FP64 resolution of the diagonal pair: leave it (threshold Jacobi)
+    if (apq * apq <= 1e-34 * ::fabs(app * aqq)) return;
     const float fpq = float(apq);
     if (fpq == 0.0f || !isfinite(fpq)) return;
     const float theta = float(aqq - app) / (2.0f * fpq);
@@ -194,6 +196,8 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
                 cs[2 * lane + 1] = s;
             }
             __syncwarp();
+            // a round whose rotations are all the identity changes nothing
+            if (__all_sync(0xffffffffu, lane >= half || cs[2 * lane + 1] == T(0))) continue;
             if (g.j < n) {
                 for (int k = g.h; k < half; k += g.G) {  // rows p, q
                     const int p = pq[2 * k], q = pq[2 * k + 1];
@@ -356,17 +360,45 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
 }
 
 // Fallback when the refinement cannot certify (eigenvalue clusters it could not
-// separate): FP64 Jacobi on S = X^T A X in the refined basis X, which is
-// diagonal up to the clusters, then X <- X W. Scratch: Y = A X and the
-// rotations W use the FP32 matrices' storage as FP64 matrices (A32+V32 and
-// R32+T32 are each m x ld doubles of contiguous space).
+// separate; its first-order updates can then also leave X non-orthogonal):
+// Newton-Schulz orthonormalisation of X in FP64 (X <- X (3I - X^T X) / 2,
+// quadratically convergent), FP64 Jacobi on S = X^T A X, which is diagonal up
+// to ~1e-6 |A| in that basis, then X <- X W. Scratch: Y and M/W use the FP32
+// matrices' storage as FP64 matrices (A32+V32 and R32+T32 are each m x ld
+// doubles of contiguous space).
 DEV void polish_eigen_warp(GaussSmem &sm, int n) {
     const int lane = threadIdx.x & 31;
     const LaneGrid g(n);
     const int ld = sm.ld;
     double *Y = reinterpret_cast<double *>(sm.A32);
-    double *Wm = reinterpret_cast<double *>(sm.R32);
-    if (g.j < n) {
+    double *M = reinterpret_cast<double *>(sm.R32);
+    for (int it = 0; it < 3; it++) {
+        double dev = 0.0;
+        if (g.j < n) {  // M = X^T X
+            for (int i = g.h; i < n; i += g.G) {
+                double v = 0.0;
+                for (int k = 0; k < n; k++) v = ::fma(sm.X[k * ld + i], sm.X[k * ld + g.j], v);
+                M[i * ld + g.j] = v;
+                const double e = v - (i == g.j ? 1.0 : 0.0);
+                dev += e * e;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) dev += __shfl_xor_sync(0xffffffffu, dev, o);
+        __syncwarp();
+        if (dev <= 1e-28) break;
+        if (g.j < n) {  // Y = X (3I - M) / 2
+            for (int i = g.h; i < n; i += g.G) {
+                double v = 1.5 * sm.X[i * ld + g.j];
+                for (int k = 0; k < n; k++) v = ::fma(-0.5 * sm.X[i * ld + k], M[k * ld + g.j], v);
+                Y[i * ld + g.j] = v;
+            }
+        }
+        __syncwarp();
+        if (g.j < n)
+            for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = Y[i * ld + g.j];
+        __syncwarp();
+    }
+    if (g.j < n) {  // Y = A X
         for (int i = g.h; i < n; i += g.G) {
             double y = 0.0;
             for (int k = 0; k < n; k++) y = ::fma(sm.A64[i * ld + k], sm.X[k * ld + g.j], y);
@@ -392,11 +424,11 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
         }
     }
     __syncwarp();
-    jacobi_warp<double>(sm.A64, Wm, sm.cs64, sm.pq, n, ld, 1e-28, 8);
+    jacobi_warp<double>(sm.A64, M, sm.cs64, sm.pq, n, ld, 1e-28, 8);
     if (g.j < n) {  // X <- X W (through Y)
         for (int i = g.h; i < n; i += g.G) {
             double v = 0.0;
-            for (int k = 0; k < n; k++) v = ::fma(sm.X[i * ld + k], Wm[k * ld + g.j], v);
+            for (int k = 0; k < n; k++) v = ::fma(sm.X[i * ld + k], M[k * ld + g.j], v);
             Y[i * ld + g.j] = v;
         }
     }
