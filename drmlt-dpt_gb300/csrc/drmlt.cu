@@ -127,6 +127,8 @@ struct Renderer {
         p.accMap = opt.acceptance_map;
         p.maxDerv = opt.max_derivative_depth;
         p.gaussDim = std::min(2 * opt.max_depth, kMaxDim);
+        p.lanes = opt.stage_lanes > 0 ? std::min(opt.stage_lanes, 32) : 16;
+        p.derivWarps = opt.deriv_warps > 0 ? std::min(opt.deriv_warps, 4) : 2;
         p.seed = opt.seed;
         return p;
     }
@@ -323,7 +325,7 @@ struct Renderer {
         if ((rc = alloc(&cv.listX, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listS, size_t(N)))) return rc;
-        G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 4;
+        G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 1;
         G = std::min(G, N);
         chunk = (N + G - 1) / G;
         G = (N + chunk - 1) / chunk;
@@ -470,7 +472,8 @@ struct Renderer {
     int launch_stage(int k, int g, int iter, cudaStream_t s) const {
         const RunParams p = params(g);
         const int nb = (p.N + kStageBlock - 1) / kStageBlock;
-        const int nbWarp = (p.N * 32 + 127) / 128;
+        const int nbS = sparse_blocks(p.N, p.lanes);
+        const int nbWarp = (p.N * 32 * p.derivWarps + 127) / 128;
         const int nbG = (p.N + kGaussWarps - 1) / kGaussWarps;
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
         switch (k) {
@@ -478,16 +481,16 @@ struct Renderer {
                 k_reset_counters<<<1, 128, 0, s>>>(p.d.counters, p.d.hist);
                 k_plan<<<nb, kStageBlock, 0, s>>>(p, iter);
                 k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
-                k_stage1<<<nb, kStageBlock, 0, s>>>(p, iter);
+                k_stage1<<<nbS, kStageBlock, 0, s>>>(p, iter);
                 return 4;
             case 1: k_derivs<<<nbWarp, 128, 0, s>>>(p, 0); return 1;
             case 2: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 0); return 1;
-            case 3: k_stage2<<<nb, kStageBlock, 0, s>>>(p, iter); return 1;
+            case 3: k_stage2<<<nbS, kStageBlock, 0, s>>>(p, iter); return 1;
             case 4: k_derivs<<<nbWarp, 128, 0, s>>>(p, 2); return 1;
             case 5: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 2); return 1;
             default:
-                if (p.drType == 0) k_ystar<<<nb, kStageBlock, 0, s>>>(p, iter);
-                k_finish<<<nb, kStageBlock, 0, s>>>(p, iter);
+                if (p.drType == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p, iter);
+                k_finish<<<nbS, kStageBlock, 0, s>>>(p, iter);
                 return p.drType == 0 ? 2 : 1;
         }
     }
@@ -605,6 +608,8 @@ void drmlt_default_options(drmlt_options *o) {
     o->device = 0;
     o->use_graph = 0;
     o->chain_groups = 0;
+    o->stage_lanes = 0;
+    o->deriv_warps = 0;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }

@@ -229,9 +229,8 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
 // FP64-accumulated residuals of an approximate eigen-decomposition (X, lam):
 // Z = A X - X diag(lam) into sm.A32 and, unless skipR, R = I - X^T X into
 // sm.R32. Both are ~1e-7 or smaller, so FP32 storage keeps their accuracy; the
-// sums cancel and run in FP64. Returns |Z|_F^2. fromFloat: X is sm.V32 (then
-// every product is exact in FP64), else sm.X.
-DEV double eigen_residuals(GaussSmem &sm, int n, bool fromFloat, bool skipR) {
+// sums cancel and run in FP64. X is sm.X. Returns |Z|_F^2.
+DEV double eigen_residuals(GaussSmem &sm, int n, bool skipR) {
     const LaneGrid g(n);
     const int ld = sm.ld;
     const double *A = sm.A64;
@@ -239,14 +238,14 @@ DEV double eigen_residuals(GaussSmem &sm, int n, bool fromFloat, bool skipR) {
     if (g.j < n) {
         const double lj = sm.lam[g.j];
         for (int i = g.h; i < n; i += g.G) {
-            const double xij = fromFloat ? double(sm.V32[i * ld + g.j]) : sm.X[i * ld + g.j];
+            const double xij = sm.X[i * ld + g.j];
             double z = -xij * lj;
             double r = i == g.j ? 1.0 : 0.0;
             for (int k = 0; k < n; k++) {
-                const double xkj = fromFloat ? double(sm.V32[k * ld + g.j]) : sm.X[k * ld + g.j];
+                const double xkj = sm.X[k * ld + g.j];
                 z = ::fma(A[i * ld + k], xkj, z);
                 if (!skipR) {
-                    const double xki = fromFloat ? double(sm.V32[k * ld + i]) : sm.X[k * ld + i];
+                    const double xki = sm.X[k * ld + i];
                     r = ::fma(-xki, xkj, r);
                 }
             }
@@ -278,10 +277,10 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
     const int ld = sm.ld;
     const double tol2 = 1e-22 * froA * froA;
     if (lane < n) sm.lam[lane] = double(sm.l32[lane]);
-    __syncwarp();
-    eigen_residuals(sm, n, true, false);
     if (g.j < n)
         for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = double(sm.V32[i * ld + g.j]);
+    __syncwarp();
+    eigen_residuals(sm, n, false);
     double *lamNew = sm.cs64;
     for (int step = 0; step < 2; step++) {
         const float *X32 = sm.V32;
@@ -340,7 +339,7 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
         if (lane < n) sm.lam[lane] = lamNew[lane];
         __syncwarp();
         // certificate: FP64 residual of the refined pairs (also the next step's Z)
-        const double res = eigen_residuals(sm, n, false, true);
+        const double res = eigen_residuals(sm, n, true);
         if (res <= tol2) return true;  // false for NaN
         if (step == 1) break;
         if (g.j < n)

@@ -92,10 +92,27 @@ struct RunParams {
     int accMap;
     int maxDerv;
     int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch
+    int lanes;           // chains per warp in the per-chain stage kernels (1..32)
+    int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
     unsigned long long seed;
 };
 
 constexpr int kStageBlock = 64;  // threads per block of the per-chain stage kernels
+
+// The per-chain stage kernels put `lanes` chains on each warp and leave the
+// other lanes idle. Lanes of a warp that trace different paths serialise, and
+// at these chain counts the GPU has room for far more warps than there are
+// chains per 32, so fewer chains per warp shortens every warp's run.
+DEV int sparse_index(int lanes, bool &active) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    active = lane < lanes;
+    return warp * lanes + lane;
+}
+inline int sparse_blocks(int n, int lanes) {
+    const int warps = (n + lanes - 1) / lanes;
+    return (warps + kStageBlock / 32 - 1) / (kStageBlock / 32);
+}
 
 // ------------------------------------------------------------- reference lambdas
 DEV bool flip_coin(float x, float d) { return (x == 1.0f) || (d < x); }      // delayed.cpp:250
@@ -225,9 +242,10 @@ static_assert(2 * kScatterBlock == kPlanBins, "k_scatter scans two bins per thre
 
 // ------------------------------------------------------------- stage 1
 __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool on;
+    const int t = sparse_index(p.lanes, on);
     StatAcc acc;
-    if (t < p.N) {
+    if (on && t < p.N) {
         const int i = p.d.order[t];
         Scratch &sc = p.d.scr[i];
         int flags = 0;
@@ -311,17 +329,18 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
 // ------------------------------------------------------------- derivatives
 // One warp per listed chain: lanes stride over the D(D+1)/2 Hessian entries.
 // which: 0 = current state, 2 = second proposal.
-__device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H) {
-    const int lane = threadIdx.x & 31;
+__device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H,
+                                int member = threadIdx.x & 31, int team = 32) {
+    const int lane = member;
     const int L = r.c + r.l - 1;
     const int dim = 2 * L;
     if (!(L <= maxDerv && ss > 1e-15f)) {
-        for (int k = lane; k < dim; k += 32) g[k] = 0.0f;
-        for (int k = lane; k < dim * dim; k += 32) H[k] = 0.0f;
+        for (int k = lane; k < dim; k += team) g[k] = 0.0f;
+        for (int k = lane; k < dim * dim; k += team) H[k] = 0.0f;
         return;
     }
     const int npairs = dim * (dim + 1) / 2;
-    for (int pidx = lane; pidx < npairs; pidx += 32) {
+    for (int pidx = lane; pidx < npairs; pidx += team) {
         // decode pidx -> (i0, j0), i0 <= j0, row-major over the upper triangle
         int i0 = 0, rem = pidx;
         while (rem >= dim - i0) {
@@ -339,14 +358,17 @@ __device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, 
     }
 }
 
+// A team of p.derivWarps warps per listed chain shares its Hessian entries.
 __global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int w = gw / p.derivWarps;
     const int n = p.d.counters[which == 0 ? 0 : 1];
     if (w >= n) return;
     const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
     const Slot &st = slot_of(p.d, chain, which);
     derivs_for_path(p.s, st.rec, st.ss, p.maxDerv, p.d.grad + size_t(w) * kMaxDim,
-                    p.d.hess + size_t(w) * kMaxDim * kMaxDim);
+                    p.d.hess + size_t(w) * kMaxDim * kMaxDim, (gw % p.derivWarps) * 32 + (threadIdx.x & 31),
+                    32 * p.derivWarps);
 }
 
 // One warp per listed chain; 4 warps per block, each with its own slice of
@@ -379,8 +401,9 @@ __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int whi
 // ------------------------------------------------------------- stage 2 proposal
 // Over the group's second-stage list only (compacted by k_stage1).
 __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.d.counters[2]) return;
+    bool on;
+    const int t = sparse_index(p.lanes, on);
+    if (!on || t >= p.d.counters[2]) return;
     const int i = p.d.listS[t];
     Scratch &sc = p.d.scr[i];
     Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
@@ -427,8 +450,9 @@ __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
 // Green's reverse path y* = z + (x - y) and its first-stage acceptance from z
 // (SmallStep::Trace, mutation.cpp:210-238), over the second-stage list only.
 __global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p, int iter) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.d.counters[2]) return;
+    bool on;
+    const int t = sparse_index(p.lanes, on);
+    if (!on || t >= p.d.counters[2]) return;
     const int i = p.d.listS[t];
     Scratch &sc = p.d.scr[i];
     const Slot &cur = slot_of(p.d, i, 0);
@@ -459,10 +483,11 @@ DEV double iso_quad(int dim, const float *a, const float *b) {
 
 // ------------------------------------------------------------- finish
 __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p, int iter) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool on;
+    const int t = sparse_index(p.lanes, on);
     const int i = p.c0 + t;
     StatAcc acc;
-    if (t < p.N && (p.d.scr[i].flags & kActive)) {
+    if (on && t < p.N && (p.d.scr[i].flags & kActive)) {
         Scratch &sc = p.d.scr[i];
         const int flags = sc.flags;
         const float a1 = sc.a1;
