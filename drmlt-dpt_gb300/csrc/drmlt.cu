@@ -161,6 +161,20 @@ struct Renderer {
             return fail(DRMLT_E_CUDA, "no CUDA device available");
         CK(cudaSetDevice(opt.device));
         if (int rc = gauss_kernels_setup()) return rc;
+        if (opt.smem_carveout >= 0) {
+            // one shared-memory carveout for every chain-loop kernel, so that
+            // kernels of different stages can share an SM
+            const int c = std::min(opt.smem_carveout, 100);
+            CK(cudaFuncSetAttribute(k_reset_counters, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_plan, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_scatter, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_stage1, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_derivs, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_gauss, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_stage2, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_ystar, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(cudaFuncSetAttribute(k_finish, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+        }
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         CK(cudaEventCreate(&ev0));
         CK(cudaEventCreate(&ev1));
@@ -610,6 +624,7 @@ void drmlt_default_options(drmlt_options *o) {
     o->chain_groups = 0;
     o->stage_lanes = 0;
     o->deriv_warps = 0;
+    o->smem_carveout = -1;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }

@@ -546,16 +546,19 @@ DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const flo
     return kind;
 }
 
-// GaussianLogPdf (src/gaussian.cpp:18-26) in FP64.
-DEV double gauss_logpdf(int dim, const double *offset, GaussView g) {
-    double d[kMaxDim];
-    for (int i = 0; i < dim; i++) d[i] = offset[i] - g.mean[i];
+
+// GaussianLogPdf (src/gaussian.cpp:18-26) in FP64 of sign * off (off: dim
+// floats) with one warp: lane k
+// projects the offset on eigenvector k, the lanes' terms are summed by shuffles.
+DEV double gauss_logpdf_warp(int dim, const float *off, double sign, GaussView g) {
+    const int lane = threadIdx.x & 31;
     double quad = 0.0;
-    for (int k = 0; k < dim; k++) {
+    if (lane < dim) {
         double proj = 0.0;
-        for (int i = 0; i < dim; i++) proj += g.V[i * dim + k] * d[i];
-        quad += g.p[k] * proj * proj;
+        for (int i = 0; i < dim; i++) proj = ::fma(g.V[i * dim + lane], sign * double(off[i]) - g.mean[i], proj);
+        quad = g.p[lane] * proj * proj;
     }
+    for (int o = 16; o > 0; o >>= 1) quad += __shfl_xor_sync(0xffffffffu, quad, o);
     return double(dim) * (-0.5 * ::log(2.0 * 3.14159265358979323846)) + 0.5 * (*g.logDet) - 0.5 * quad;
 }
 

@@ -40,6 +40,7 @@ struct Scratch {
     int flags;
     int key, rank;      // stage-1 work class and rank within it (k_plan)
     float aStar;        // Green's reverse first-stage acceptance (k_ystar)
+    double logRatio;    // H2MC: log N_z(-o) - log N_x(o) (k_gauss at z)
     float offset[kMaxDim];
 };
 
@@ -391,6 +392,14 @@ __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int whi
     const int kind = compute_gaussian_warp(dim, H2mcParam(p.sigma1), dim <= sm.m ? st.ss : 0.0f,
                                            p.d.grad + size_t(w) * kMaxDim, p.d.hess + size_t(w) * kMaxDim * kMaxDim, sm,
                                            GaussView(gauss_of(p.d, chain, which)));
+    if (which == 2) {
+        // the H2MC kernel ratio of PH2MCSmallStep::Mutate (drsmallstep.cpp:191-196), FP64
+        Scratch &sc = p.d.scr[chain];
+        const int d = dim <= sm.m ? dim : 0;
+        const double px = gauss_logpdf_warp(d, sc.offset, -1.0, GaussView(gauss_of(p.d, chain, 2)));
+        const double py = gauss_logpdf_warp(d, sc.offset, 1.0, GaussView(gauss_of(p.d, chain, 0)));
+        if ((threadIdx.x & 31) == 0) sc.logRatio = px - py;
+    }
     if ((threadIdx.x & 31) == 0) {
         st.gaussInit = 1;
         if (kind != kGaussIsotropic) atomicAdd(&p.d.stats[kStatGauss], 1ull);
@@ -502,14 +511,7 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p, int iter) {
             const int dim = path_dim(cur.rec.c, cur.rec.l);
             if (aniso) {
                 if (flags & kZValid) {
-                    double o[kMaxDim], mo[kMaxDim];
-                    for (int k = 0; k < dim; k++) {
-                        o[k] = double(sc.offset[k]);
-                        mo[k] = -o[k];
-                    }
-                    const double py = gauss_logpdf(dim, o, GaussView(gauss_of(p.d, i, 0)));
-                    const double px = gauss_logpdf(dim, mo, GaussView(gauss_of(p.d, i, 2)));
-                    a2 = float(::exp(px - py)) * S.ss / cur.ss;
+                    a2 = float(::exp(sc.logRatio)) * S.ss / cur.ss;
                 } else {
                     a2 = 0.0f;
                 }

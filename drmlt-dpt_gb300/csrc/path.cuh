@@ -399,6 +399,7 @@ DEV void make_rec(const FullPath &f, int c, int l, PathRec &r) {
         r.u[k++] = f.lgtPos[1];
         r.u[k++] = f.lgtDir[0];
         r.u[k++] = f.lgtDir[1];
+        #pragma unroll 1
         for (int i = 0; i < nl - 1; i++) {
             r.u[k++] = f.lgt[i].rnd[0];
             r.u[k++] = f.lgt[i].rnd[1];
@@ -407,6 +408,7 @@ DEV void make_rec(const FullPath &f, int c, int l, PathRec &r) {
     if (c > 1) {
         r.u[k++] = f.screen[0];
         r.u[k++] = f.screen[1];
+        #pragma unroll 1
         for (int i = 0; i < nc - 1; i++) {
             r.u[k++] = f.cam[i].rnd[0];
             r.u[k++] = f.cam[i].rnd[1];
@@ -416,12 +418,14 @@ DEV void make_rec(const FullPath &f, int c, int l, PathRec &r) {
             r.u[k++] = lastCam->dl[1];
         }
     }
+    #pragma unroll 1
     for (int i = 0; i < nl; i++) {
         r.tri[i] = f.lgt[i].tri;
         r.disc[i] = f.lgt[i].disc;
         r.rr[i] = f.lgt[i].rr;
         if (f.lgt[i].useAbs) r.useAbs |= 1u << i;
     }
+    #pragma unroll 1
     for (int i = 0; i < nc; i++) {
         r.tri[nl + i] = f.cam[i].tri;
         r.disc[nl + i] = f.cam[i].disc;
@@ -452,6 +456,7 @@ DEV void generate_path_bidir(const SceneView &s, int minDepth, int maxDepth, R &
     emit_from_light(s, pickProb, f.lgtLight, f.lgtPrim, f.lgtPos, f.lgtDir, org, dir, lps[0]);
     f.nLgt = 0;
     int nStates = 1;
+    #pragma unroll 1
     for (int d = 0; d < kMaxFull - 1; d++) {
         SVert &v = f.lgt[d];
         clear_vert(v);
@@ -495,6 +500,7 @@ DEV void generate_path_bidir(const SceneView &s, int minDepth, int maxDepth, R &
     float minT, maxT;
     emit_from_camera(s, f.screen[0], f.screen[1], org, dir, minT, maxT, cp);
     f.nCam = 0;
+    #pragma unroll 1
     for (int d = 0; d < kMaxFull; d++) {
         SVert &v = f.cam[d];
         clear_vert(v);
@@ -528,6 +534,7 @@ DEV void generate_path_bidir(const SceneView &s, int minDepth, int maxDepth, R &
             if (direct_lighting(s, d, cp, f.screen[0], f.screen[1], dlPick, v, e)) sink(e);
         }
         const int maxLgtDepth = maxDepth == -1 ? (nStates - 1) : min(maxDepth - d - 3, nStates - 1);
+        #pragma unroll 1
         for (int ld = 0; ld <= maxLgtDepth; ld++) {
             if (d + ld + 3 >= minDepth) {
                 Emit e;
@@ -569,6 +576,7 @@ DEV bool generate_subpath(const SceneView &s, int camLength, int lgtLength, R &r
         const float ud = rng.uniform();
         f.lgtPrim = L.type == kLightArea ? sample_discrete(s.lightTriCdf + L.triCdfOffset, L.numTris, ud) : -1;
         emit_from_light(s, pickProb, f.lgtLight, f.lgtPrim, f.lgtPos, f.lgtDir, org, dir, lp);
+        #pragma unroll 1
         for (int d = 0; d < kMaxFull; d++) {
             SVert &v = f.lgt[d];
             clear_vert(v);
@@ -602,6 +610,7 @@ DEV bool generate_subpath(const SceneView &s, int camLength, int lgtLength, R &r
     zero_state(cp);
     float minT, maxT;
     emit_from_camera(s, f.screen[0], f.screen[1], org, dir, minT, maxT, cp);
+    #pragma unroll 1
     for (int d = 0; d < kMaxFull; d++) {
         SVert &v = f.cam[d];
         clear_vert(v);
@@ -676,6 +685,7 @@ DEV bool perturb_path(const SceneView &s, const PathRec &in, const float *offset
         const float dirp[2] = {out.u[2], out.u[3]};
         V3 org, dir;
         emit_from_light(s, pickProb, in.lgtLight, in.lgtPrim, pos, dirp, org, dir, lp);
+        #pragma unroll 1
         for (int d = 0; d < nl; d++) {
             SVert v;
             clear_vert(v);
@@ -717,6 +727,7 @@ DEV bool perturb_path(const SceneView &s, const PathRec &in, const float *offset
     zero_state(cp);
     emit_from_camera(s, sx, sy, org, dir, minT, maxT, cp);
     bool lightCoords = false;
+    #pragma unroll 1
     for (int d = 0; d < nc; d++) {
         const int vi = nl + d;
         SVert v;
@@ -786,6 +797,7 @@ DEV void generate_path_direct(const SceneView &s, int px, int py, int minDepth, 
     sample_primary(s.cam, sx, sy, org, dir, minT, maxT);
     V3 throughput(1.0f, 1.0f, 1.0f);
     float lastBsdfPdf = 1.0f;
+    #pragma unroll 1
     for (int d = 0; d < 8; d++) {
         Isect isect;
         int tri = -1;

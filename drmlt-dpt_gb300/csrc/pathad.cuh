@@ -385,6 +385,7 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
         lp.throughput = lp.throughput * (1.0f / pick);
         lp.prev = tmis(directPdf / emissionPdf);
         lp.cur = L.type == kLightPoint ? tmis(cosLight / emissionPdf) : T(0.0f);
+        #pragma unroll 1
         for (int d = 0; d < nl; d++) {
             const int tri = r.tri[d];
             ad_intersect(s, tri, org, dir, lp.isect);
@@ -445,6 +446,7 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
             cp.prev = tmis(pixelCount / cameraPdf);
             cp.cur = T(0.0f);
         }
+        #pragma unroll 1
         for (int d = 0; d < nc; d++) {
             const int vi = nl + d;
             const int tri = r.tri[vi];

@@ -114,6 +114,8 @@ typedef struct drmlt_options {
                                      CUDA stream so the groups' kernels overlap (0 = default, 1) */
     int32_t stage_lanes;          /* chains per warp in the per-chain stage kernels, 1..32 (0 = 16) */
     int32_t deriv_warps;          /* warps sharing one chain's Hessian entries, 1..4 (0 = 2) */
+    int32_t smem_carveout;        /* shared-memory carveout (percent) for every chain-loop kernel,
+                                     -1 = the driver's choice per kernel */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
