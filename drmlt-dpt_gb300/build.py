@@ -1,4 +1,5 @@
-"""Builds libdrmlt.so in-tree for sm_103a (nvcc, one translation unit + the host BVH builder).
+"""Builds libdrmlt.so in-tree for sm_103a (nvcc: the chain-loop translation unit, the
+path-derivative translation unit and the host BVH builder, compiled in parallel).
 
 usage: python drmlt-dpt_gb300/build.py [--force]
 """
@@ -16,6 +17,10 @@ LIB = os.path.join(LIBDIR, "libdrmlt.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I" + os.path.join(REPO, "include")]
+# The derivative kernel is instruction-fetch bound on its long hyper-dual code;
+# fast-math intrinsics keep the transcendental calls short. Its outputs are
+# derivatives (checked to 1e-3) and never a path contribution.
+TU_FLAGS = {"derivs.cu": ["--use_fast_math"]}
 
 
 def _sources():
@@ -35,9 +40,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     objs = []
     jobs = []
-    for src in ("drmlt.cu", "bvh.cpp"):
+    for src in ("drmlt.cu", "derivs.cu", "bvh.cpp"):
         obj = os.path.join(LIBDIR, src + ".o")
-        cmd = [NVCC] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [NVCC] + ARCH + FLAGS + TU_FLAGS.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             cmd = [NVCC] + ARCH + FLAGS + ["-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT))

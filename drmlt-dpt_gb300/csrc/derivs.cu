@@ -1,0 +1,78 @@
+// Path derivatives for H2MC: gradient and Hessian of log f with respect to the
+// primary sample coordinates (the chad-generated evaluate_path_bidir_*_derv of
+// the reference, registered in src/path.cpp:2987-3175), by hyper-dual forward
+// mode on the AD path function of pathad.cuh.
+#include "chain.cuh"
+#include "derivs.h"
+
+namespace drmlt {
+
+// One warp per listed chain: lanes stride over the D(D+1)/2 Hessian entries.
+// which: 0 = current state, 2 = second proposal.
+__device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H,
+                                int member = threadIdx.x & 31, int team = 32) {
+    const int lane = member;
+    const int L = r.c + r.l - 1;
+    const int dim = 2 * L;
+    if (!(L <= maxDerv && ss > 1e-15f)) {
+        for (int k = lane; k < dim; k += team) g[k] = 0.0f;
+        for (int k = lane; k < dim * dim; k += team) H[k] = 0.0f;
+        return;
+    }
+    const int npairs = dim * (dim + 1) / 2;
+    for (int pidx = lane; pidx < npairs; pidx += team) {
+        // decode pidx -> (i0, j0), i0 <= j0, row-major over the upper triangle
+        int i0 = 0, rem = pidx;
+        while (rem >= dim - i0) {
+            rem -= dim - i0;
+            i0++;
+        }
+        const int j0 = i0 + rem;
+        HyperDual u[kMaxDim];
+        for (int k = 0; k < dim; k++)
+            u[k] = HyperDual(r.u[k], k == i0 ? 1.0f : 0.0f, k == j0 ? 1.0f : 0.0f, 0.0f);
+        const HyperDual f = ad_eval_path<HyperDual>(s, r, u);
+        H[i0 * dim + j0] = f.ab;
+        H[j0 * dim + i0] = f.ab;
+        if (i0 == j0) g[i0] = f.a;
+    }
+}
+
+// A team of p.derivWarps warps per listed chain shares its Hessian entries.
+__global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int w = gw / p.derivWarps;
+    const int n = p.d.counters[which == 0 ? 0 : 1];
+    if (w >= n) return;
+    const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
+    const Slot &st = slot_of(p.d, chain, which);
+    derivs_for_path(p.s, st.rec, st.ss, p.maxDerv, p.d.grad + size_t(w) * kMaxDim,
+                    p.d.hess + size_t(w) * kMaxDim * kMaxDim, (gw % p.derivWarps) * 32 + (threadIdx.x & 31),
+                    32 * p.derivWarps);
+}
+
+__global__ void __launch_bounds__(128) k_gradhess_paths(SceneView s, const PathRec *paths, const float *u, int n,
+                                                        float *grad, float *hess) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= n) return;
+    PathRec r = paths[w];
+    const int dim = path_dim(r.c, r.l);
+    for (int k = 0; k < dim; k++) r.u[k] = u[size_t(w) * kMaxDim + k];
+    // derivatives are always taken here (no ss / depth gate)
+    derivs_for_path(s, r, 1.0f, kMaxLen, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim);
+}
+
+void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s) {
+    k_derivs<<<blocks, 128, 0, s>>>(p, which);
+}
+
+void launch_gradhess_paths(const SceneView &s, const PathRec *paths, const float *u, int n, float *grad,
+                           float *hess, cudaStream_t st) {
+    k_gradhess_paths<<<(n * 32 + 127) / 128, 128, 0, st>>>(s, paths, u, n, grad, hess);
+}
+
+cudaError_t set_derivs_carveout(int percent) {
+    return cudaFuncSetAttribute(k_derivs, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+}
+
+}  // namespace drmlt

@@ -1,0 +1,20 @@
+// Host launchers of the path-derivative kernels, which are compiled in their
+// own translation unit (derivs.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace drmlt {
+
+struct RunParams;
+struct SceneView;
+struct PathRec;
+
+// Gradient + Hessian of log f for the chains of list `which` (0: listX at the
+// current states, 2: listZ at the second proposals) of one chain group.
+void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s);
+// The same for caller-supplied paths and primary samples (u: n x kMaxDim).
+void launch_gradhess_paths(const SceneView &s, const PathRec *paths, const float *u, int n, float *grad,
+                           float *hess, cudaStream_t st);
+cudaError_t set_derivs_carveout(int percent);
+
+}  // namespace drmlt

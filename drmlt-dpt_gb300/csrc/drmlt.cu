@@ -169,7 +169,7 @@ struct Renderer {
             CK(cudaFuncSetAttribute(k_plan, cudaFuncAttributePreferredSharedMemoryCarveout, c));
             CK(cudaFuncSetAttribute(k_scatter, cudaFuncAttributePreferredSharedMemoryCarveout, c));
             CK(cudaFuncSetAttribute(k_stage1, cudaFuncAttributePreferredSharedMemoryCarveout, c));
-            CK(cudaFuncSetAttribute(k_derivs, cudaFuncAttributePreferredSharedMemoryCarveout, c));
+            CK(set_derivs_carveout(c));
             CK(cudaFuncSetAttribute(k_gauss, cudaFuncAttributePreferredSharedMemoryCarveout, c));
             CK(cudaFuncSetAttribute(k_stage2, cudaFuncAttributePreferredSharedMemoryCarveout, c));
             CK(cudaFuncSetAttribute(k_ystar, cudaFuncAttributePreferredSharedMemoryCarveout, c));
@@ -497,10 +497,10 @@ struct Renderer {
                 k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
                 k_stage1<<<nbS, kStageBlock, 0, s>>>(p, iter);
                 return 4;
-            case 1: k_derivs<<<nbWarp, 128, 0, s>>>(p, 0); return 1;
+            case 1: launch_derivs(p, 0, nbWarp, s); return 1;
             case 2: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 0); return 1;
             case 3: k_stage2<<<nbS, kStageBlock, 0, s>>>(p, iter); return 1;
-            case 4: k_derivs<<<nbWarp, 128, 0, s>>>(p, 2); return 1;
+            case 4: launch_derivs(p, 2, nbWarp, s); return 1;
             case 5: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 2); return 1;
             default:
                 if (p.drType == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p, iter);

@@ -1,187 +1,21 @@
 // Device kernels of the DRMLT chain loop (delayed.cpp:334-673), its prepass
 // (delayed.cpp:14-173) and the direct-lighting pass (integrator.h:33-75).
 //
-// One thread owns one Markov chain in the stage kernels. Each iteration runs
+// Each iteration runs, per chain (16 chains per warp by default in the stage kernels):
+//   plan/scatter  order the chains by stage-1 work class (technique)
 //   stage1   coin flips, large step or isotropic small step, first acceptance
 //   derivs   gradient + Hessian of log f for chains that need a Gaussian at x
-//            (one warp per chain, one Hessian entry per lane and pass)
-//   gauss    FP64 eigen-decomposition + H2MC Gaussian (one thread per chain)
+//            (a team of warps per chain, one Hessian entry per lane and pass; derivs.cu)
+//   gauss    H2MC Gaussian, FP32 Jacobi refined to FP64 (one warp per chain)
 //   stage2   second-stage proposal z (H2MC sample or isotropic sigma2)
-//   derivs + gauss at z for H2MC proposals
-//   finish   Green (y* trace) or Mira acceptance, weighted splats, state swap
-// Chain states live in HBM as three slots per chain (current, first proposal,
-// second proposal) addressed through a per-chain permutation, so accepting a
-// proposal swaps two indices instead of copying a state.
+//   derivs + gauss at z for H2MC proposals, with the FP64 log-density ratio
+//   ystar    Green's reverse path y* (second-stage chains only)
+//   finish   Green or Mira acceptance, weighted splats, state swap
 #pragma once
-#include "pathad.cuh"
-#include "gauss.cuh"
+#include "chain.cuh"
+#include "derivs.h"
 
 namespace drmlt {
-
-// MarkovState (src/mutation.h:38-59): path, its contribution and one
-// toSplat entry (screen, rgb value = contrib * b / ls).
-struct Slot {
-    PathRec rec;
-    float screen[2];
-    float rgb[3];
-    float ls, ss;
-    float splat[5];
-    int hasSplat;
-    int valid;
-    int gaussInit;
-};
-
-enum : int {
-    kActive = 1, kAccept1 = 2, kLarge = 4, kSecond = 8, kAniso = 16, kZValid = 32, kAccept2 = 64
-};
-
-struct Scratch {
-    float a1, a2;
-    int flags;
-    int key, rank;      // stage-1 work class and rank within it (k_plan)
-    float aStar;        // Green's reverse first-stage acceptance (k_ystar)
-    double logRatio;    // H2MC: log N_z(-o) - log N_x(o) (k_gauss at z)
-    float offset[kMaxDim];
-};
-
-// Stage-1 work classes: 0 idle chain; 1 + 14 c + l small step of technique
-// (c, l); 200 + 14 L + lgtLength large step of sampled length L.
-constexpr int kPlanBins = 512;
-
-enum : int {
-    kStatLarge = 0, kStatLargeAcc, kStatStage1, kStatStage1Acc, kStatIso, kStatIsoAcc, kStatH2mc,
-    kStatH2mcAcc, kStatMutations, kStatGauss, kStatGaussFallback, kNumStats
-};
-
-struct ChainView {
-    Slot *slots;        // N x 3
-    double *gauss;      // N x 3 x kGaussStride
-    int *perm;          // N x 3: slot of (current, first, second)
-    Scratch *scr;       // N
-    int *listX;         // chains needing a Gaussian at the current state
-    int *listZ;         // chains needing a Gaussian at the second proposal
-    int *listS;         // chains taking a second stage this iteration
-    int *order;         // stage-1 processing order (chains grouped by work class)
-    int *hist;          // kPlanBins counters of the work classes
-    int *counters;      // [0] = |listX|, [1] = |listZ|, [2] = |listS|
-    float *grad;        // N x kMaxDim (indexed by list position)
-    float *hess;        // N x kMaxDim^2
-    unsigned long long *stats;
-    float *film;        // W x H x 3 (indirect)
-    float *direct;      // W x H x 3
-    const float *lengthCdf;
-    const float *lengthFunc;
-    int lengthCount;
-    float lengthFuncInt;
-};
-
-// One launch covers one chain group: chains c0 .. c0 + N - 1. The lists,
-// counters and gradient/Hessian rows in `d` are the group's own slices.
-struct RunParams {
-    SceneView s;
-    ChainView d;
-    int N;
-    int c0;
-    long long samplesPerChain;
-    long long extraChains;
-    float b;
-    float sigma1, sigma2;
-    float largeProb, anisoProb;
-    int drType;          // 0 green, 1 mira
-    int integrator;      // 0 drmlt, 1 h2mc, 2 mcmc
-    float uniformMix;
-    int accMap;
-    int maxDerv;
-    int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch
-    int lanes;           // chains per warp in the per-chain stage kernels (1..32)
-    int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
-    unsigned long long seed;
-};
-
-constexpr int kStageBlock = 64;  // threads per block of the per-chain stage kernels
-
-// The per-chain stage kernels put `lanes` chains on each warp and leave the
-// other lanes idle. Lanes of a warp that trace different paths serialise, and
-// at these chain counts the GPU has room for far more warps than there are
-// chains per 32, so fewer chains per warp shortens every warp's run.
-DEV int sparse_index(int lanes, bool &active) {
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    active = lane < lanes;
-    return warp * lanes + lane;
-}
-inline int sparse_blocks(int n, int lanes) {
-    const int warps = (n + lanes - 1) / lanes;
-    return (warps + kStageBlock / 32 - 1) / (kStageBlock / 32);
-}
-
-// ------------------------------------------------------------- reference lambdas
-DEV bool flip_coin(float x, float d) { return (x == 1.0f) || (d < x); }      // delayed.cpp:250
-DEV float metropolis_clamp(float x) { return x < 1.0f ? x : 1.0f; }         // std::min(1.0f, x)
-DEV bool is_invalid(float x) { return isnan(x) || isinf(x) || x < 0.0f; }   // delayed.cpp:252
-DEV float clamp01(float x) {                                                 // Clamp(x, 0, 1)
-    const float t = (x < 0.0f) ? 0.0f : x;
-    return (1.0f < t) ? 1.0f : t;
-}
-
-DEV Slot &slot_of(const ChainView &d, int chain, int which) { return d.slots[3 * chain + d.perm[3 * chain + which]]; }
-DEV double *gauss_of(const ChainView &d, int chain, int which) {
-    return d.gauss + size_t(3 * chain + d.perm[3 * chain + which]) * kGaussStride;
-}
-
-DEV void set_contrib(Slot &st, const Emit &e, float b) {
-    st.screen[0] = e.screen[0];
-    st.screen[1] = e.screen[1];
-    st.rgb[0] = e.rgb.x;
-    st.rgb[1] = e.rgb.y;
-    st.rgb[2] = e.rgb.z;
-    st.ls = e.ls;
-    st.ss = e.ss;
-    const float w = b / e.ls;
-    st.splat[0] = e.screen[0];
-    st.splat[1] = e.screen[1];
-    st.splat[2] = e.rgb.x * w;
-    st.splat[3] = e.rgb.y * w;
-    st.splat[4] = e.rgb.z * w;
-    st.hasSplat = 1;
-}
-
-// Splat (src/image.h:65-74): nearest pixel, finite values only.
-DEV void splat(float *film, int W, int H, float sx, float sy, float r, float g, float b) {
-    if (r == 0.0f && g == 0.0f && b == 0.0f) return;
-    if (!(isfinite(r) && isfinite(g) && isfinite(b))) return;
-    int ix = int(sx * float(W));
-    int iy = int(sy * float(H));
-    ix = ix < 0 ? 0 : (ix > W - 1 ? W - 1 : ix);
-    iy = iy < 0 ? 0 : (iy > H - 1 ? H - 1 : iy);
-    float *px = film + 3 * (size_t(iy) * W + ix);
-    atomicAdd(px, r);
-    atomicAdd(px + 1, g);
-    atomicAdd(px + 2, b);
-}
-
-// Block-aggregated statistics: one global atomic per counter per block.
-struct StatAcc {
-    unsigned c[kNumStats];
-    DEV StatAcc() {
-        for (int k = 0; k < kNumStats; k++) c[k] = 0u;
-    }
-};
-DEV void flush_stats(const StatAcc &acc, unsigned long long *global) {
-    __shared__ unsigned sh[kNumStats];
-    if (threadIdx.x < kNumStats) sh[threadIdx.x] = 0u;
-    __syncthreads();
-    for (int k = 0; k < kNumStats; k++)
-        if (acc.c[k]) atomicAdd_block(&sh[k], acc.c[k]);
-    __syncthreads();
-    if (threadIdx.x < kNumStats && sh[threadIdx.x]) atomicAdd(global + threadIdx.x, (unsigned long long)sh[threadIdx.x]);
-}
-
-DEV long long samples_of(const RunParams &p, int i) { return p.samplesPerChain + (i < p.extraChains ? 1 : 0); }
-
-DEV float length_pmf(const ChainView &d, int len) {
-    return d.lengthFunc[len] / (d.lengthFuncInt * float(d.lengthCount));
-}
 
 // ------------------------------------------------------------- stage-1 plan
 // Draws each chain's stage-1 coin and, for a large step, its length and light
@@ -328,49 +162,7 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
 }
 
 // ------------------------------------------------------------- derivatives
-// One warp per listed chain: lanes stride over the D(D+1)/2 Hessian entries.
-// which: 0 = current state, 2 = second proposal.
-__device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H,
-                                int member = threadIdx.x & 31, int team = 32) {
-    const int lane = member;
-    const int L = r.c + r.l - 1;
-    const int dim = 2 * L;
-    if (!(L <= maxDerv && ss > 1e-15f)) {
-        for (int k = lane; k < dim; k += team) g[k] = 0.0f;
-        for (int k = lane; k < dim * dim; k += team) H[k] = 0.0f;
-        return;
-    }
-    const int npairs = dim * (dim + 1) / 2;
-    for (int pidx = lane; pidx < npairs; pidx += team) {
-        // decode pidx -> (i0, j0), i0 <= j0, row-major over the upper triangle
-        int i0 = 0, rem = pidx;
-        while (rem >= dim - i0) {
-            rem -= dim - i0;
-            i0++;
-        }
-        const int j0 = i0 + rem;
-        HyperDual u[kMaxDim];
-        for (int k = 0; k < dim; k++)
-            u[k] = HyperDual(r.u[k], k == i0 ? 1.0f : 0.0f, k == j0 ? 1.0f : 0.0f, 0.0f);
-        const HyperDual f = ad_eval_path<HyperDual>(s, r, u);
-        H[i0 * dim + j0] = f.ab;
-        H[j0 * dim + i0] = f.ab;
-        if (i0 == j0) g[i0] = f.a;
-    }
-}
-
-// A team of p.derivWarps warps per listed chain shares its Hessian entries.
-__global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int w = gw / p.derivWarps;
-    const int n = p.d.counters[which == 0 ? 0 : 1];
-    if (w >= n) return;
-    const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
-    const Slot &st = slot_of(p.d, chain, which);
-    derivs_for_path(p.s, st.rec, st.ss, p.maxDerv, p.d.grad + size_t(w) * kMaxDim,
-                    p.d.hess + size_t(w) * kMaxDim * kMaxDim, (gw % p.derivWarps) * 32 + (threadIdx.x & 31),
-                    32 * p.derivWarps);
-}
+// k_derivs lives in derivs.cu (its own translation unit); see derivs.h.
 
 // One warp per listed chain; 4 warps per block, each with its own slice of
 // dynamic shared memory (gauss_smem_doubles(maxDim) doubles).

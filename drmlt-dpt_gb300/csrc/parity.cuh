@@ -13,16 +13,6 @@ __global__ void k_eval_paths(SceneView s, const PathRec *paths, const float *u, 
     logf[i] = ad_eval_path<float>(s, paths[i], u + size_t(i) * kMaxDim);
 }
 
-__global__ void k_gradhess_paths(SceneView s, const PathRec *paths, const float *u, int n, float *grad, float *hess) {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= n) return;
-    PathRec r = paths[w];
-    const int dim = path_dim(r.c, r.l);
-    for (int k = 0; k < dim; k++) r.u[k] = u[size_t(w) * kMaxDim + k];
-    // derivatives are always taken here (no ss / depth gate)
-    derivs_for_path(s, r, 1.0f, kMaxLen, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim);
-}
-
 struct NoJitter {
     DEV float normal() { return 0.0f; }
 };
@@ -246,7 +236,7 @@ int drmlt_path_grad_hess(void *handle, const drmlt_path *paths, const float *u, 
     if ((rc = dp.put(reinterpret_cast<const PathRec *>(paths), n)) || (rc = du.put(u, size_t(n) * kMaxDim)) ||
         (rc = dg.alloc(size_t(n) * kMaxDim)) || (rc = dh.alloc(size_t(n) * kMaxDim * kMaxDim)))
         return rc;
-    k_gradhess_paths<<<(n * 32 + 127) / 128, 128>>>(r->sv, dp.p, du.p, n, dg.p, dh.p);
+    launch_gradhess_paths(r->sv, dp.p, du.p, n, dg.p, dh.p, 0);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
     if ((rc = dg.get(grad, size_t(n) * kMaxDim))) return rc;
