@@ -488,7 +488,7 @@ struct Renderer {
         const int nb = (p.N + kStageBlock - 1) / kStageBlock;
         const int nbS = sparse_blocks(p.N, p.lanes);
         const int nbWarp = (p.N * 32 * p.derivWarps + 127) / 128;
-        const int nbG = (p.N + kGaussWarps - 1) / kGaussWarps;
+        const int nbG = p.N;  // one block per listed chain; blocks past the list exit
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
         switch (k) {
             case 0:
@@ -498,10 +498,10 @@ struct Renderer {
                 k_stage1<<<nbS, kStageBlock, 0, s>>>(p, iter);
                 return 4;
             case 1: launch_derivs(p, 0, nbWarp, s); return 1;
-            case 2: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 0); return 1;
+            case 2: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0); return 1;
             case 3: k_stage2<<<nbS, kStageBlock, 0, s>>>(p, iter); return 1;
             case 4: launch_derivs(p, 2, nbWarp, s); return 1;
-            case 5: k_gauss<<<nbG, 32 * kGaussWarps, gsm, s>>>(p, 2); return 1;
+            case 5: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 2); return 1;
             default:
                 if (p.drType == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p, iter);
                 k_finish<<<nbS, kStageBlock, 0, s>>>(p, iter);
@@ -782,7 +782,7 @@ extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const 
     CK(cudaMemsetAsync(cov, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double), st));
     // dims are device data here: scratch is sized for kMaxDim, and an odd or
     // out-of-range dimension yields zero outputs and a NaN log-determinant
-    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps, gauss_smem_bytes(kMaxDim), st>>>(
+    k_gauss_batch<<<n, 32 * kGaussTeamWarps, gauss_smem_bytes(kMaxDim), st>>>(
         dims, ss, grad, hess, n, sigma, kMaxDim, g_noallocStorePtr[dev], mean, inv_cov, cov, log_det);
     CK(cudaGetLastError());
     return DRMLT_OK;

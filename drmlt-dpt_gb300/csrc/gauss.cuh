@@ -59,9 +59,9 @@ DEV void gauss_isotropic(int dim, double sigma, GaussView g) {
     *g.dimv = double(dim);
 }
 
-// Shared-memory scratch of one warp for a Gaussian of dimension <= m. Matrices
-// are row-major with a padded row stride ld = m + 1, so a warp walking down a
-// column hits distinct banks.
+// Shared-memory scratch for one Gaussian of dimension <= m. Matrices are
+// row-major with a padded row stride ld = m + 1, so threads walking down a
+// column hit distinct banks.
 struct GaussSmem {
     int m, ld;
     double *A64;   // m x ld: the symmetrised Hessian (destroyed by the FP64 fallback)
@@ -92,32 +92,61 @@ struct GaussSmem {
     }
 };
 
-// doubles of scratch per warp (kept a multiple of 2 for 16-byte alignment)
-HD constexpr int gauss_smem_doubles(int m) {
-    return ((2 * m * (m + 1) + 3 * m) + (4 * m * (m + 1) + 3 * m + 2 * m + 1) / 2 + 1) & ~1;
-}
+// doubles of GaussSmem for dimension m, and of shared memory per Gaussian:
+// GaussSmem, then 32 doubles for the team reductions (rounded up to a
+// multiple of 2 for 16-byte alignment)
+HD constexpr int gauss_scratch_doubles(int m) { return 2 * m * (m + 1) + 3 * m + (4 * m * (m + 1) + 5 * m + 1) / 2 + 1; }
+HD constexpr int gauss_smem_doubles(int m) { return (gauss_scratch_doubles(m) + 32 + 1) & ~1; }
+DEV double *gauss_reduction(double *base, int m) { return base + gauss_scratch_doubles(m); }
 
-// Lane layout for an n x n elementwise pass: lane = h * np2 + j, column j,
-// rows h, h + G, ... (np2 = next power of two >= n, G = 32 / np2 row groups).
-struct LaneGrid {
-    int j, h, G;
-    DEV explicit LaneGrid(int n) {
-        const int lane = threadIdx.x & 31;
-        const int lg = n <= 8 ? 3 : (n <= 16 ? 4 : 5);
-        j = lane & ((1 << lg) - 1);
-        h = lane >> lg;
-        G = 32 >> lg;
+// The threads of one block (whole warps) cooperate on one Gaussian. red: 32
+// doubles of shared scratch for the reductions.
+struct Team {
+    int tid, size;
+    double *red;
+    DEV explicit Team(double *r) : tid(threadIdx.x), size(blockDim.x), red(r) {}
+    DEV void sync() const { __syncthreads(); }
+    DEV bool all(bool pred) const { return __syncthreads_and(pred) != 0; }
+    DEV double sum(double v) const {
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        __syncthreads();  // earlier readers of red are done
+        if ((tid & 31) == 0) red[tid >> 5] = v;
+        __syncthreads();
+        double t = 0.0;
+        for (int w = 0; w < (size >> 5); w++) t += red[w];
+        return t;
+    }
+    DEV float sum(float v) const {
+        float *r = reinterpret_cast<float *>(red);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        __syncthreads();
+        if ((tid & 31) == 0) r[tid >> 5] = v;
+        __syncthreads();
+        float t = 0.0f;
+        for (int w = 0; w < (size >> 5); w++) t += r[w];
+        return t;
     }
 };
 
+// Thread layout of an n x n elementwise pass: tid = h * np2 + j, column j,
+// rows h, h + G, ... (np2 = next power of two >= n, G = team size / np2).
+struct LaneGrid {
+    int j, h, G;
+    DEV LaneGrid(int n, const Team &t) {
+        const int lg = n <= 8 ? 3 : (n <= 16 ? 4 : 5);
+        j = t.tid & ((1 << lg) - 1);
+        h = t.tid >> lg;
+        G = t.size >> lg;
+    }
+};
 
 // Jacobi rotation (c, s) that annihilates a_pq. FP32: the classic formula.
 // FP64 (used only to polish an almost diagonal matrix): the tangent comes from
 // the FP32 formula, which leaves ~1e-7 a_pq behind and keeps the sweeps
-// converging, and c = (1 + t^2)^-1/2 is brought to FP64 accuracy by two steps of
-// Newton's iteration for the reciprocal square root
-// from the FP32 estimate, so the rotation is orthogonal in
-// FP64 without FP64 division or square-root sequences.
+// converging, and c = (1 + t^2)^-1/2 is brought to FP64 accuracy by two steps
+// of Newton's iteration for the reciprocal square root from the FP32
+// estimate, so the rotation is orthogonal in FP64 without FP64 division or
+// square-root sequences.
 DEV void rot_params(float app, float aqq, float apq, float &c, float &s) {
     c = 1.0f;
     s = 0.0f;
@@ -156,17 +185,17 @@ DEV int rr_player(int pos, int round, int m) {
     return 1 + t;
 }
 
-// Two-sided cyclic Jacobi, one warp, round-robin ordering: each round rotates
-// n/2 disjoint index pairs at once. A (n x ld, symmetric, n even) is destroyed:
-// its diagonal ends up holding the eigenvalues and V the eigenvectors as
-// columns. T = float for the fast first pass, double for the fallback.
+// Two-sided cyclic Jacobi by one team, round-robin ordering: each round
+// rotates n/2 disjoint index pairs at once. A (n x ld, symmetric, n even) is
+// destroyed: its diagonal ends up holding the eigenvalues and V the
+// eigenvectors as columns. T = float for the fast first pass, double for the
+// polish.
 template <class T>
-DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int maxSweeps) {
-    const int lane = threadIdx.x & 31;
-    const LaneGrid g(n);
+DEV void jacobi_team(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int maxSweeps, const Team &tm) {
+    const LaneGrid g(n, tm);
     for (int i = g.h; i < n; i += g.G)
         if (g.j < n) V[i * ld + g.j] = i == g.j ? T(1) : T(0);
-    __syncwarp();
+    tm.sync();
     const int half = n / 2, m = n - 1;
     T prevOff = T(0);
     for (int sweep = 0; sweep < maxSweeps; sweep++) {
@@ -177,27 +206,24 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
             if (i == g.j) diag += a * a;
             else if (g.j > i) off += a * a;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            off += __shfl_xor_sync(0xffffffffu, off, o);
-            diag += __shfl_xor_sync(0xffffffffu, diag, o);
-        }
+        off = tm.sum(off);
+        diag = tm.sum(diag);
         // converged, or (single precision) stalled at round-off
         if (off <= offTol * diag || off == T(0) || (sweep >= 6 && off > T(0.5) * prevOff)) break;
         prevOff = off;
         for (int round = 0; round < m; round++) {
-            if (lane < half) {
-                int p = rr_player(lane, round, m), q = rr_player(n - 1 - lane, round, m);
+            if (tm.tid < half) {
+                int p = rr_player(tm.tid, round, m), q = rr_player(n - 1 - tm.tid, round, m);
                 if (p > q) { const int t = p; p = q; q = t; }
                 T c, s;
                 rot_params(A[p * ld + p], A[q * ld + q], A[p * ld + q], c, s);
-                pq[2 * lane] = p;
-                pq[2 * lane + 1] = q;
-                cs[2 * lane] = c;
-                cs[2 * lane + 1] = s;
+                pq[2 * tm.tid] = p;
+                pq[2 * tm.tid + 1] = q;
+                cs[2 * tm.tid] = c;
+                cs[2 * tm.tid + 1] = s;
             }
-            __syncwarp();
-            // a round whose rotations are all the identity changes nothing
-            if (__all_sync(0xffffffffu, lane >= half || cs[2 * lane + 1] == T(0))) continue;
+            // (a barrier) a round whose rotations are all the identity changes nothing
+            if (tm.all(tm.tid >= half || cs[2 * tm.tid + 1] == T(0))) continue;
             if (g.j < n) {
                 for (int k = g.h; k < half; k += g.G) {  // rows p, q
                     const int p = pq[2 * k], q = pq[2 * k + 1];
@@ -207,7 +233,7 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
                     A[q * ld + g.j] = s * a + c * b;
                 }
             }
-            __syncwarp();
+            tm.sync();
             if (g.j < n) {
                 for (int k = g.h; k < half; k += g.G) {  // columns p, q and the eigenvector columns
                     const int p = pq[2 * k], q = pq[2 * k + 1];
@@ -221,7 +247,7 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
                     V[r + q] = s * va + c * vb;
                 }
             }
-            __syncwarp();
+            tm.sync();
         }
     }
 }
@@ -230,8 +256,8 @@ DEV void jacobi_warp(T *A, T *V, T *cs, int *pq, int n, int ld, T offTol, int ma
 // Z = A X - X diag(lam) into sm.A32 and, unless skipR, R = I - X^T X into
 // sm.R32. Both are ~1e-7 or smaller, so FP32 storage keeps their accuracy; the
 // sums cancel and run in FP64. X is sm.X. Returns |Z|_F^2.
-DEV double eigen_residuals(GaussSmem &sm, int n, bool skipR) {
-    const LaneGrid g(n);
+DEV double eigen_residuals(GaussSmem &sm, int n, bool skipR, const Team &tm) {
+    const LaneGrid g(n, tm);
     const int ld = sm.ld;
     const double *A = sm.A64;
     double res = 0.0;
@@ -244,19 +270,14 @@ DEV double eigen_residuals(GaussSmem &sm, int n, bool skipR) {
             for (int k = 0; k < n; k++) {
                 const double xkj = sm.X[k * ld + g.j];
                 z = ::fma(A[i * ld + k], xkj, z);
-                if (!skipR) {
-                    const double xki = sm.X[k * ld + i];
-                    r = ::fma(-xki, xkj, r);
-                }
+                if (!skipR) r = ::fma(-sm.X[k * ld + i], xkj, r);
             }
             sm.A32[i * ld + g.j] = float(z);
             if (!skipR) sm.R32[i * ld + g.j] = float(r);
             res += z * z;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) res += __shfl_xor_sync(0xffffffffu, res, o);
-    __syncwarp();
-    return res;
+    return tm.sum(res);  // includes a barrier
 }
 
 // Iterative refinement of the symmetric eigen-decomposition (Ogita & Aishima,
@@ -270,17 +291,16 @@ DEV double eigen_residuals(GaussSmem &sm, int n, bool skipR) {
 // T, E and X E are ~1e-7 and are formed in FP32 from a float copy of X; only
 // the residual sums and X + X E are FP64. A step is accepted when the FP64
 // residual of (X', lam~) is below 1e-11 |A|_F; at most two steps, then the
-// caller falls back to FP64 Jacobi. Leaves X and lam in sm.
-DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
-    const int lane = threadIdx.x & 31;
-    const LaneGrid g(n);
+// caller falls back to the FP64 polish. Leaves X and lam in sm.
+DEV bool refine_eigen_team(GaussSmem &sm, int n, double froA, const Team &tm) {
+    const LaneGrid g(n, tm);
     const int ld = sm.ld;
     const double tol2 = 1e-22 * froA * froA;
-    if (lane < n) sm.lam[lane] = double(sm.l32[lane]);
+    if (tm.tid < n) sm.lam[tm.tid] = double(sm.l32[tm.tid]);
     if (g.j < n)
         for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = double(sm.V32[i * ld + g.j]);
-    __syncwarp();
-    eigen_residuals(sm, n, false);
+    tm.sync();
+    eigen_residuals(sm, n, false, tm);
     double *lamNew = sm.cs64;
     for (int step = 0; step < 2; step++) {
         const float *X32 = sm.V32;
@@ -293,9 +313,10 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
                 sm.T32[i * ld + g.j] = t;
             }
         }
-        __syncwarp();
-        if (lane < n)
-            lamNew[lane] = sm.lam[lane] + double(sm.T32[lane * ld + lane]) / (1.0 - double(sm.R32[lane * ld + lane]));
+        tm.sync();
+        if (tm.tid < n)
+            lamNew[tm.tid] =
+                sm.lam[tm.tid] + double(sm.T32[tm.tid * ld + tm.tid]) / (1.0 - double(sm.R32[tm.tid * ld + tm.tid]));
         float offS = 0.0f, nR = 0.0f;
         if (g.j < n) {
             const float lj = float(sm.lam[g.j]);
@@ -308,12 +329,9 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
                 }
             }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            offS += __shfl_xor_sync(0xffffffffu, offS, o);
-            nR += __shfl_xor_sync(0xffffffffu, nR, o);
-        }
+        offS = tm.sum(offS);
+        nR = tm.sum(nR);  // the barriers also publish lamNew
         const float delta = 2.0f * (sqrtf(offS) + float(froA) * sqrtf(nR));
-        __syncwarp();
         // E in place of T
         if (g.j < n) {
             const double ltj = lamNew[g.j];
@@ -327,7 +345,7 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
                 sm.T32[i * ld + g.j] = e;
             }
         }
-        __syncwarp();
+        tm.sync();
         // X' = X + X E: the product in FP32 (it is ~1e-7), the sum in FP64
         if (g.j < n) {
             for (int i = g.h; i < n; i += g.G) {
@@ -336,15 +354,14 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
                 sm.X[i * ld + g.j] += double(c);
             }
         }
-        if (lane < n) sm.lam[lane] = lamNew[lane];
-        __syncwarp();
+        if (tm.tid < n) sm.lam[tm.tid] = lamNew[tm.tid];
+        tm.sync();
         // certificate: FP64 residual of the refined pairs (also the next step's Z)
-        const double res = eigen_residuals(sm, n, true);
+        const double res = eigen_residuals(sm, n, true, tm);
         if (res <= tol2) return true;  // false for NaN
         if (step == 1) break;
         if (g.j < n)
             for (int i = g.h; i < n; i += g.G) sm.V32[i * ld + g.j] = float(sm.X[i * ld + g.j]);
-        __syncwarp();
         // R for the refined X (FP64; Z is already in place)
         if (g.j < n) {
             for (int i = g.h; i < n; i += g.G) {
@@ -353,7 +370,7 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
                 sm.R32[i * ld + g.j] = float(r);
             }
         }
-        __syncwarp();
+        tm.sync();
     }
     return false;
 }
@@ -365,9 +382,8 @@ DEV bool refine_eigen_warp(GaussSmem &sm, int n, double froA) {
 // to ~1e-6 |A| in that basis, then X <- X W. Scratch: Y and M/W use the FP32
 // matrices' storage as FP64 matrices (A32+V32 and R32+T32 are each m x ld
 // doubles of contiguous space).
-DEV void polish_eigen_warp(GaussSmem &sm, int n) {
-    const int lane = threadIdx.x & 31;
-    const LaneGrid g(n);
+DEV void polish_eigen_team(GaussSmem &sm, int n, const Team &tm) {
+    const LaneGrid g(n, tm);
     const int ld = sm.ld;
     double *Y = reinterpret_cast<double *>(sm.A32);
     double *M = reinterpret_cast<double *>(sm.R32);
@@ -382,8 +398,7 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
                 dev += e * e;
             }
         }
-        for (int o = 16; o > 0; o >>= 1) dev += __shfl_xor_sync(0xffffffffu, dev, o);
-        __syncwarp();
+        dev = tm.sum(dev);
         if (dev <= 1e-28) break;
         if (g.j < n) {  // Y = X (3I - M) / 2
             for (int i = g.h; i < n; i += g.G) {
@@ -392,10 +407,10 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
                 Y[i * ld + g.j] = v;
             }
         }
-        __syncwarp();
+        tm.sync();
         if (g.j < n)
             for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = Y[i * ld + g.j];
-        __syncwarp();
+        tm.sync();
     }
     if (g.j < n) {  // Y = A X
         for (int i = g.h; i < n; i += g.G) {
@@ -404,7 +419,7 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
             Y[i * ld + g.j] = y;
         }
     }
-    __syncwarp();
+    tm.sync();
     if (g.j < n) {  // S = X^T Y over A64 (A is no longer needed)
         for (int i = g.h; i < n; i += g.G) {
             double v = 0.0;
@@ -412,7 +427,7 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
             sm.A64[i * ld + g.j] = v;
         }
     }
-    __syncwarp();
+    tm.sync();
     if (g.j < n) {  // symmetrise S against round-off
         for (int i = g.h; i < n; i += g.G) {
             if (i < g.j) {
@@ -422,8 +437,8 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
             }
         }
     }
-    __syncwarp();
-    jacobi_warp<double>(sm.A64, M, sm.cs64, sm.pq, n, ld, 1e-28, 8);
+    tm.sync();
+    jacobi_team<double>(sm.A64, M, sm.cs64, sm.pq, n, ld, 1e-28, 8, tm);
     if (g.j < n) {  // X <- X W (through Y)
         for (int i = g.h; i < n; i += g.G) {
             double v = 0.0;
@@ -431,56 +446,56 @@ DEV void polish_eigen_warp(GaussSmem &sm, int n) {
             Y[i * ld + g.j] = v;
         }
     }
-    __syncwarp();
+    tm.sync();
     if (g.j < n)
         for (int i = g.h; i < n; i += g.G) sm.X[i * ld + g.j] = Y[i * ld + g.j];
-    if (lane < n) sm.lam[lane] = sm.A64[lane * ld + lane];
-    __syncwarp();
+    if (tm.tid < n) sm.lam[tm.tid] = sm.A64[tm.tid * ld + tm.tid];
+    tm.sync();
 }
 
 enum : int { kGaussIsotropic = 0, kGaussRefined = 1, kGaussFp64Jacobi = 2 };
 
-// ComputeGaussian with one warp: grad (D floats), hess (D x D floats,
-// row-major) in global memory; scratch in this warp's shared memory (GaussSmem
-// sized for the launch's largest dimension). Non-finite derivatives are
-// scrubbed to zero first (drsmallstep.cpp:149-154). All 32 lanes must call it.
-// The eigen-decomposition is FP32 Jacobi refined to FP64 (refine_eigen_warp),
-// or FP64 Jacobi when the refinement's certificate fails. Returns which of the
-// three (isotropic fallback, refined, FP64 Jacobi) produced the Gaussian.
-DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const float *grad, const float *hess,
-                               GaussSmem &sm, GaussView g) {
-    const int lane = threadIdx.x & 31;
+// ComputeGaussian by one team (the whole block): grad (D floats), hess (D x D
+// floats, row-major) in global memory; scratch in the block's shared memory
+// (GaussSmem sized for the launch's largest dimension, then the team's
+// reduction scratch). Non-finite derivatives are scrubbed to zero first
+// (drsmallstep.cpp:149-154). Every thread of the block must call it. The
+// eigen-decomposition is FP32 Jacobi refined to FP64 (refine_eigen_team), or
+// the FP64 polish when the refinement's certificate fails. Returns which of
+// the three (isotropic fallback, refined, FP64 polish) produced the Gaussian.
+DEV int compute_gaussian_team(int dim, const H2mcParam &prm, float ss, const float *grad, const float *hess,
+                              GaussSmem &sm, GaussView g, const Team &tm) {
     const int ld = sm.ld;
     bool finite = true;
-    for (int i = lane; i < dim; i += 32) finite = finite && isfinite(grad[i]);
-    for (int i = lane; i < dim * dim; i += 32) finite = finite && isfinite(hess[i]);
-    finite = __all_sync(0xffffffffu, finite);
+    for (int i = tm.tid; i < dim; i += tm.size) finite = finite && isfinite(grad[i]);
+    for (int i = tm.tid; i < dim * dim; i += tm.size) finite = finite && isfinite(hess[i]);
+    finite = tm.all(finite);
     double fro = 0.0;
-    for (int e = lane; e < dim * dim; e += 32) {
+    for (int e = tm.tid; e < dim * dim; e += tm.size) {
         const double h = finite ? double(hess[e]) : 0.0;
         fro += h * h;
     }
-    for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    fro = tm.sum(fro);
     const double sigma = double(prm.sigma);
     const double invSigmaSq = 1.0 / (sigma * sigma);
     if (ss <= 1e-15f || ::sqrt(fro) < 0.5 / (sigma * sigma)) {
-        for (int e = lane; e < dim * dim; e += 32) g.V[e] = (e / dim == e % dim) ? 1.0 : 0.0;
-        for (int i = lane; i < dim; i += 32) {
+        for (int e = tm.tid; e < dim * dim; e += tm.size) g.V[e] = (e / dim == e % dim) ? 1.0 : 0.0;
+        for (int i = tm.tid; i < dim; i += tm.size) {
             g.p[i] = invSigmaSq;
             g.mean[i] = 0.0;
         }
-        if (lane == 0) {
+        if (tm.tid == 0) {
             *g.logDet = double(dim) * ::log(invSigmaSq);
             *g.dimv = double(dim);
         }
-        __syncwarp();
+        tm.sync();
         return kGaussIsotropic;
     }
     // symmetrise: the reference maps the row-major Hessian as a column-major
     // matrix and SelfAdjointEigenSolver reads its lower triangle, i.e. the
     // row-major upper triangle
     {
-        const LaneGrid lg(dim);
+        const LaneGrid lg(dim, tm);
         if (lg.j < dim) {
             for (int i = lg.h; i < dim; i += lg.G) {
                 const int k = lg.j;
@@ -490,19 +505,19 @@ DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const flo
             }
         }
     }
-    __syncwarp();
-    jacobi_warp<float>(sm.A32, sm.V32, sm.cs32, sm.pq, dim, ld, 1e-14f, 12);
-    if (lane < dim) sm.l32[lane] = sm.A32[lane * ld + lane];
-    __syncwarp();
+    tm.sync();
+    jacobi_team<float>(sm.A32, sm.V32, sm.cs32, sm.pq, dim, ld, 1e-14f, 12, tm);
+    if (tm.tid < dim) sm.l32[tm.tid] = sm.A32[tm.tid * ld + tm.tid];
+    tm.sync();
     int kind = kGaussRefined;
-    if (!refine_eigen_warp(sm, dim, ::sqrt(fro))) {
+    if (!refine_eigen_team(sm, dim, ::sqrt(fro), tm)) {
         kind = kGaussFp64Jacobi;
-        polish_eigen_warp(sm, dim);
+        polish_eigen_team(sm, dim, tm);
     }
-    // per eigenvalue (lane k): H2MC bounding and the drifted mean's eigen-coordinates
-    double mt = 0.0, logp = 0.0;
-    if (lane < dim) {
-        const int k = lane;
+    // per eigenvalue (thread k): H2MC bounding and the drifted mean's eigen-coordinates
+    double logp = 0.0;
+    if (tm.tid < dim) {
+        const int k = tm.tid;
         const double lam = sm.lam[k];
         double vg = 0.0;
         for (int i = 0; i < dim; i++) vg += sm.X[i * ld + k] * (finite ? double(grad[i]) : 0.0);
@@ -526,39 +541,34 @@ DEV int compute_gaussian_warp(int dim, const H2mcParam &prm, float ss, const flo
         eb = eb > 1e-10 ? 1.0 / eb : 0.0;
         const double post = eb + invSigmaSq;
         g.p[k] = post;
-        mt = eb / post * o;
         logp = ::log(post);
-        sm.cs64[k] = mt;
+        sm.cs64[k] = eb / post * o;
     }
-    for (int o = 16; o > 0; o >>= 1) logp += __shfl_xor_sync(0xffffffffu, logp, o);
-    __syncwarp();
-    for (int e = lane; e < dim * dim; e += 32) g.V[e] = sm.X[(e / dim) * ld + e % dim];
-    for (int i = lane; i < dim; i += 32) {
+    logp = tm.sum(logp);  // includes a barrier
+    for (int e = tm.tid; e < dim * dim; e += tm.size) g.V[e] = sm.X[(e / dim) * ld + e % dim];
+    for (int i = tm.tid; i < dim; i += tm.size) {
         double mu = 0.0;
         for (int k = 0; k < dim; k++) mu += sm.X[i * ld + k] * sm.cs64[k];
         g.mean[i] = mu;
     }
-    if (lane == 0) {
+    if (tm.tid == 0) {
         *g.logDet = logp;
         *g.dimv = double(dim);
     }
-    __syncwarp();
+    tm.sync();
     return kind;
 }
 
-
 // GaussianLogPdf (src/gaussian.cpp:18-26) in FP64 of sign * off (off: dim
-// floats) with one warp: lane k
-// projects the offset on eigenvector k, the lanes' terms are summed by shuffles.
-DEV double gauss_logpdf_warp(int dim, const float *off, double sign, GaussView g) {
-    const int lane = threadIdx.x & 31;
+// floats) by one team: thread k projects the offset on eigenvector k.
+DEV double gauss_logpdf_team(int dim, const float *off, double sign, GaussView g, const Team &tm) {
     double quad = 0.0;
-    if (lane < dim) {
+    if (tm.tid < dim) {
         double proj = 0.0;
-        for (int i = 0; i < dim; i++) proj = ::fma(g.V[i * dim + lane], sign * double(off[i]) - g.mean[i], proj);
-        quad = g.p[lane] * proj * proj;
+        for (int i = 0; i < dim; i++) proj = ::fma(g.V[i * dim + tm.tid], sign * double(off[i]) - g.mean[i], proj);
+        quad = g.p[tm.tid] * proj * proj;
     }
-    for (int o = 16; o > 0; o >>= 1) quad += __shfl_xor_sync(0xffffffffu, quad, o);
+    quad = tm.sum(quad);
     return double(dim) * (-0.5 * ::log(2.0 * 3.14159265358979323846)) + 0.5 * (*g.logDet) - 0.5 * quad;
 }
 

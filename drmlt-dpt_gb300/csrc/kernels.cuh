@@ -164,35 +164,35 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
 // ------------------------------------------------------------- derivatives
 // k_derivs lives in derivs.cu (its own translation unit); see derivs.h.
 
-// One warp per listed chain; 4 warps per block, each with its own slice of
-// dynamic shared memory (gauss_smem_doubles(maxDim) doubles).
-constexpr int kGaussWarps = 4;
-inline size_t gauss_smem_bytes(int maxDim) { return size_t(kGaussWarps) * gauss_smem_doubles(maxDim) * sizeof(double); }
+// One block (a team of kGaussTeamWarps warps) per listed chain, with
+// gauss_smem_doubles(maxDim) doubles of dynamic shared memory.
+constexpr int kGaussTeamWarps = 4;
+inline size_t gauss_smem_bytes(int maxDim) { return size_t(gauss_smem_doubles(maxDim)) * sizeof(double); }
 
-__global__ void __launch_bounds__(32 * kGaussWarps) k_gauss(RunParams p, int which) {
+__global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int which) {
     extern __shared__ double gsm[];
-    const int wib = threadIdx.x >> 5;
-    const int w = blockIdx.x * kGaussWarps + wib;
+    const int w = blockIdx.x;
     const int n = p.d.counters[which == 0 ? 0 : 1];
     if (w >= n) return;
     const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
     Slot &st = slot_of(p.d, chain, which);
     const int dim = path_dim(st.rec.c, st.rec.l);
-    GaussSmem sm(gsm + size_t(wib) * gauss_smem_doubles(p.gaussDim), p.gaussDim);
+    GaussSmem sm(gsm, p.gaussDim);
+    const Team tm(gauss_reduction(gsm, p.gaussDim));
     // dim <= gaussDim holds by construction (max_depth bounds every path); the
     // isotropic branch needs no scratch, so an impossible larger dim stays in bounds
-    const int kind = compute_gaussian_warp(dim, H2mcParam(p.sigma1), dim <= sm.m ? st.ss : 0.0f,
+    const int kind = compute_gaussian_team(dim, H2mcParam(p.sigma1), dim <= sm.m ? st.ss : 0.0f,
                                            p.d.grad + size_t(w) * kMaxDim, p.d.hess + size_t(w) * kMaxDim * kMaxDim, sm,
-                                           GaussView(gauss_of(p.d, chain, which)));
+                                           GaussView(gauss_of(p.d, chain, which)), tm);
     if (which == 2) {
         // the H2MC kernel ratio of PH2MCSmallStep::Mutate (drsmallstep.cpp:191-196), FP64
         Scratch &sc = p.d.scr[chain];
         const int d = dim <= sm.m ? dim : 0;
-        const double px = gauss_logpdf_warp(d, sc.offset, -1.0, GaussView(gauss_of(p.d, chain, 2)));
-        const double py = gauss_logpdf_warp(d, sc.offset, 1.0, GaussView(gauss_of(p.d, chain, 0)));
-        if ((threadIdx.x & 31) == 0) sc.logRatio = px - py;
+        const double px = gauss_logpdf_team(d, sc.offset, -1.0, GaussView(gauss_of(p.d, chain, 2)), tm);
+        const double py = gauss_logpdf_team(d, sc.offset, 1.0, GaussView(gauss_of(p.d, chain, 0)), tm);
+        if (threadIdx.x == 0) sc.logRatio = px - py;
     }
-    if ((threadIdx.x & 31) == 0) {
+    if (threadIdx.x == 0) {
         st.gaussInit = 1;
         if (kind != kGaussIsotropic) atomicAdd(&p.d.stats[kStatGauss], 1ull);
         if (kind == kGaussFp64Jacobi) atomicAdd(&p.d.stats[kStatGaussFallback], 1ull);

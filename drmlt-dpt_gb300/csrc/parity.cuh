@@ -120,28 +120,28 @@ __global__ void k_replay(SceneView s, int mode, const float *tapes, const int *t
     outConsumed[i] = rng.pos;
 }
 
-// dims[i] must be even and <= maxDim (checked by the callers); dynamic shared
-// memory gauss_smem_bytes(maxDim).
-__global__ void __launch_bounds__(32 * kGaussWarps) k_gauss_batch(const int *dims, const float *ss, const float *grad,
-                                                                 const float *hess, int n, float sigma, int maxDim,
-                                                                 double *store, double *mean, double *invCov,
-                                                                 double *cov, double *logDet) {
+// One block (team) per Gaussian. dims[i] must be even and <= maxDim (checked by
+// the callers); dynamic shared memory gauss_smem_bytes(maxDim).
+__global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss_batch(const int *dims, const float *ss,
+                                                                     const float *grad, const float *hess, int n,
+                                                                     float sigma, int maxDim, double *store,
+                                                                     double *mean, double *invCov, double *cov,
+                                                                     double *logDet) {
     extern __shared__ double gsm[];
-    const int wib = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * kGaussWarps + wib;
+    const int i = blockIdx.x;
     if (i >= n) return;
     const int dim = dims[i];
     if (dim <= 0 || dim > maxDim || (dim & 1)) {
-        if (lane == 0) logDet[i] = __longlong_as_double(0x7ff8000000000000ll);
+        if (threadIdx.x == 0) logDet[i] = __longlong_as_double(0x7ff8000000000000ll);
         return;
     }
     GaussView g(store + size_t(i) * kGaussStride);
-    GaussSmem sm(gsm + size_t(wib) * gauss_smem_doubles(maxDim), maxDim);
-    compute_gaussian_warp(dim, H2mcParam(sigma), ss[i], grad + size_t(i) * kMaxDim, hess + size_t(i) * kMaxDim * kMaxDim,
-                          sm, g);
-    for (int r = lane; r < dim; r += 32) mean[size_t(i) * kMaxDim + r] = g.mean[r];
-    for (int e = lane; e < dim * dim; e += 32) {
+    GaussSmem sm(gsm, maxDim);
+    const Team tm(gauss_reduction(gsm, maxDim));
+    compute_gaussian_team(dim, H2mcParam(sigma), ss[i], grad + size_t(i) * kMaxDim, hess + size_t(i) * kMaxDim * kMaxDim,
+                          sm, g, tm);
+    for (int r = threadIdx.x; r < dim; r += blockDim.x) mean[size_t(i) * kMaxDim + r] = g.mean[r];
+    for (int e = threadIdx.x; e < dim * dim; e += blockDim.x) {
         const int r = e / dim, c = e % dim;
         double ic = 0.0, cv = 0.0;
         for (int k = 0; k < dim; k++) {
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(32 * kGaussWarps) k_gauss_batch(const int *dim
         invCov[size_t(i) * kMaxDim * kMaxDim + r * dim + c] = ic;
         cov[size_t(i) * kMaxDim * kMaxDim + r * dim + c] = cv;
     }
-    if (lane == 0) logDet[i] = *g.logDet;
+    if (threadIdx.x == 0) logDet[i] = *g.logDet;
 }
 
 __global__ void k_trace_rays(SceneView s, const float *org, const float *dir, float tmin, float tmax, int n,
@@ -337,7 +337,7 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
     CK(cudaMemset(dm.p, 0, size_t(n) * kMaxDim * sizeof(double)));
     CK(cudaMemset(dic.p, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double)));
     CK(cudaMemset(dc.p, 0, size_t(n) * kMaxDim * kMaxDim * sizeof(double)));
-    k_gauss_batch<<<(n + kGaussWarps - 1) / kGaussWarps, 32 * kGaussWarps, gauss_smem_bytes(maxDim)>>>(
+    k_gauss_batch<<<n, 32 * kGaussTeamWarps, gauss_smem_bytes(maxDim)>>>(
         dd.p, dss.p, dg.p, dh.p, n, r->opt.perturb_stddev, maxDim, dstore.p, dm.p, dic.p, dc.p, dl.p);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
