@@ -53,9 +53,10 @@ struct ChainView {
     int *listX;         // chains needing a Gaussian at the current state
     int *listZ;         // chains needing a Gaussian at the second proposal
     int *listS;         // chains taking a second stage this iteration
+    int *listA;         // chains taking the anisotropic (H2MC) second stage
     int *order;         // stage-1 processing order (chains grouped by work class)
     int *hist;          // kPlanBins counters of the work classes
-    int *counters;      // [0] = |listX|, [1] = |listZ|, [2] = |listS|
+    int *counters;      // [0] = |listX|, [1] = |listZ|, [2] = |listS|, [3] = |listA|
     float *grad;        // N x kMaxDim (indexed by list position)
     float *hess;        // N x kMaxDim^2
     unsigned long long *stats;

@@ -141,6 +141,7 @@ struct Renderer {
         p.d.listX += p.c0;
         p.d.listZ += p.c0;
         p.d.listS += p.c0;
+        p.d.listA += p.c0;
         p.d.counters += 4 * g;
         p.d.hist += size_t(kPlanBins) * g;
         p.d.order += p.c0;
@@ -339,6 +340,7 @@ struct Renderer {
         if ((rc = alloc(&cv.listX, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listS, size_t(N)))) return rc;
+        if ((rc = alloc(&cv.listA, size_t(N)))) return rc;
         G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 1;
         G = std::min(G, N);
         chunk = (N + G - 1) / G;
@@ -478,7 +480,7 @@ struct Renderer {
 
     // Stage k of iteration `iter` for chain group g on stream s:
     //   0 stage1 (counter reset, plan, order, stage-1 kernel), 1 derivatives at x,
-    //   2 Gaussians at x, 3 stage2, 4 derivatives at z, 5 Gaussians at z,
+    //   2 Gaussians at x and the H2MC offsets, 3 stage2, 4 derivatives at z, 5 Gaussians at z,
     //   6 finish (Green's y* trace, acceptance, splats, swap).
     // The list-driven kernels are sized for the whole group and exit past the
     // list's device-side length.
@@ -498,7 +500,10 @@ struct Renderer {
                 k_stage1<<<nbS, kStageBlock, 0, s>>>(p, iter);
                 return 4;
             case 1: launch_derivs(p, 0, nbWarp, s); return 1;
-            case 2: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0); return 1;
+            case 2:
+                k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0);
+                k_h2mc_offset<<<(p.N * 32 + 127) / 128, 128, 0, s>>>(p, iter);
+                return 2;
             case 3: k_stage2<<<nbS, kStageBlock, 0, s>>>(p, iter); return 1;
             case 4: launch_derivs(p, 2, nbWarp, s); return 1;
             case 5: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 2); return 1;

@@ -572,16 +572,5 @@ DEV double gauss_logpdf_team(int dim, const float *off, double sign, GaussView g
     return double(dim) * (-0.5 * ::log(2.0 * 3.14159265358979323846)) + 0.5 * (*g.logDet) - 0.5 * quad;
 }
 
-// GenerateSample (src/gaussian.cpp:36-47): offset = covL n + mean.
-template <class R>
-DEV void gauss_sample(int dim, GaussView g, R &rng, double *offset) {
-    double z[kMaxDim];
-    for (int k = 0; k < dim; k++) z[k] = double(rng.normal()) / ::sqrt(g.p[k]);
-    for (int i = 0; i < dim; i++) {
-        double o = g.mean[i];
-        for (int k = 0; k < dim; k++) o += g.V[i * dim + k] * z[k];
-        offset[i] = o;
-    }
-}
 
 }  // namespace drmlt

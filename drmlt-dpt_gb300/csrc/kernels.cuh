@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
                     flags |= kAniso;
                     acc.c[kStatH2mc]++;
                     if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+                    p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
                 } else {
                     acc.c[kStatIso]++;
                 }
@@ -199,6 +200,34 @@ __global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int
     }
 }
 
+// ------------------------------------------------------------- H2MC offsets
+// GenerateSample (src/gaussian.cpp:36-47) for the chains taking the
+// anisotropic second stage, one warp per chain: offset = mean + V diag(p^-1/2) n
+// in FP64, with n the first dim normals of the chain's stage-2 stream (which
+// k_stage2 then skips).
+__global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p, int iter) {
+    __shared__ double zs[4][kMaxDim];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= p.d.counters[3]) return;
+    const int i = p.d.listA[w];
+    const Slot &cur = slot_of(p.d, i, 0);
+    const int dim = path_dim(cur.rec.c, cur.rec.l);
+    const GaussView g(gauss_of(p.d, i, 0));
+    if (lane == 0) {
+        Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
+        for (int k = 0; k < dim; k++) zs[wib][k] = double(rng.normal());
+    }
+    __syncwarp();
+    if (lane < dim) zs[wib][lane] /= ::sqrt(g.p[lane]);
+    __syncwarp();
+    if (lane < dim) {
+        double o = g.mean[lane];
+        for (int k = 0; k < dim; k++) o = ::fma(g.V[lane * dim + k], zs[wib][k], o);
+        p.d.scr[i].offset[lane] = float(o);
+    }
+}
+
 // ------------------------------------------------------------- stage 2 proposal
 // Over the group's second-stage list only (compacted by k_stage1).
 __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
@@ -214,12 +243,11 @@ __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
     float off[kMaxDim];
     const bool aniso = sc.flags & kAniso;
     if (aniso) {
-        // PH2MCSmallStep::Mutate (drsmallstep.cpp:113-212)
-        double od[kMaxDim];
-        gauss_sample(dim, GaussView(gauss_of(p.d, i, 0)), rng, od);
+        // PH2MCSmallStep::Mutate (drsmallstep.cpp:113-212): the offset was
+        // sampled by k_h2mc_offset from this stream's first dim normals
         for (int k = 0; k < dim; k++) {
-            off[k] = float(od[k]);
-            sc.offset[k] = off[k];
+            rng.normal();
+            off[k] = sc.offset[k];
         }
     } else {
         // SmallStep::Mutate with the second-stage sigma (mutation.cpp:167-208)

@@ -70,3 +70,22 @@ def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_
     mb = img.reshape(8, H // 8, 8, W // 8, 3).mean(axis=(1, 3))
     rel = np.abs(mb - rb) / np.maximum(rb, 1e-3)
     assert rel.mean() < 0.06, rel.mean()
+
+
+def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
+    """Chain groups, chains per warp and derivative-team size only change the
+    scheduling: the chains take the same steps (integer counters identical,
+    film equal up to the order of the floating-point splat additions)."""
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
+    out = []
+    for kw in (dict(), dict(chain_groups=4, stage_lanes=4, deriv_warps=1), dict(chain_groups=3, stage_lanes=32,
+                                                                               deriv_warps=4)):
+        with Renderer(sd, num_chains=4096, **kw) as r:
+            r.prepass()
+            r.run(12)
+            out.append((r.stats(), r.film().astype(np.float64)))
+    for st, film in out[1:]:
+        assert st == out[0][0]
+        np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
