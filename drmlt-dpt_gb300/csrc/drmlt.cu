@@ -78,7 +78,7 @@ struct Renderer {
     float lastRunMs = 0.0f;
     long long launches = 0;  // kernels launched by run() so far
     cudaGraphExec_t graph = nullptr;
-    int *dIter = nullptr;
+    int *dIters = nullptr;  // per chain group: its current iteration
     // chain groups, each stepped on its own stream
     int G = 1, chunk = 0;
     std::vector<cudaStream_t> gstreams;
@@ -99,6 +99,7 @@ struct Renderer {
     }
     ~Renderer() {
         if (graph) cudaGraphExecDestroy(graph);
+        if (forkEv) cudaEventDestroy(forkEv);
         for (cudaStream_t s : gstreams) cudaStreamDestroy(s);
         for (cudaEvent_t e : gevents) cudaEventDestroy(e);
         for (void *p : owned) cudaFree(p);
@@ -128,6 +129,7 @@ struct Renderer {
         p.maxDerv = opt.max_derivative_depth;
         p.gaussDim = std::min(2 * opt.max_depth, kMaxDim);
         p.lanes = opt.stage_lanes > 0 ? std::min(opt.stage_lanes, 32) : 16;
+        p.iterp = dIters;
         p.derivWarps = opt.deriv_warps > 0 ? std::min(opt.deriv_warps, 4) : 2;
         p.seed = opt.seed;
         return p;
@@ -145,6 +147,7 @@ struct Renderer {
         p.d.counters += 4 * g;
         p.d.hist += size_t(kPlanBins) * g;
         p.d.order += p.c0;
+        p.iterp = dIters + g;
         p.d.grad += size_t(p.c0) * kMaxDim;
         p.d.hess += size_t(p.c0) * kMaxDim * kMaxDim;
         return p;
@@ -355,6 +358,7 @@ struct Renderer {
         }
         if ((rc = alloc(&cv.counters, 4 * size_t(G)))) return rc;
         if ((rc = alloc(&cv.hist, size_t(kPlanBins) * G))) return rc;
+        if ((rc = alloc(&dIters, size_t(G)))) return rc;
         if ((rc = alloc(&cv.order, size_t(N)))) return rc;
         if ((rc = alloc(&cv.grad, size_t(N) * kMaxDim))) return rc;
         if ((rc = alloc(&cv.hess, size_t(N) * kMaxDim * kMaxDim))) return rc;
@@ -374,6 +378,10 @@ struct Renderer {
     }
 
     int prepass(float *bOut) {
+        if (graph) {  // its launch parameters carry the old normalisation
+            cudaGraphExecDestroy(graph);
+            graph = nullptr;
+        }
         const int minDepth = std::max(opt.min_depth, 3);
         const int ns = opt.num_init_samples;
         if (ns <= 0) return fail(DRMLT_E_ARG, "num_init_samples must be positive");
@@ -485,7 +493,7 @@ struct Renderer {
     // The list-driven kernels are sized for the whole group and exit past the
     // list's device-side length.
     static constexpr int kNumStagesRun = 7;
-    int launch_stage(int k, int g, int iter, cudaStream_t s) const {
+    int launch_stage(int k, int g, cudaStream_t s) const {
         const RunParams p = params(g);
         const int nb = (p.N + kStageBlock - 1) / kStageBlock;
         const int nbS = sparse_blocks(p.N, p.lanes);
@@ -495,28 +503,29 @@ struct Renderer {
         switch (k) {
             case 0:
                 k_reset_counters<<<1, 128, 0, s>>>(p.d.counters, p.d.hist);
-                k_plan<<<nb, kStageBlock, 0, s>>>(p, iter);
+                k_plan<<<nb, kStageBlock, 0, s>>>(p);
                 k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
-                k_stage1<<<nbS, kStageBlock, 0, s>>>(p, iter);
+                k_stage1<<<nbS, kStageBlock, 0, s>>>(p);
                 return 4;
             case 1: launch_derivs(p, 0, nbWarp, s); return 1;
             case 2:
                 k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0);
-                k_h2mc_offset<<<(p.N * 32 + 127) / 128, 128, 0, s>>>(p, iter);
+                k_h2mc_offset<<<(p.N * 32 + 127) / 128, 128, 0, s>>>(p);
                 return 2;
-            case 3: k_stage2<<<nbS, kStageBlock, 0, s>>>(p, iter); return 1;
+            case 3: k_stage2<<<nbS, kStageBlock, 0, s>>>(p); return 1;
             case 4: launch_derivs(p, 2, nbWarp, s); return 1;
             case 5: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 2); return 1;
             default:
-                if (p.drType == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p, iter);
-                k_finish<<<nbS, kStageBlock, 0, s>>>(p, iter);
-                return p.drType == 0 ? 2 : 1;
+                if (p.drType == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p);
+                k_finish<<<nbS, kStageBlock, 0, s>>>(p);
+                k_advance_iter<<<1, 1, 0, s>>>(dIters + g);
+                return p.drType == 0 ? 3 : 2;
         }
     }
     // returns the number of kernels launched
-    int launch_iteration(int g, int iter, cudaStream_t s) const {
+    int launch_iteration(int g, cudaStream_t s) const {
         int n = 0;
-        for (int k = 0; k < kNumStagesRun; k++) n += launch_stage(k, g, iter, s);
+        for (int k = 0; k < kNumStagesRun; k++) n += launch_stage(k, g, s);
         return n;
     }
 
@@ -530,13 +539,13 @@ struct Renderer {
         for (int k = 0; k <= kNumStages; k++) CK(cudaEventCreate(&ev[k]));
         for (int k = 0; k < kNumStages; k++) ms[k] = 0.0f;
         long long mutations = 0;
+        k_set_iters<<<1, 32, 0, stream>>>(dIters, G, int(iterDone));
         for (long long it = iterDone; it < end; it++) {
-            const int iter = int(it);
             // stage by stage over all groups on one stream, so each stage's
             // events bracket that stage for every chain
             cudaEventRecord(ev[0], stream);
             for (int k = 0; k < kNumStagesRun; k++) {
-                for (int g = 0; g < G; g++) launch_stage(k, g, iter, stream);
+                for (int g = 0; g < G; g++) launch_stage(k, g, stream);
                 cudaEventRecord(ev[k + 1], stream);
             }
             CK(cudaEventSynchronize(ev[kNumStages]));
@@ -554,21 +563,68 @@ struct Renderer {
         return DRMLT_OK;
     }
 
+    // One iteration of every chain group as a CUDA graph: forked from the main
+    // stream onto the group streams and joined back, replayed once per
+    // iteration by run() (the kernels read the iteration from dIters, which the
+    // graph advances). Built after the prepass, since the launch parameters
+    // carry its normalisation b.
+    long long graphLaunches = 0;
+    cudaEvent_t forkEv = nullptr;
+    int build_graph() {
+        if (!forkEv) CK(cudaEventCreateWithFlags(&forkEv, cudaEventDisableTiming));
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        long long n = 0;
+        cudaError_t e = cudaEventRecord(forkEv, stream);
+        for (int g = 0; g < G && e == cudaSuccess; g++) {
+            e = cudaStreamWaitEvent(gstreams[g], forkEv, 0);
+            if (e == cudaSuccess) n += launch_iteration(g, gstreams[g]);
+            if (e == cudaSuccess) e = cudaEventRecord(gevents[g], gstreams[g]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, gevents[g], 0);
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        cudaGraph_t gr = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(stream, &gr);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return fail(DRMLT_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        const cudaError_t e3 = cudaGraphInstantiate(&graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e3 != cudaSuccess) {
+            graph = nullptr;
+            return fail(DRMLT_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e3));
+        }
+        graphLaunches = n;
+        return DRMLT_OK;
+    }
+
     long long total_iterations() const { return samplesPerChain + (extraChains > 0 ? 1 : 0); }
 
     int run(long long iterations, long long *done) {
         if (!prepassDone) return fail(DRMLT_E_STATE, "run before prepass");
         const long long end = std::min(iterDone + iterations, total_iterations());
         long long mutations = 0;
-        CK(cudaEventRecord(ev0, stream));
-        for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(gstreams[g], ev0, 0));
-        for (long long it = iterDone; it < end; it++) {
-            for (int g = 0; g < G; g++) launches += launch_iteration(g, int(it), gstreams[g]);
-            mutations += (it < samplesPerChain) ? N : extraChains;
+        if (opt.use_graph && !graph) {
+            if (int rc = build_graph()) return rc;
         }
-        for (int g = 0; g < G; g++) {
-            CK(cudaEventRecord(gevents[g], gstreams[g]));
-            CK(cudaStreamWaitEvent(stream, gevents[g], 0));
+        k_set_iters<<<1, 32, 0, stream>>>(dIters, G, int(iterDone));
+        CK(cudaEventRecord(ev0, stream));
+        if (graph) {
+            for (long long it = iterDone; it < end; it++) {
+                CK(cudaGraphLaunch(graph, stream));
+                launches += graphLaunches;
+                mutations += (it < samplesPerChain) ? N : extraChains;
+            }
+        } else {
+            for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(gstreams[g], ev0, 0));
+            for (long long it = iterDone; it < end; it++) {
+                for (int g = 0; g < G; g++) launches += launch_iteration(g, gstreams[g]);
+                mutations += (it < samplesPerChain) ? N : extraChains;
+            }
+            for (int g = 0; g < G; g++) {
+                CK(cudaEventRecord(gevents[g], gstreams[g]));
+                CK(cudaStreamWaitEvent(stream, gevents[g], 0));
+            }
         }
         CK(cudaEventRecord(ev1, stream));
         CK(cudaGetLastError());
@@ -625,7 +681,7 @@ void drmlt_default_options(drmlt_options *o) {
     o->max_derivative_depth = 9;
     o->seed = 0x1234ABCDull;
     o->device = 0;
-    o->use_graph = 0;
+    o->use_graph = 1;
     o->chain_groups = 0;
     o->stage_lanes = 0;
     o->deriv_warps = 0;

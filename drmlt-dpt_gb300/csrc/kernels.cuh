@@ -36,7 +36,8 @@ DEV int plan_key(const RunParams &p, int i, int iter) {
     return 1 + 14 * cur.rec.c + cur.rec.l;
 }
 
-__global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p, int iter) {
+__global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p) {
+    const int iter = *p.iterp;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.N) return;
     const int i = p.c0 + t;
@@ -76,7 +77,8 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(RunParams p) {
 static_assert(2 * kScatterBlock == kPlanBins, "k_scatter scans two bins per thread");
 
 // ------------------------------------------------------------- stage 1
-__global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p, int iter) {
+__global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
+    const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes, on);
     StatAcc acc;
@@ -205,7 +207,8 @@ __global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int
 // anisotropic second stage, one warp per chain: offset = mean + V diag(p^-1/2) n
 // in FP64, with n the first dim normals of the chain's stage-2 stream (which
 // k_stage2 then skips).
-__global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p, int iter) {
+__global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p) {
+    const int iter = *p.iterp;
     __shared__ double zs[4][kMaxDim];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -230,7 +233,8 @@ __global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p, int iter) {
 
 // ------------------------------------------------------------- stage 2 proposal
 // Over the group's second-stage list only (compacted by k_stage1).
-__global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
+__global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
+    const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes, on);
     if (!on || t >= p.d.counters[2]) return;
@@ -278,7 +282,8 @@ __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p, int iter) {
 
 // Green's reverse path y* = z + (x - y) and its first-stage acceptance from z
 // (SmallStep::Trace, mutation.cpp:210-238), over the second-stage list only.
-__global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p, int iter) {
+__global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p) {
+    const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes, on);
     if (!on || t >= p.d.counters[2]) return;
@@ -311,7 +316,8 @@ DEV double iso_quad(int dim, const float *a, const float *b) {
 }
 
 // ------------------------------------------------------------- finish
-__global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p, int iter) {
+__global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
+    const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes, on);
     const int i = p.c0 + t;
@@ -406,6 +412,13 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p, int iter) {
         sc.a2 = a2;
     }
     flush_stats(acc, p.d.stats);
+}
+
+// One chain group's iteration counter, advanced after each of its iterations
+// on the group's stream (so a captured iteration replays as the next one).
+__global__ void k_advance_iter(int *iterp) { *iterp += 1; }
+__global__ void k_set_iters(int *iters, int n, int value) {
+    for (int g = threadIdx.x; g < n; g += blockDim.x) iters[g] = value;
 }
 
 __global__ void k_reset_counters(int *counters, int *hist) {

@@ -109,7 +109,7 @@ typedef struct drmlt_options {
     int32_t max_derivative_depth; /* --max-derivatives-depth (default 9) */
     uint64_t seed;                /* GPU random-stream key */
     int32_t device;               /* CUDA device ordinal */
-    int32_t use_graph;            /* capture each iteration as a CUDA graph */
+    int32_t use_graph;            /* replay each iteration as one CUDA graph (default 1) */
     int32_t chain_groups;         /* chains are split into this many groups, each stepped on its own
                                      CUDA stream so the groups' kernels overlap (0 = default, 1) */
     int32_t stage_lanes;          /* chains per warp in the per-chain stage kernels, 1..32 (0 = 16) */

@@ -73,15 +73,15 @@ def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_
 
 
 def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
-    """Chain groups, chains per warp and derivative-team size only change the
-    scheduling: the chains take the same steps (integer counters identical,
+    """Graph replay, chain groups, chains per warp and derivative-team size only
+    change the scheduling: the chains take the same steps (integer counters identical,
     film equal up to the order of the floating-point splat additions)."""
     from drmlt import scene as dscene
     from drmlt.integrator import Renderer
     sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
     out = []
-    for kw in (dict(), dict(chain_groups=4, stage_lanes=4, deriv_warps=1), dict(chain_groups=3, stage_lanes=32,
-                                                                               deriv_warps=4)):
+    for kw in (dict(), dict(use_graph=0), dict(chain_groups=4, stage_lanes=4, deriv_warps=1),
+               dict(chain_groups=3, stage_lanes=32, deriv_warps=4, use_graph=0)):
         with Renderer(sd, num_chains=4096, **kw) as r:
             r.prepass()
             r.run(12)
