@@ -200,6 +200,7 @@ def run_ours(args, world, rank, local):
 
     out = None
     if rank == 0:
+        relmse = time_to_relmse(sd, local) if not args.no_relmse else None
         cpu = cpu_baseline_sample(xml) if not args.no_cpu else None
         out = {
             "metric": METRIC, "value": value, "unit": "mutations/s", "n_gpus": world, "steps": args.steps,
@@ -211,6 +212,7 @@ def run_ours(args, world, rank, local):
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
+            "time_to_relmse": relmse,
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "wall_s_timed_region": wall,
@@ -221,6 +223,54 @@ def run_ours(args, world, rank, local):
     if world > 1:
         torch.distributed.destroy_process_group()
     return out
+
+
+def rel_mse(img, ref):
+    """Mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2)."""
+    return float(np.mean((img - ref) ** 2 / (ref * ref + 1e-2)))
+
+
+def time_to_relmse(sd, device, target=0.01, ref_spp=64):
+    """Seconds of GPU rendering until the image is within relMSE `target` of a
+    long render (ref_spp samples per pixel, different random streams) of the
+    same scene: the direct-lighting pass, the prepass and the chain-loop device
+    time up to the first checkpoint (doubling iteration counts) that meets the
+    target. Partial images scale the indirect film by total / done iterations."""
+    from drmlt.integrator import Renderer
+
+    def render_ref():
+        r = Renderer(sd, device=device, seed=0xBADC0FFE, spp=ref_spp)
+        r.render()
+        img = r.film().astype(np.float64)
+        r.close()
+        return img
+
+    ref = render_ref()
+    r = Renderer(sd, device=device, seed=0x5EED1234)
+    t0 = time.perf_counter()
+    r.direct()
+    r.prepass()
+    setup_s = time.perf_counter() - t0
+    direct_img = r.film().astype(np.float64)
+    total = r.total_iterations()
+    done, run_s, hit, checkpoints = 0, 0.0, None, []
+    step = 8
+    while done < total:
+        n = min(step, total - done)
+        r.run(n)
+        run_s += r.last_run_ms() * 1e-3
+        done += n
+        img = direct_img + (r.film().astype(np.float64) - direct_img) * (total / done)
+        e = rel_mse(img, ref)
+        checkpoints.append([done, round(setup_s + run_s, 4), e])
+        if e <= target:
+            hit = setup_s + run_s
+            break
+        step = done
+    r.close()
+    return {"value": hit, "unit": "s", "target_relmse": target, "reference": "%d spp GPU render" % ref_spp,
+            "setup_s": setup_s, "iterations": done, "spp_equivalent": done * sd.options.numChains /
+            (sd.width * sd.height), "checkpoints": checkpoints}
 
 
 def cpu_baseline_sample(xml: str, seconds: float = 15.0):
@@ -267,6 +317,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE measurement")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":
