@@ -24,7 +24,8 @@ struct Slot {
 };
 
 enum : int {
-    kActive = 1, kAccept1 = 2, kLarge = 4, kSecond = 8, kAniso = 16, kZValid = 32, kAccept2 = 64
+    kActive = 1, kAccept1 = 2, kLarge = 4, kSecond = 8, kAniso = 16, kZValid = 32, kAccept2 = 64,
+    kSingle = 128  // integrator=h2mc: the anisotropic proposal is the only stage
 };
 
 struct Scratch {

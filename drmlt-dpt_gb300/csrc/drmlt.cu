@@ -516,10 +516,10 @@ struct Renderer {
             case 4: launch_derivs(p, 2, nbWarp, s); return 1;
             case 5: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 2); return 1;
             default:
-                if (p.drType == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p);
+                if (p.drType == 0 && p.integrator == 0) k_ystar<<<nbS, kStageBlock, 0, s>>>(p);
                 k_finish<<<nbS, kStageBlock, 0, s>>>(p);
                 k_advance_iter<<<1, 1, 0, s>>>(dIters + g);
-                return p.drType == 0 ? 3 : 2;
+                return p.drType == 0 && p.integrator == 0 ? 3 : 2;
         }
     }
     // returns the number of kernels launched

@@ -33,6 +33,7 @@ DEV int plan_key(const RunParams &p, int i, int iter) {
         lgtLength = lgtLength < 0 ? 0 : (lgtLength > length ? length : lgtLength);
         return 200 + 14 * length + lgtLength;
     }
+    if (p.integrator == 1 && !(rng.uniform() < p.uniformMix)) return 0;  // H2MC step: no stage-1 trace
     return 1 + 14 * cur.rec.c + cur.rec.l;
 }
 
@@ -122,8 +123,18 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
                     accept1 = flip_coin(a1, rng.uniform());
                     if (accept1) acc.c[kStatLargeAcc]++;
                 }
+            } else if (p.integrator == 1 && !(rng.uniform() < p.uniformMix)) {
+                // H2MCIntegrator (src/integrators/h2mc.cpp:200-240): H2MCSmallStep::Mutate
+                // (h2mc.cpp:448-606) without its lens branch, as the single stage,
+                // run by the second-stage kernels
+                flags |= kSecond | kAniso | kSingle;
+                acc.c[kStatH2mc]++;
+                p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
+                if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+                p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
             } else {
-                // SmallStep::Mutate with perturbStdDev (src/mutation.cpp:126-166)
+                // SmallStep::Mutate with perturbStdDev (src/mutation.cpp:126-166); for
+                // integrator=h2mc the uniform-mixing step (h2mc.cpp:454-459)
                 acc.c[kStatStage1]++;
                 const int dim = path_dim(cur.rec.c, cur.rec.l);
                 float off[kMaxDim];
@@ -344,6 +355,10 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
             }
             if (is_invalid(a2)) {
                 a2 = 0.0f;
+            } else if (flags & kSingle) {
+                // the usual MH acceptance, Clamp(a, 0, 1) (h2mc.cpp:580-584, 220)
+                a2 = clamp01(a2);
+                accept2 = flip_coin(a2, rng.uniform());
             } else if (p.drType == 0) {
                 // Green & Mira (2001) (delayed.cpp:473-500); y* traced by k_ystar
                 float aStar = sc.aStar;

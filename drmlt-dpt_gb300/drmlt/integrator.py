@@ -8,6 +8,8 @@ on the GPU through the C ABI; this module only marshals arguments.
 """
 from __future__ import annotations
 
+import warnings
+
 import ctypes as C
 
 import numpy as np
@@ -26,6 +28,9 @@ def make_options(sd: SceneData, *, seed: int = 0x1234ABCD, device: int = 0,
     if d.integrator not in _INTEGRATORS:
         raise ValueError("Unknown integrator %r" % d.integrator)
     o.integrator = _INTEGRATORS[d.integrator]
+    if d.integrator in ("h2mc", "mcmc") and d.lensPerturbProb > 0:
+        warnings.warn("the lens mutation of integrator=%s (h2mc.cpp:466-532) is not implemented; "
+                      "lensperturbprob=%g is treated as 0" % (d.integrator, d.lensPerturbProb))
     o.dr_type = capi.DR_MIRA if d.type == "mira" else capi.DR_GREEN
     o.aniso_perturb_prob = d.anisoPerturbProb
     o.aniso_perturb_stddev = d.anisoperturbstddev

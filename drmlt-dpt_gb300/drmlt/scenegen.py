@@ -163,10 +163,13 @@ def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int =
     return path
 
 
-def config1(outdir: str, spp: int = 64) -> str:
-    """Plain DRMLT (green) on the 256x256 Lambertian Cornell box, max depth 5, 4096 chains."""
+def config1(outdir: str, spp: int = 64, integrator: str = "drmlt", acceptance_map: bool = False,
+            extra: dict | None = None) -> str:
+    """Plain DRMLT (green) on the 256x256 Lambertian Cornell box, max depth 5, 4096 chains
+    (other integrators / the acceptance map on the same scene for the render tests)."""
     return write_cornell(outdir, seed=1, width=256, height=256, phong=False,
-                         options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type="green"))
+                         options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type="green", integrator=integrator,
+                                              acceptanceMap=acceptance_map, extra=dict(extra or {})))
 
 
 def config2(outdir: str, dr_type: str = "mira", spp: int = 64) -> str:

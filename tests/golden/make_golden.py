@@ -45,8 +45,12 @@ CONFIGS = {
 }
 
 # full renders: (output suffix, scene writer with the render's spp, derivative depth)
+NO_LENS = {"lensperturbprob": "0"}  # the lens mutation of h2mc / mcmc is not part of this build
 RENDERS = {
-    "cfg1": [("render", lambda d: scenegen.config1(d, spp=16), 5)],
+    "cfg1": [("render", lambda d: scenegen.config1(d, spp=16), 5),
+             ("render_h2mc", lambda d: scenegen.config1(d, spp=16, integrator="h2mc", extra=NO_LENS), 5),
+             ("render_mcmc", lambda d: scenegen.config1(d, spp=16, integrator="mcmc", extra=NO_LENS), 5),
+             ("render_accmap", lambda d: scenegen.config1(d, spp=16, acceptance_map=True), 5)],
     "cfg2": [("render_mira", lambda d: scenegen.config2(d, "mira", spp=1), 8),
              ("render_green", lambda d: scenegen.config2(d, "green", spp=1), 8)],
 }
@@ -64,12 +68,15 @@ def read_pfm(path):
 
 
 def _stats(log: str) -> dict:
-    """The last 'Rendering Statistics' block. delayed.cpp:312-320 prints the
-    H2MC ratio under the 'isotropic' label and vice versa; undone here."""
+    """The last 'Rendering Statistics' block. DRMLT (delayed.cpp:312-320) prints
+    the H2MC ratio under the 'isotropic' label and vice versa; undone here.
+    H2MC / MCMC (h2mc.cpp:139-149, mcmc.cpp:76-86) print large, small and lens."""
     block = log[log.rindex("Rendering Statistics"):]
-    vals = re.findall(r":\s*([-0-9.e]+)\s*\((\d+)\)", block)
-    (rl, nl), (r1, n1), (rh, nh), (ri, ni) = [(float(a), int(b)) for a, b in vals[:4]]
-    return dict(large=[rl, nl], stage1=[r1, n1], stage2_h2mc=[rh, nh], stage2_iso=[ri, ni])
+    vals = [[float(a) if a not in ("nan", "-nan") else None, int(b)]
+            for a, b in re.findall(r":\s*(-?nan|[-0-9.e]+)\s*\((\d+)\)", block)]
+    if "First stage" in block:
+        return dict(large=vals[0], stage1=vals[1], stage2_h2mc=vals[2], stage2_iso=vals[3])
+    return dict(large=vals[0], small=vals[1], lens=vals[2])
 
 
 def render(cfg: str, blocks: int = 16):

@@ -22,7 +22,9 @@ from helpers import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-RENDERS = [("cfg1", "render", "green"), ("cfg2", "render_mira", "mira"), ("cfg2", "render_green", "green")]
+RENDERS = [("cfg1", "render", "green"), ("cfg2", "render_mira", "mira"), ("cfg2", "render_green", "green"),
+           ("cfg1", "render_accmap", "green")]
+SINGLE_STAGE = [("cfg1", "render_h2mc", "h2mc"), ("cfg1", "render_mcmc", "mcmc")]
 
 
 def _fixture(cfg, name):
@@ -33,9 +35,13 @@ def _fixture(cfg, name):
         return json.load(f)
 
 
-def _scene(cfg, dr_type, root):
+def _scene(cfg, dr_type, root, name="render"):
     from drmlt import scenegen
-    d = os.path.join(root, "%s_%s_render" % (cfg, dr_type))
+    d = os.path.join(root, "%s_%s_%s" % (cfg, dr_type, name))
+    if name == "render_accmap":
+        return scenegen.config1(d, spp=16, acceptance_map=True)
+    if dr_type in ("h2mc", "mcmc"):
+        return scenegen.config1(d, spp=16, integrator=dr_type, extra={"lensperturbprob": "0"})
     if cfg == "cfg1":
         return scenegen.config1(d, spp=16)
     return scenegen.config2(d, dr_type, spp=1)
@@ -46,7 +52,7 @@ def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_
     from drmlt import scene as dscene
     from drmlt.integrator import Renderer
     ref = _fixture(cfg, name)
-    sd = dscene.load_scene(_scene(cfg, dr_type, scene_root))
+    sd = dscene.load_scene(_scene(cfg, dr_type, scene_root, name))
     with Renderer(sd) as r:
         r.render()
         img = r.film().astype(np.float64)
@@ -89,3 +95,29 @@ def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
     for st, film in out[1:]:
         assert st == out[0][0]
         np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("cfg,name,integrator", SINGLE_STAGE)
+def test_single_stage_integrators_match_reference(built_lib, scene_root, cfg, name, integrator):
+    """integrator=h2mc (H2MC small step with uniform mixing, h2mc.cpp:200-240,
+    448-606) and integrator=mcmc (mcmc.cpp) against `dpt -d` renders of the
+    same scene, with lensperturbprob = 0 (the lens mutation is not part of this
+    build). Small-step ratio within 0.012, large step 0.006, image as above."""
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    ref = _fixture(cfg, name)
+    sd = dscene.load_scene(_scene(cfg, integrator, scene_root, name))
+    with Renderer(sd) as r:
+        r.render()
+        img = r.film().astype(np.float64)
+        st = r.stats()
+    assert st["stage2_iso"] == 0 and (integrator == "h2mc") == (st["stage2_h2mc"] > 0)
+    large = st["large_step_accepted"] / st["large_step"]
+    small = (st["stage1_accepted"] + st["stage2_h2mc_accepted"]) / (st["stage1"] + st["stage2_h2mc"])
+    assert abs(large - ref["stats"]["large"][0]) <= 0.006, (large, ref["stats"]["large"])
+    assert abs(small - ref["stats"]["small"][0]) <= 0.012, (small, ref["stats"]["small"])
+    np.testing.assert_allclose(img.mean(axis=(0, 1)), ref["mean"], rtol=0.02)
+    rb = np.array(ref["blocks"]).reshape(8, 2, 8, 2, 3).mean(axis=(1, 3))
+    H, W, _ = img.shape
+    mb = img.reshape(8, H // 8, 8, W // 8, 3).mean(axis=(1, 3))
+    assert (np.abs(mb - rb) / np.maximum(rb, 1e-3)).mean() < 0.06
