@@ -108,10 +108,10 @@ def write_workload(tmp: str, spp: int = 64) -> str:
 
 
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
-# HBM). A Slot is 340 B, the scratch 112 B, a
-# stored FP64 Gaussian 4.9 KB.
-SLOT_B = 340
-SCRATCH_B = 112
+# HBM). A Slot is 328 B, the per-chain scratch 128 B (both asserted in
+# csrc/chain.cuh), a stored FP64 Gaussian 5008 B.
+SLOT_B = 328
+SCRATCH_B = 128
 GAUSS_B = 8 * (24 * 24 + 2 * 24 + 2)
 
 
@@ -313,7 +313,7 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")

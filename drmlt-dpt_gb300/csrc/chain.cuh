@@ -37,8 +37,14 @@ struct Scratch {
     float offset[kMaxDim];
 };
 
-// Stage-1 work classes: 0 idle chain; 1 + 14 c + l small step of technique
-// (c, l); 200 + 14 L + lgtLength large step of sampled length L.
+// byte sizes that the throughput accounting (bench.py) assumes
+static_assert(sizeof(Slot) == 328, "Slot layout");
+static_assert(sizeof(Scratch) == 128, "Scratch layout");
+
+// Stage-1 work classes: 0 idle chain; 1 + 16 (c + l) + c small step of
+// technique (c, l); 256 + 16 L + lgtLength large step of sampled length L.
+// Higher classes are longer work; k_scatter orders the chains by descending
+// class, so the longest traces start first and the short ones fill the tail.
 constexpr int kPlanBins = 512;
 
 enum : int {

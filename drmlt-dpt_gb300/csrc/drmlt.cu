@@ -344,7 +344,7 @@ struct Renderer {
         if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listS, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listA, size_t(N)))) return rc;
-        G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 1;
+        G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 2;
         G = std::min(G, N);
         chunk = (N + G - 1) / G;
         G = (N + chunk - 1) / chunk;

@@ -31,10 +31,10 @@ DEV int plan_key(const RunParams &p, int i, int iter) {
         const int length = sample_discrete(p.d.lengthCdf, p.d.lengthCount, rng.uniform());
         int lgtLength = int(rng.uniform() * float(length + 1));
         lgtLength = lgtLength < 0 ? 0 : (lgtLength > length ? length : lgtLength);
-        return 200 + 14 * length + lgtLength;
+        return 256 + 16 * length + lgtLength;
     }
     if (p.integrator == 1 && !(rng.uniform() < p.uniformMix)) return 0;  // H2MC step: no stage-1 trace
-    return 1 + 14 * cur.rec.c + cur.rec.l;
+    return 1 + 16 * (cur.rec.c + cur.rec.l) + cur.rec.c;
 }
 
 __global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p) {
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(RunParams p) {
     for (int t = blockIdx.x * blockDim.x + tid; t < p.N; t += gridDim.x * blockDim.x) {
         const int i = p.c0 + t;
         const Scratch &sc = p.d.scr[i];
-        p.d.order[start[sc.key] + sc.rank] = i;
+        p.d.order[p.N - 1 - (start[sc.key] + sc.rank)] = i;  // descending class
     }
 }
 static_assert(2 * kScatterBlock == kPlanBins, "k_scatter scans two bins per thread");

@@ -111,7 +111,7 @@ typedef struct drmlt_options {
     int32_t device;               /* CUDA device ordinal */
     int32_t use_graph;            /* replay each iteration as one CUDA graph (default 1) */
     int32_t chain_groups;         /* chains are split into this many groups, each stepped on its own
-                                     CUDA stream so the groups' kernels overlap (0 = default, 1) */
+                                     CUDA stream so the groups' kernels overlap (0 = default, 2) */
     int32_t stage_lanes;          /* chains per warp in the per-chain stage kernels, 1..32 (0 = 16) */
     int32_t deriv_warps;          /* warps sharing one chain's Hessian entries, 1..4 (0 = 2) */
     int32_t smem_carveout;        /* shared-memory carveout (percent) for every chain-loop kernel,
