@@ -12,9 +12,180 @@ struct BsdfOut {
 
 DEV V3 kd_of(const Bsdf &b) { return V3(b.kd[0], b.kd[1], b.kd[2]); }
 DEV V3 ks_of(const Bsdf &b) { return V3(b.ks[0], b.ks[1], b.ks[2]); }
+DEV V3 kt_of(const Bsdf &b) { return V3(b.kt[0], b.kt[1], b.kt[2]); }
 
-// Lambertian::Evaluate (src/lambertian.cpp:15-38), Phong::Evaluate (src/phong.cpp:21-62).
+// ---------------------------------------------------------------- rough dielectric
+// BeckmennDistributionTerm (src/microfacet.h:6-18), isotropic roughness.
+DEV float beckmann_d(const V3 &h, float alpha) {
+    const float cosTheta2 = sq(h.z);
+    const float e = (sq(h.x) / sq(alpha) + sq(h.y) / sq(alpha)) / cosTheta2;
+    return expf(-e) / (kPi * alpha * alpha * sq(cosTheta2));
+}
+
+// BeckmennGeometryTerm (src/microfacet.h:20-38, 62-67): the rational
+// approximation of the shadowing-masking term, per direction.
+DEV float beckmann_g1(float alpha, float cosTheta) {
+    const float tanTheta = sqrtf(fabsf(1.0f - sq(cosTheta))) / cosTheta;
+    if (tanTheta <= 0.0f) return 1.0f;
+    const float a = 1.0f / (alpha * tanTheta);
+    if (a >= 1.6f) return 1.0f;
+    const float a2 = a * a;
+    return (3.535f * a + 2.181f * a2) / (1.0f + 2.276f * a + 2.577f * a2);
+}
+
+// FresnelDielectricExt (src/microfacet.h:69-115); cosThetaT is signed as there.
+DEV float fresnel_dielectric(float cosThetaI_, float &cosThetaT_, float eta, float invEta) {
+    const float scale = cosThetaI_ > 0.0f ? invEta : eta;
+    const float cosThetaTSqr = 1.0f - (1.0f - sq(cosThetaI_)) * sq(scale);
+    if (cosThetaTSqr <= 0.0f) {
+        cosThetaT_ = 0.0f;
+        return 1.0f;
+    }
+    const float cosThetaI = fabsf(cosThetaI_);
+    const float cosThetaT = sqrtf(cosThetaTSqr);
+    const float Rs = (cosThetaI - eta * cosThetaT) / (cosThetaI + eta * cosThetaT);
+    const float Rp = (eta * cosThetaI - cosThetaT) / (eta * cosThetaI + cosThetaT);
+    cosThetaT_ = cosThetaI_ > 0.0f ? -cosThetaT : cosThetaT;
+    return 0.5f * (sq(Rs) + sq(Rp));
+}
+
+// SampleMicronormal (src/microfacet.h:166-185), primal form.
+DEV V3 sample_micronormal(float r0, float r1, float alpha, float &pdfW) {
+    const float phiM = kTwoPi * r1;
+    const float sinPhiM = sinf(phiM), cosPhiM = cosf(phiM);
+    const float alphaSqr = sq(alpha);
+    const float tanThetaMSqr = alphaSqr * (-logf(fmaxf(1.0f - r0, 1e-6f)));
+    const float cosThetaM = 1.0f / sqrtf(1.0f + tanThetaMSqr);
+    const float cosThetaMSqr = sq(cosThetaM);
+    pdfW = (1.0f - r0) / (kPi * alphaSqr * cosThetaM * cosThetaMSqr);
+    const float sinThetaM = sqrtf(fmaxf(1.0f - cosThetaMSqr, 0.0f));
+    return V3(sinThetaM * cosPhiM, sinThetaM * sinPhiM, cosThetaM);
+}
+
+// Refract (src/utils.h:202-210).
+DEV V3 refract_dir(const V3 &wi, const V3 &n, float cosThetaT, float eta, float invEta) {
+    const float e = cosThetaT < 0.0f ? invEta : eta;
+    return n * (dot(wi, n) * e + cosThetaT) - wi * e;
+}
+
+// Evaluate<adjoint> of src/roughdielectric.cpp:22-124.
+template <bool adjoint>
+DEV void rough_dielectric_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &wo, BsdfOut &o) {
+    const float cosWi = dot(wi, normal);
+    o.contrib = V3(0.0f, 0.0f, 0.0f);
+    o.cosWo = 0.0f;
+    o.pdf = o.revPdf = 0.0f;
+    if (fabsf(cosWi) < kCosEps) return;
+    o.cosWo = dot(wo, normal);
+    const float cosWo = o.cosWo;
+    if (fabsf(cosWo) < kCosEps) return;
+    const bool reflect = cosWi * cosWo > 0.0f;
+    const float eta_ = cosWi > 0.0f ? b.eta : b.invEta;
+    const float revEta_ = cosWo > 0.0f ? b.eta : b.invEta;
+    V3 H = reflect ? normalize(V3(wi + wo)) : normalize(V3(wi + wo * eta_));
+    if (dot(H, normal) < 0.0f) H = -H;
+    const float cosHWi = dot(wi, H), cosHWo = dot(wo, H);
+    if (fabsf(cosHWi) < kCosEps || fabsf(cosHWo) < kCosEps) return;
+    if (cosHWi * cosWi <= 0.0f || cosHWo * cosWo <= 0.0f) return;
+    V3 b0, b1;
+    coordinate_system(normal, b0, b1);
+    const V3 localH(dot(b0, H), dot(b1, H), dot(normal, H));
+    const float alp = b.alpha;
+    const float D = beckmann_d(localH, alp);
+    if (D <= 0.0f) return;
+    const float revCosHWi = cosHWo, revCosHWo = cosHWi;
+    float ct;
+    const float F = fresnel_dielectric(cosHWi, ct, b.eta, b.invEta);
+    const float aCosWi = fabsf(cosWi), aCosWo = fabsf(cosWo);
+    const float G = beckmann_g1(alp, aCosWi) * beckmann_g1(alp, aCosWo);
+    const float scaledAlpha = alp * (1.2f - 0.2f * sqrtf(aCosWi));
+    const float prob = localH.z * beckmann_d(localH, scaledAlpha);
+    if (prob < 1e-20f) return;
+    const float revScaledAlpha = alp * (1.2f - 0.2f * sqrtf(aCosWo));
+    const float revProb = localH.z * beckmann_d(localH, revScaledAlpha);
+    if (reflect) {
+        const float scalar = fabsf(F * D * G / (4.0f * cosWi));
+        o.contrib = ks_of(b) * scalar;
+        o.pdf = fabsf(prob * F / (4.0f * cosHWo));
+        o.revPdf = fabsf(revProb * F / (4.0f * revCosHWo));
+    } else {
+        const float sqrtDenom = cosHWi + eta_ * cosHWo;
+        const float revSqrtDenom = revCosHWi + revEta_ * revCosHWo;
+        const float factor = adjoint ? 1.0f : sq(1.0f / eta_);
+        const float scalar = fabsf(factor * ((1.0f - F) * D * G * sq(eta_) * cosHWi * cosHWo) / (cosWi * sq(sqrtDenom)));
+        o.contrib = kt_of(b) * scalar;
+        o.pdf = fabsf(prob * (1.0f - F) * (sq(eta_) * cosHWo) / sq(sqrtDenom));
+        o.revPdf = fabsf(revProb * (1.0f - F) * (sq(revEta_) * revCosHWo) / sq(revSqrtDenom));
+    }
+}
+
+// Sample<adjoint> of src/roughdielectric.cpp:147-254.
+template <bool adjoint>
+DEV bool rough_dielectric_sample(const Bsdf &b, const V3 &wi, const V3 &normal, float r0, float r1, float uDiscrete,
+                                 V3 &wo, BsdfOut &o) {
+    const float cosWi = dot(wi, normal);
+    if (fabsf(cosWi) < kCosEps) return false;
+    const float alp = b.alpha;
+    const float scaledAlp = alp * (1.2f - 0.2f * sqrtf(fabsf(cosWi)));
+    float mPdf;
+    const V3 localH = sample_micronormal(r0, r1, scaledAlp, mPdf);
+    o.pdf = mPdf;
+    V3 b0, b1;
+    coordinate_system(normal, b0, b1);
+    const V3 H = localH.x * b0 + localH.y * b1 + localH.z * normal;
+    const float cosHWi = dot(wi, H);
+    if (fabsf(cosHWi) < kCosEps) return false;
+    float cosThetaT = 0.0f;
+    const float F = fresnel_dielectric(cosHWi, cosThetaT, b.eta, b.invEta);
+    V3 refl;
+    float cosHWo;
+    if (uDiscrete <= F) {
+        wo = reflect(wi, H);
+        if (F <= 0.0f || dot(normal, wo) * dot(normal, wi) <= 0.0f) return false;
+        refl = ks_of(b);
+        cosHWo = dot(wo, H);
+        o.pdf = fabsf(o.pdf * F / (4.0f * cosHWo));
+        const float rev_dwh_dwo = 1.0f / (4.0f * cosHWi);
+        o.cosWo = dot(wo, normal);
+        if (fabsf(o.cosWo) < kCosEps) return false;
+        const float revScaledAlp = alp * (1.2f - 0.2f * sqrtf(fabsf(o.cosWo)));
+        o.revPdf = fabsf(F * beckmann_d(localH, revScaledAlp) * localH.z * rev_dwh_dwo);
+    } else {
+        wo = refract_dir(wi, H, cosThetaT, b.eta, b.invEta);
+        if (F >= 1.0f || cosThetaT == 0.0f || dot(normal, wo) * dot(normal, wi) >= 0.0f) return false;
+        const float eta_ = cosWi > 0.0f ? b.eta : b.invEta;
+        const float factor = adjoint ? 1.0f : sq(1.0f / eta_);
+        refl = kt_of(b) * factor;
+        cosHWo = dot(wo, H);
+        const float sqrtDenom = cosHWi + eta_ * cosHWo;
+        const float dwh_dwo = (sq(eta_) * cosHWo) / sq(sqrtDenom);
+        o.pdf = fabsf(o.pdf * (1.0f - F) * fabsf(dwh_dwo));
+        o.cosWo = dot(wo, normal);
+        if (fabsf(o.cosWo) < kCosEps) return false;
+        const float revEta_ = o.cosWo > 0.0f ? b.eta : b.invEta;
+        const float revSqrtDenom = cosHWo + revEta_ * cosHWi;
+        const float rev_dwh_dwo = (sq(revEta_) * cosHWi) / sq(revSqrtDenom);
+        const float revScaledAlp = alp * (1.2f - 0.2f * sqrtf(fabsf(o.cosWo)));
+        o.revPdf = fabsf((1.0f - F) * beckmann_d(localH, revScaledAlp) * localH.z * rev_dwh_dwo);
+    }
+    if (fabsf(cosHWo) < kCosEps) return false;
+    if (o.pdf < 1e-20f) return false;
+    if (cosHWi * cosWi <= 0.0f || cosHWo * o.cosWo <= 0.0f) return false;
+    const float aCosWi = fabsf(cosWi), aCosWo = fabsf(o.cosWo);
+    const float D = beckmann_d(localH, alp);
+    const float G = beckmann_g1(alp, aCosWi) * beckmann_g1(alp, aCosWo);
+    o.contrib = refl * fabsf((D * G * cosHWi) / (mPdf * aCosWi));
+    return true;
+}
+
+// Lambertian::Evaluate (src/lambertian.cpp:15-38), Phong::Evaluate (src/phong.cpp:21-62),
+// RoughDielectric::Evaluate / EvaluateAdjoint (src/roughdielectric.cpp:126-144).
+template <bool adjoint = false>
 DEV void bsdf_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &wo, BsdfOut &o) {
+    if (b.type == kBsdfRoughDielectric) {
+        rough_dielectric_evaluate<adjoint>(b, wi, normal, wo, o);
+        return;
+    }
     o.contrib = V3(0.0f, 0.0f, 0.0f);
     o.pdf = 0.0f;
     o.revPdf = 0.0f;
@@ -53,9 +224,12 @@ DEV void bsdf_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &
     if (max_coeff(o.contrib) < 1e-10f) o.contrib = V3(0.0f, 0.0f, 0.0f);
 }
 
-// Lambertian::Sample (src/lambertian.cpp:56-90), Phong::Sample (src/phong.cpp:64-147).
+// Lambertian::Sample (src/lambertian.cpp:56-90), Phong::Sample (src/phong.cpp:64-147),
+// RoughDielectric::Sample / SampleAdjoint (src/roughdielectric.cpp:256-282).
+template <bool adjoint = false>
 DEV bool bsdf_sample(const Bsdf &b, const V3 &wi, const V3 &normal, float r0, float r1, float uDiscrete,
                      V3 &wo, BsdfOut &o) {
+    if (b.type == kBsdfRoughDielectric) return rough_dielectric_sample<adjoint>(b, wi, normal, r0, r1, uDiscrete, wo, o);
     float cosWi = dot(wi, normal);
     if (fabsf(cosWi) < kCosEps) return false;
     V3 n = normal;
@@ -122,8 +296,10 @@ DEV bool bsdf_sample(const Bsdf &b, const V3 &wi, const V3 &normal, float r0, fl
     return true;
 }
 
-// BSDF::Roughness: Lambertian 1 (src/lambertian.h:38-40), Phong (src/phong.cpp:149-156).
+// BSDF::Roughness: Lambertian 1 (src/lambertian.h:38-40), Phong (src/phong.cpp:149-156),
+// RoughDielectric alpha (src/roughdielectric.h:60-62).
 DEV float bsdf_roughness(const Bsdf &b, float uDiscrete) {
+    if (b.type == kBsdfRoughDielectric) return b.alpha;
     if (b.type == kBsdfPhong && uDiscrete < b.ksWeight) return sqrtf(2.0f / (2.0f + 4.0f * b.exponent));
     return 1.0f;
 }

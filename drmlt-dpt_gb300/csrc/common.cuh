@@ -119,6 +119,7 @@ struct Bsdf {
     float ksWeight;   // Phong::GetKsWeight (src/phong.cpp:158-167), precomputed on the host
     float intIOR, extIOR, alpha;
     float kt[3];
+    float eta, invEta;  // RoughDielectric: intIOR / extIOR and its inverse (src/roughdielectric.h:17)
 };
 
 struct Light {

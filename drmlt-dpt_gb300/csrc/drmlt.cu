@@ -218,7 +218,6 @@ struct Renderer {
             Bsdf &b0 = bsdfs[i];
             std::memset(&b0, 0, sizeof(Bsdf));
             b0.type = in.type;
-            if (in.type == DRMLT_BSDF_ROUGHDIELECTRIC) return fail(DRMLT_E_ARG, "roughdielectric is not supported yet");
             b0.twoSided = in.two_sided;
             for (int k = 0; k < 3; k++) {
                 b0.kd[k] = in.kd[k];
@@ -234,6 +233,12 @@ struct Renderer {
             b0.intIOR = in.int_ior;
             b0.extIOR = in.ext_ior;
             b0.alpha = in.alpha;
+            if (in.type == DRMLT_BSDF_ROUGHDIELECTRIC) {
+                if (!(in.int_ior > 0.0f && in.ext_ior > 0.0f && in.alpha > 0.0f))
+                    return fail(DRMLT_E_ARG, "roughdielectric needs positive IORs and alpha");
+                b0.eta = in.int_ior / in.ext_ior;
+                b0.invEta = 1.0f / b0.eta;
+            }
         }
         // lights, light pick distribution and per-area-light triangle CDFs
         std::vector<Light> lights(sd->num_lights);

@@ -143,7 +143,7 @@ DEV bool connect_to_camera(const SceneView &s, int lgtDepth, const BState &ps, c
     if (occluded(s, ps.isect.position, dirToCamera, dist)) return false;
     const Bsdf &bsdf = bsdf_of_tri(s, v.tri);
     BsdfOut bo;
-    bsdf_evaluate(bsdf, ps.wi, ps.isect.shadingNormal, dirToCamera, bo);
+    bsdf_evaluate<true>(bsdf, ps.wi, ps.isect.shadingNormal, dirToCamera, bo);
     if (is_zero(bo.contrib)) return false;
     const float factor = shading_normal_correction<true>(ps.wi, ps.isect, dirToCamera);
     if (factor <= 0.0f) return false;
@@ -185,7 +185,7 @@ DEV bool bsdf_sampling(const SceneView &s, const BState &ps, SVert &v, BState &n
     float nextSsJ;
     float nextLcJ;
     if (!perturb || !v.useAbs) {
-        if (!bsdf_sample(bsdf, ps.wi, ps.isect.shadingNormal, v.rnd[0], v.rnd[1], v.disc, dir, bo)) return false;
+        if (!bsdf_sample<adjoint>(bsdf, ps.wi, ps.isect.shadingNormal, v.rnd[0], v.rnd[1], v.disc, dir, bo)) return false;
         if (v.useAbs) {
             float jac;
             to_spherical(dir, v.rnd[0], v.rnd[1], jac);
@@ -199,7 +199,7 @@ DEV bool bsdf_sampling(const SceneView &s, const BState &ps, SVert &v, BState &n
     } else {
         float jac;
         dir = sample_sphere(v.rnd[0], v.rnd[1], jac);
-        bsdf_evaluate(bsdf, ps.wi, ps.isect.shadingNormal, dir, bo);
+        bsdf_evaluate<adjoint>(bsdf, ps.wi, ps.isect.shadingNormal, dir, bo);
         if (is_zero(bo.contrib) || bo.pdf <= 0.0f) return false;
         bo.contrib = bo.contrib * (1.0f / bo.pdf);
         nextLcJ = 1.0f / jac;
@@ -297,7 +297,7 @@ DEV bool connect_vertex(const SceneView &s, int camDepth, int lgtDepth, const BS
     if (camFactor <= 0.0f) return false;
     const V3 camF = cb.contrib * camFactor;
     BsdfOut lb;
-    bsdf_evaluate(bsdf_of_tri(s, lv.tri), lp.wi, lp.isect.shadingNormal, -dirToLight, lb);
+    bsdf_evaluate<true>(bsdf_of_tri(s, lv.tri), lp.wi, lp.isect.shadingNormal, -dirToLight, lb);
     if (is_zero(lb.contrib)) return false;
     const float lgtFactor = shading_normal_correction<true>(lp.wi, lp.isect, -dirToLight);
     if (lgtFactor <= 0.0f) return false;

@@ -74,12 +74,17 @@ HD HyperDual pow(const HyperDual &x, float e) {
     const float d2 = e * (e - 1.0f) * powf(x.v, e - 2.0f);
     return chain(x, p, d1, d2);
 }
+HD HyperDual exp(const HyperDual &x) {
+    const float e = expf(x.v);
+    return chain(x, e, e, e);
+}
 HD HyperDual fabs(const HyperDual &x) { return x.v >= 0.0f ? x : -x; }
 HD HyperDual fmax(const HyperDual &x, float c) { return x.v >= c ? x : HyperDual(c); }
 HD float sqrt(float x) { return sqrtf(x); }
 HD float sin(float x) { return sinf(x); }
 HD float cos(float x) { return cosf(x); }
 HD float log(float x) { return logf(x); }
+HD float exp(float x) { return expf(x); }
 HD float fabs(float x) { return fabsf(x); }
 HD float fmax(float x, float c) { return fmaxf(x, c); }
 HD float val(const HyperDual &x) { return x.v; }
@@ -134,9 +139,153 @@ struct TBsdf {
     T cosWo, pdf, revPdf;
 };
 
-// EvaluateLambertian / EvaluatePhong (AD forms).
+// ---------------------------------------------------------------- rough dielectric (AD forms)
+// BeckmennDistributionTerm (src/microfacet.h:6-18) with a constant or a path-dependent roughness.
+template <class T, class A>
+DEV T ad_beckmann_d(const TV3<T> &h, const A &alpha) {
+    const T cosTheta2 = h.z * h.z;
+    const T e = (h.x * h.x / (alpha * alpha) + h.y * h.y / (alpha * alpha)) / cosTheta2;
+    return exp(-e) / (kPi * alpha * alpha * (cosTheta2 * cosTheta2));
+}
+
+// The AD BeckmennGeometryTerm (src/microfacet.h:40-60): 1 + 1e-6 under the root.
 template <class T>
-DEV void ad_evaluate(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo, TBsdf<T> &o) {
+DEV T ad_beckmann_g1(float alpha, const T &cosTheta) {
+    const T tanTheta = sqrt(fabs((1.0f + 1e-6f) - cosTheta * cosTheta)) / cosTheta;
+    if (val(tanTheta) <= 0.0f) return T(1.0f);
+    const T a = 1.0f / (alpha * tanTheta);
+    if (val(a) >= 1.6f) return T(1.0f);
+    const T a2 = a * a;
+    return (3.535f * a + 2.181f * a2) / (1.0f + 2.276f * a + 2.577f * a2);
+}
+
+// The AD FresnelDielectricExt (src/microfacet.h:117-145).
+template <class T>
+DEV T ad_fresnel(const T &cosThetaI_, T &cosThetaT_, float eta, float invEta) {
+    const float scale = val(cosThetaI_) > 0.0f ? invEta : eta;
+    const T cosThetaTSqr = 1.0f - (1.0f - cosThetaI_ * cosThetaI_) * (scale * scale);
+    if (val(cosThetaTSqr) <= 0.0f) {
+        cosThetaT_ = T(0.0f);
+        return T(1.0f);
+    }
+    const T cosThetaI = fabs(cosThetaI_);
+    const T cosThetaT = sqrt(cosThetaTSqr);
+    const T etaCosThetaT = eta * cosThetaT;
+    const T etaCosThetaI = eta * cosThetaI;
+    const T Rs = (cosThetaI - etaCosThetaT) / (cosThetaI + etaCosThetaT);
+    const T Rp = (etaCosThetaI - cosThetaT) / (etaCosThetaI + cosThetaT);
+    cosThetaT_ = val(cosThetaI_) > 0.0f ? -cosThetaT : cosThetaT;
+    return 0.5f * (Rs * Rs + Rp * Rp);
+}
+
+// EvaluateRoughDielectric (src/roughdielectric.cpp:284-374).
+template <class T>
+DEV void ad_rough_dielectric_evaluate(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo,
+                                      TBsdf<T> &o, bool adjoint) {
+    const T cosWi = dot(wi, normal);
+    o.cosWo = dot(wo, normal);
+    const T cosWo = o.cosWo;
+    const bool reflect = val(cosWi) * val(cosWo) > 0.0f;
+    const float eta_ = val(cosWi) > 0.0f ? b.eta : b.invEta;
+    const float revEta_ = val(cosWo) > 0.0f ? b.eta : b.invEta;
+    TV3<T> H = reflect ? tnorm(TV3<T>(wi + wo)) : tnorm(TV3<T>(wi + wo * eta_));
+    if (val(dot(H, normal)) < 0.0f) H = -H;
+    const T cosHWi = dot(wi, H), cosHWo = dot(wo, H);
+    TV3<T> b0, b1;
+    tframe(normal, b0, b1);
+    const TV3<T> localH(dot(b0, H), dot(b1, H), dot(normal, H));
+    const float alpha = b.alpha;
+    const T D = ad_beckmann_d(localH, alpha);
+    const T revCosHWi = cosHWo, revCosHWo = cosHWi;
+    T ct;
+    const T F = ad_fresnel(cosHWi, ct, b.eta, b.invEta);
+    const T aCosWi = fabs(cosWi), aCosWo = fabs(cosWo);
+    const T G = ad_beckmann_g1(alpha, aCosWi) * ad_beckmann_g1(alpha, aCosWo);
+    const T scaledAlpha = alpha * (1.2f - 0.2f * sqrt(aCosWi));
+    const T prob = localH.z * ad_beckmann_d(localH, scaledAlpha);
+    const T revScaledAlpha = alpha * (1.2f - 0.2f * sqrt(aCosWo));
+    const T revProb = localH.z * ad_beckmann_d(localH, revScaledAlpha);
+    if (reflect) {
+        const T scalar = fabs(F * D * G / (4.0f * cosWi));
+        o.contrib = tv<T>(ks_of(b)) * scalar;
+        o.pdf = fabs(prob * F / (4.0f * cosHWo));
+        o.revPdf = fabs(revProb * F / (4.0f * revCosHWo));
+    } else {
+        const T sqrtDenom = cosHWi + eta_ * cosHWo;
+        const T revSqrtDenom = revCosHWi + revEta_ * revCosHWo;
+        const float factor = adjoint ? 1.0f : (1.0f / eta_) * (1.0f / eta_);
+        const T scalar = fabs(factor * ((1.0f - F) * D * G * (eta_ * eta_) * cosHWi * cosHWo) /
+                              (cosWi * (sqrtDenom * sqrtDenom)));
+        o.contrib = tv<T>(kt_of(b)) * scalar;
+        o.pdf = fabs(prob * (1.0f - F) * ((eta_ * eta_) * cosHWo) / (sqrtDenom * sqrtDenom));
+        o.revPdf = fabs(revProb * (1.0f - F) * ((revEta_ * revEta_) * revCosHWo) / (revSqrtDenom * revSqrtDenom));
+    }
+}
+
+// SampleRoughDielectric with fixDiscrete = false (src/roughdielectric.cpp:376-481).
+template <class T>
+DEV void ad_rough_dielectric_sample(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const T &r0, const T &r1,
+                                    float uDiscrete, TV3<T> &wo, TBsdf<T> &o, bool adjoint) {
+    const T cosWi = dot(wi, normal);
+    const float alpha = b.alpha;
+    const T scaledAlpha = alpha * (1.2f - 0.2f * sqrt(fabs(cosWi)));
+    // SampleMicronormal (src/microfacet.h:166-185), AD form (1e-6 floor on sin^2)
+    const T phiM = kTwoPi * r1;
+    const T alphaSqr = scaledAlpha * scaledAlpha;
+    const T tanThetaMSqr = alphaSqr * (-log(fmax(1.0f - r0, 1e-6f)));
+    const T cosThetaM = 1.0f / sqrt(1.0f + tanThetaMSqr);
+    const T cosThetaMSqr = cosThetaM * cosThetaM;
+    const T mPdf = (1.0f - r0) / (kPi * alphaSqr * cosThetaM * cosThetaMSqr);
+    const T sinThetaM = sqrt(fmax(1.0f - cosThetaMSqr, 1e-6f));
+    const TV3<T> localH(sinThetaM * cos(phiM), sinThetaM * sin(phiM), cosThetaM);
+    TV3<T> b0, b1;
+    tframe(normal, b0, b1);
+    const TV3<T> H = localH.x * b0 + localH.y * b1 + localH.z * normal;
+    const T cosHWi = dot(wi, H);
+    T cosThetaT;
+    const T F = ad_fresnel(cosHWi, cosThetaT, b.eta, b.invEta);
+    TV3<T> refl;
+    if (uDiscrete <= val(F)) {
+        wo = treflect(wi, H);
+        refl = tv<T>(ks_of(b));
+        const T cosHWo = dot(wo, H);
+        o.pdf = fabs(mPdf * F / (4.0f * cosHWo));
+        const T rev_dwh_dwo = 1.0f / (4.0f * cosHWi);
+        o.cosWo = dot(wo, normal);
+        const T revScaledAlp = alpha * (1.2f - 0.2f * sqrt(fabs(o.cosWo)));
+        o.revPdf = fabs(F * ad_beckmann_d(localH, revScaledAlp) * localH.z * rev_dwh_dwo);
+    } else {
+        const float etaR = val(cosThetaT) < 0.0f ? b.invEta : b.eta;  // Refract (src/utils.h:202-210)
+        wo = H * (dot(wi, H) * etaR + cosThetaT) - wi * etaR;
+        const float eta_ = val(cosWi) > 0.0f ? b.eta : b.invEta;
+        const float factor = adjoint ? 1.0f : (1.0f / eta_) * (1.0f / eta_);
+        refl = tv<T>(kt_of(b) * factor);
+        const T cosHWo = dot(wo, H);
+        const T sqrtDenom = cosHWi + eta_ * cosHWo;
+        const T dwh_dwo = ((eta_ * eta_) * cosHWo) / (sqrtDenom * sqrtDenom);
+        o.pdf = fabs(mPdf * (1.0f - F) * fabs(dwh_dwo));
+        o.cosWo = dot(wo, normal);
+        const float revEta_ = val(o.cosWo) > 0.0f ? b.eta : b.invEta;
+        const T revSqrtDenom = cosHWo + revEta_ * cosHWi;
+        const T rev_dwh_dwo = ((revEta_ * revEta_) * cosHWi) / (revSqrtDenom * revSqrtDenom);
+        const T revScaledAlp = alpha * (1.2f - 0.2f * sqrt(fabs(o.cosWo)));
+        o.revPdf = fabs((1.0f - F) * ad_beckmann_d(localH, revScaledAlp) * localH.z * rev_dwh_dwo);
+    }
+    const T aCosWi = fabs(cosWi), aCosWo = fabs(o.cosWo);
+    const T D = ad_beckmann_d(localH, alpha);
+    const T G = ad_beckmann_g1(alpha, aCosWi) * ad_beckmann_g1(alpha, aCosWo);
+    o.contrib = refl * fabs(D * G * cosHWi / (mPdf * aCosWi));
+}
+
+// EvaluateLambertian / EvaluatePhong / EvaluateRoughDielectric (AD forms);
+// adjoint selects EvaluateBSDF(true, ...) where the BSDF distinguishes it.
+template <class T>
+DEV void ad_evaluate(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo, TBsdf<T> &o,
+                     bool adjoint = false) {
+    if (b.type == kBsdfRoughDielectric) {
+        ad_rough_dielectric_evaluate(b, wi, normal, wo, o, adjoint);
+        return;
+    }
     T cosWi = dot(normal, wi);
     TV3<T> n = normal;
     if (!(val(cosWi) > 0.0f)) {
@@ -175,10 +324,14 @@ DEV void ad_evaluate(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, cons
     o.contrib = o.contrib * o.cosWo;
 }
 
-// SampleLambertian / SamplePhong (AD forms, fixDiscrete = false).
+// SampleLambertian / SamplePhong / SampleRoughDielectric (AD forms, fixDiscrete = false).
 template <class T>
 DEV void ad_sample(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const T &r0, const T &r1, float uDiscrete,
-                   TV3<T> &wo, TBsdf<T> &o) {
+                   TV3<T> &wo, TBsdf<T> &o, bool adjoint = false) {
+    if (b.type == kBsdfRoughDielectric) {
+        ad_rough_dielectric_sample(b, wi, normal, r0, r1, uDiscrete, wo, o, adjoint);
+        return;
+    }
     T cosWi = dot(wi, normal);
     TV3<T> n = normal;
     if (!(val(cosWi) > 0.0f)) {
@@ -321,7 +474,7 @@ DEV void ad_bsdf_sampling(const SceneView &s, int tri, const T &r0, const T &r1,
         ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o);
         jacobian = fabs(dot(nextNormal, dir) * invDistSq) / shapePdf;
     } else if (!useAbs) {
-        ad_sample(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dir, o);
+        ad_sample(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dir, o, adjoint);
     } else {
         const T scaledTheta = kTwoPi * r0;
         const T scaledPhi = kPi * r1;
@@ -329,7 +482,7 @@ DEV void ad_bsdf_sampling(const SceneView &s, int tri, const T &r0, const T &r1,
         const T cosPhi = cos(scaledPhi);
         jacobian = fabs(sinPhi);
         dir = TV3<T>(sinPhi * cos(scaledTheta), sinPhi * sin(scaledTheta), cosPhi);
-        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o);
+        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o, adjoint);
     }
     TV3<T> contrib = o.contrib;
     if (adjoint) contrib = contrib * ad_snc(ps.wi, ps.isect, dir);
@@ -410,7 +563,7 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
                     const T dist = sqrt(distSq);
                     dirToCamera = dirToCamera * (1.0f / dist);
                     TBsdf<T> o;
-                    ad_evaluate(bsdf_of_tri(s, tri), lp.wi, lp.isect.shadingNormal, dirToCamera, o);
+                    ad_evaluate(bsdf_of_tri(s, tri), lp.wi, lp.isect.shadingNormal, dirToCamera, o, true);
                     const TV3<T> bsdfContrib = o.contrib * ad_snc(lp.wi, lp.isect, dirToCamera);
                     const T invCosAtCamera = -(1.0f / dot(camDir, dirToCamera));
                     const T ip = s.cam.dist * invCosAtCamera;
@@ -522,7 +675,7 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
                     dirToLight = dirToLight * (1.0f / dist);
                     TBsdf<T> cb, lb;
                     ad_evaluate(b, cp.wi, cp.isect.shadingNormal, dirToLight, cb);
-                    ad_evaluate(bsdf_of_tri(s, lgtVertTri), lp.wi, lp.isect.shadingNormal, -dirToLight, lb);
+                    ad_evaluate(bsdf_of_tri(s, lgtVertTri), lp.wi, lp.isect.shadingNormal, -dirToLight, lb, true);
                     const TV3<T> lgtF = lb.contrib * ad_snc(lp.wi, lp.isect, -dirToLight);
                     const T G = 1.0f / distSq;
                     const T camA = cb.pdf * lb.cosWo * G;

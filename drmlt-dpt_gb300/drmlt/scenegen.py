@@ -10,6 +10,8 @@ Workloads:
     radiance 15. Walls/boxes are Lambertian with reflectance U[0.2, 0.8]^3, or
     Phong (exponent log-U[10, 1000], ks U[0.1, 0.5]) when ``phong=True``.
     Pinhole camera, fov 40 degrees.
+  * ``config3``: the Lambertian box plus a rough-dielectric (Beckmann) sphere of
+    528 smooth-shaded triangles, alpha U[0.05, 0.5] from the seed, IOR 1.5.
 """
 from __future__ import annotations
 
@@ -76,6 +78,32 @@ def _write_obj(path, quads):
         f.write("\n".join(lines) + "\n")
 
 
+def _write_sphere_obj(path, center, radius, n_theta=12, n_phi=24):
+    """UV sphere with per-vertex normals (outward), triangles wound counter-clockwise seen from outside."""
+    c = np.asarray(center, np.float64)
+    verts, norms, faces = [], [], []
+    for i in range(n_theta + 1):
+        th = np.pi * i / n_theta
+        for j in range(n_phi):
+            ph = 2.0 * np.pi * j / n_phi
+            d = np.array([np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)])
+            verts.append(c + radius * d)
+            norms.append(d)
+    idx = lambda i, j: i * n_phi + (j % n_phi) + 1
+    for i in range(n_theta):
+        for j in range(n_phi):
+            a, b, cc, d = idx(i, j), idx(i, j + 1), idx(i + 1, j + 1), idx(i + 1, j)
+            if i > 0:
+                faces.append((a, b, cc))
+            if i < n_theta - 1:
+                faces.append((a, cc, d))
+    lines = ["v %.9g %.9g %.9g" % tuple(v) for v in verts]
+    lines += ["vn %.9g %.9g %.9g" % tuple(n) for n in norms]
+    lines += ["f %d//%d %d//%d %d//%d" % (f[0], f[0], f[1], f[1], f[2], f[2]) for f in faces]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 @dataclass
 class SceneOptions:
     """The reference's ``<dpt>`` option block (src/dptoptions.h:7-38)."""
@@ -121,7 +149,7 @@ class SceneOptions:
 
 def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int = 256,
                   phong: bool = False, options: SceneOptions | None = None,
-                  filename: str = "scene.xml") -> str:
+                  filename: str = "scene.xml", sphere: dict | None = None) -> str:
     """Writes the Cornell-box workload; returns the XML path."""
     os.makedirs(outdir, exist_ok=True)
     rng = np.random.default_rng(seed)
@@ -143,6 +171,12 @@ def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int =
             bsdf = '<bsdf type="diffuse"><rgb name="reflectance" value="%.9g %.9g %.9g"/></bsdf>' % tuple(kd)
         shapes.append('  <shape type="obj"><string name="filename" value="%s.obj"/>%s</shape>'
                       % (name, bsdf))
+    if sphere is not None:
+        _write_sphere_obj(os.path.join(outdir, "sphere.obj"), sphere["center"], sphere["radius"])
+        shapes.append('  <shape type="obj"><string name="filename" value="sphere.obj"/>'
+                      '<bsdf type="roughdielectric"><float name="alpha" value="%.9g"/>'
+                      '<float name="intIOR" value="%.9g"/><float name="extIOR" value="1"/></bsdf></shape>'
+                      % (sphere["alpha"], sphere["ior"]))
     # Area light: 0.25 x 0.25 quad just below the ceiling, facing down.
     _write_obj(os.path.join(outdir, "light.obj"),
                [((-0.125, 0.999, -0.125), (0.25, 0.0, 0.0), (0.0, 0.0, 0.25))])
@@ -176,3 +210,12 @@ def config2(outdir: str, dr_type: str = "mira", spp: int = 64) -> str:
     """H2MC second stage on the Phong Cornell box at 1024x1024, max depth 8, 16384 chains."""
     return write_cornell(outdir, seed=2, width=1024, height=1024, phong=True,
                          options=SceneOptions(maxdepth=8, numchains=16384, spp=spp, type=dr_type))
+
+
+def config3(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
+    """The Lambertian Cornell box (seed 3) with a rough-dielectric sphere: alpha
+    U[0.05, 0.5] from the seed, IOR 1.5; 256x256, max depth 5, 4096 chains."""
+    alpha = float(np.random.default_rng(1003).uniform(0.05, 0.5))
+    return write_cornell(outdir, seed=3, width=256, height=256, phong=False,
+                         options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type=dr_type),
+                         sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5))

@@ -52,8 +52,8 @@ typedef struct drmlt_bsdf {
     float kd[3];         /* Lambertian reflectance / Phong diffuse */
     float ks[3];         /* Phong specular */
     float exponent;      /* Phong exponent */
-    float int_ior, ext_ior, alpha;  /* rough dielectric (not yet supported) */
-    float kt[3];
+    float int_ior, ext_ior, alpha;  /* rough dielectric (Beckmann): IORs and roughness */
+    float kt[3];         /* rough dielectric: specular transmittance (ks: reflectance) */
 } drmlt_bsdf;
 
 typedef struct drmlt_light {

@@ -64,8 +64,9 @@ static inline float modulo1(float a) { float r = std::fmod(a, 1.0f); return r < 
 // ---------------------------------------------------------------- scene
 struct Bsdf {
     int type, twoSided;
-    V3 kd, ks;
+    V3 kd, ks, kt;
     float expo, ksW;
+    float alpha, eta, invEta;  // rough dielectric (src/roughdielectric.h:10-18)
 };
 struct Light {
     int type, shape, triOff, ntri;
@@ -170,7 +171,123 @@ static void frame(V3 n, V3 &b1, V3 &b2) {
     b2 = mk(b, 1.0f - sq(n.y) * a, -n.y);
 }
 static V3 reflect(V3 wi, V3 n) { return sub(mul(n, 2.0f * dot(wi, n)), wi); }
-static void bsdf_eval(const Bsdf &b, V3 wi, V3 n, V3 wo, BOut &o) {
+// ---- rough dielectric, Beckmann microfacets (src/roughdielectric.cpp, src/microfacet.h)
+static float beck_d(V3 h, float a) {
+    const float c2 = sq(h.z);
+    return std::exp(-((sq(h.x) / sq(a) + sq(h.y) / sq(a)) / c2)) / (PI * a * a * sq(c2));
+}
+static float beck_g1(float a, float c) {
+    const float t = std::sqrt(std::fabs(1.0f - sq(c))) / c;
+    if (t <= 0.0f) return 1.0f;
+    const float x = 1.0f / (a * t);
+    if (x >= 1.6f) return 1.0f;
+    return (3.535f * x + 2.181f * x * x) / (1.0f + 2.276f * x + 2.577f * x * x);
+}
+static float fresnel(float ci_, float &ct_, float eta, float inv) {
+    const float sc = ci_ > 0.0f ? inv : eta;
+    const float ct2 = 1.0f - (1.0f - sq(ci_)) * sq(sc);
+    if (ct2 <= 0.0f) { ct_ = 0.0f; return 1.0f; }
+    const float ci = std::fabs(ci_), ct = std::sqrt(ct2);
+    const float rs = (ci - eta * ct) / (ci + eta * ct), rp = (eta * ci - ct) / (eta * ci + ct);
+    ct_ = ci_ > 0.0f ? -ct : ct;
+    return 0.5f * (sq(rs) + sq(rp));
+}
+static void rd_eval(const Bsdf &b, V3 wi, V3 n, V3 wo, BOut &o, bool adj) {
+    o.f = mk(0, 0, 0);
+    o.cosWo = 0;
+    o.pdf = o.rev = 0;
+    const float cwi = dot(wi, n);
+    if (std::fabs(cwi) < COS_EPS) return;
+    const float cwo = dot(wo, n);
+    o.cosWo = cwo;
+    if (std::fabs(cwo) < COS_EPS) return;
+    const bool refl = cwi * cwo > 0.0f;
+    const float e = cwi > 0.0f ? b.eta : b.invEta, re = cwo > 0.0f ? b.eta : b.invEta;
+    V3 H = refl ? norm(add(wi, wo)) : norm(add(wi, mul(wo, e)));
+    if (dot(H, n) < 0.0f) H = neg(H);
+    const float chi = dot(wi, H), cho = dot(wo, H);
+    if (std::fabs(chi) < COS_EPS || std::fabs(cho) < COS_EPS) return;
+    if (chi * cwi <= 0.0f || cho * cwo <= 0.0f) return;
+    V3 b0, b1;
+    frame(n, b0, b1);
+    const V3 lh = mk(dot(b0, H), dot(b1, H), dot(n, H));
+    const float D = beck_d(lh, b.alpha);
+    if (D <= 0.0f) return;
+    float ct;
+    const float F = fresnel(chi, ct, b.eta, b.invEta);
+    const float aci = std::fabs(cwi), aco = std::fabs(cwo);
+    const float G = beck_g1(b.alpha, aci) * beck_g1(b.alpha, aco);
+    const float prob = lh.z * beck_d(lh, b.alpha * (1.2f - 0.2f * std::sqrt(aci)));
+    if (prob < 1e-20f) return;
+    const float rprob = lh.z * beck_d(lh, b.alpha * (1.2f - 0.2f * std::sqrt(aco)));
+    if (refl) {
+        o.f = mul(b.ks, std::fabs(F * D * G / (4.0f * cwi)));
+        o.pdf = std::fabs(prob * F / (4.0f * cho));
+        o.rev = std::fabs(rprob * F / (4.0f * chi));
+    } else {
+        const float den = chi + e * cho, rden = cho + re * chi;
+        const float fac = adj ? 1.0f : sq(1.0f / e);
+        o.f = mul(b.kt, std::fabs(fac * ((1.0f - F) * D * G * sq(e) * chi * cho) / (cwi * sq(den))));
+        o.pdf = std::fabs(prob * (1.0f - F) * (sq(e) * cho) / sq(den));
+        o.rev = std::fabs(rprob * (1.0f - F) * (sq(re) * chi) / sq(rden));
+    }
+}
+static bool rd_sample(const Bsdf &b, V3 wi, V3 n, float r0, float r1, float ud, V3 &wo, BOut &o, bool adj) {
+    const float cwi = dot(wi, n);
+    if (std::fabs(cwi) < COS_EPS) return false;
+    // SampleMicronormal (src/microfacet.h:166-185)
+    const float sa = b.alpha * (1.2f - 0.2f * std::sqrt(std::fabs(cwi)));
+    const float phi = TWO_PI * r1, a2 = sq(sa);
+    const float t2 = a2 * (-std::log(std::max(1.0f - r0, 1e-6f)));
+    const float cm = 1.0f / std::sqrt(1.0f + t2), cm2 = sq(cm);
+    const float mpdf = (1.0f - r0) / (PI * a2 * cm * cm2);
+    const float sm = std::sqrt(std::max(1.0f - cm2, 0.0f));
+    const V3 lh = mk(sm * std::cos(phi), sm * std::sin(phi), cm);
+    V3 b0, b1;
+    frame(n, b0, b1);
+    const V3 H = add(add(mul(b0, lh.x), mul(b1, lh.y)), mul(n, lh.z));
+    const float chi = dot(wi, H);
+    if (std::fabs(chi) < COS_EPS) return false;
+    float ct = 0.0f;
+    const float F = fresnel(chi, ct, b.eta, b.invEta);
+    V3 kr;
+    float cho;
+    o.pdf = mpdf;
+    if (ud <= F) {
+        wo = reflect(wi, H);
+        if (F <= 0.0f || dot(n, wo) * dot(n, wi) <= 0.0f) return false;
+        kr = b.ks;
+        cho = dot(wo, H);
+        o.pdf = std::fabs(o.pdf * F / (4.0f * cho));
+        o.cosWo = dot(wo, n);
+        if (std::fabs(o.cosWo) < COS_EPS) return false;
+        o.rev = std::fabs(F * beck_d(lh, b.alpha * (1.2f - 0.2f * std::sqrt(std::fabs(o.cosWo)))) * lh.z *
+                          (1.0f / (4.0f * chi)));
+    } else {
+        const float er = ct < 0.0f ? b.invEta : b.eta;  // Refract (src/utils.h:202-210)
+        wo = sub(mul(H, dot(wi, H) * er + ct), mul(wi, er));
+        if (F >= 1.0f || ct == 0.0f || dot(n, wo) * dot(n, wi) >= 0.0f) return false;
+        const float e = cwi > 0.0f ? b.eta : b.invEta;
+        kr = mul(b.kt, adj ? 1.0f : sq(1.0f / e));
+        cho = dot(wo, H);
+        const float den = chi + e * cho;
+        o.pdf = std::fabs(o.pdf * (1.0f - F) * std::fabs((sq(e) * cho) / sq(den)));
+        o.cosWo = dot(wo, n);
+        if (std::fabs(o.cosWo) < COS_EPS) return false;
+        const float re = o.cosWo > 0.0f ? b.eta : b.invEta, rden = cho + re * chi;
+        o.rev = std::fabs((1.0f - F) * beck_d(lh, b.alpha * (1.2f - 0.2f * std::sqrt(std::fabs(o.cosWo)))) * lh.z *
+                          ((sq(re) * chi) / sq(rden)));
+    }
+    if (std::fabs(cho) < COS_EPS || o.pdf < 1e-20f) return false;
+    if (chi * cwi <= 0.0f || cho * o.cosWo <= 0.0f) return false;
+    const float D = beck_d(lh, b.alpha);
+    const float G = beck_g1(b.alpha, std::fabs(cwi)) * beck_g1(b.alpha, std::fabs(o.cosWo));
+    o.f = mul(kr, std::fabs((D * G * chi) / (mpdf * std::fabs(cwi))));
+    return true;
+}
+
+static void bsdf_eval(const Bsdf &b, V3 wi, V3 n, V3 wo, BOut &o, bool adj = false) {
+    if (b.type == DRMLT_BSDF_ROUGHDIELECTRIC) { rd_eval(b, wi, n, wo, o, adj); return; }
     o.f = mk(0, 0, 0);
     o.pdf = o.rev = 0;
     float cwi = dot(n, wi);
@@ -199,7 +316,8 @@ static void bsdf_eval(const Bsdf &b, V3 wi, V3 n, V3 wo, BOut &o) {
     o.f = mul(o.f, o.cosWo);
     if (maxc(o.f) < 1e-10f) o.f = mk(0, 0, 0);
 }
-static bool bsdf_sample(const Bsdf &b, V3 wi, V3 n, float r0, float r1, float ud, V3 &wo, BOut &o) {
+static bool bsdf_sample(const Bsdf &b, V3 wi, V3 n, float r0, float r1, float ud, V3 &wo, BOut &o, bool adj = false) {
+    if (b.type == DRMLT_BSDF_ROUGHDIELECTRIC) return rd_sample(b, wi, n, r0, r1, ud, wo, o, adj);
     float cwi = dot(wi, n);
     if (std::fabs(cwi) < COS_EPS) return false;
     if (cwi < 0) {
@@ -249,6 +367,7 @@ static bool bsdf_sample(const Bsdf &b, V3 wi, V3 n, float r0, float r1, float ud
     return true;
 }
 static float roughness(const Bsdf &b, float ud) {
+    if (b.type == DRMLT_BSDF_ROUGHDIELECTRIC) return b.alpha;
     return (b.type == DRMLT_BSDF_PHONG && ud < b.ksW) ? std::sqrt(2.0f / (2.0f + 4.0f * b.expo)) : 1.0f;
 }
 template <bool adj>
@@ -423,7 +542,7 @@ static bool to_camera(const Scene &s, int ld, const St &ps, const Vx &v, Em &e) 
     dc = mul(dc, 1.0f / dist);
     if (occluded(s, ps.is.p, dc, dist)) return false;
     BOut bo;
-    bsdf_eval(bsdf_of(s, v.tri), ps.wi, ps.is.ns, dc, bo);
+    bsdf_eval(bsdf_of(s, v.tri), ps.wi, ps.is.ns, dc, bo, true);
     if (iszero(bo.f)) return false;
     const float f = snc<true>(ps.wi, ps.is, dc);
     if (f <= 0) return false;
@@ -442,7 +561,7 @@ static bool bsdf_sampling(const Scene &s, const St &ps, Vx &v, St &nx, bool fres
     BOut bo;
     float ssJ, lcJ;
     if (!perturb || !v.useAbs) {
-        if (!bsdf_sample(b, ps.wi, ps.is.ns, v.rnd[0], v.rnd[1], v.disc, dir, bo)) return false;
+        if (!bsdf_sample(b, ps.wi, ps.is.ns, v.rnd[0], v.rnd[1], v.disc, dir, bo, adj)) return false;
         if (v.useAbs) {
             float th = 0.0f;
             if (!(dir.y == 0 && dir.x == 0)) {
@@ -466,7 +585,7 @@ static bool bsdf_sampling(const Scene &s, const St &ps, Vx &v, St &nx, bool fres
         const float th = TWO_PI * v.rnd[0], ph = PI * v.rnd[1], sp = std::sin(ph);
         float jac = std::fabs(sp);
         dir = mk(sp * std::cos(th), sp * std::sin(th), std::cos(ph));
-        bsdf_eval(b, ps.wi, ps.is.ns, dir, bo);
+        bsdf_eval(b, ps.wi, ps.is.ns, dir, bo, adj);
         if (iszero(bo.f) || bo.pdf <= 0) return false;
         bo.f = mul(bo.f, 1.0f / bo.pdf);
         lcJ = 1.0f / jac;
@@ -523,7 +642,7 @@ static bool connect(const Scene &s, int cd, int ld, const St &lp, const Vx &lv, 
     if (iszero(cb.f)) return false;
     const float cf = snc<false>(cp.wi, cp.is, d);
     if (cf <= 0) return false;
-    bsdf_eval(bsdf_of(s, lv.tri), lp.wi, lp.is.ns, neg(d), lb);
+    bsdf_eval(bsdf_of(s, lv.tri), lp.wi, lp.is.ns, neg(d), lb, true);
     if (iszero(lb.f)) return false;
     const float lf = snc<true>(lp.wi, lp.is, neg(d));
     if (lf <= 0) return false;

@@ -21,6 +21,7 @@ from drmlt import scene as dscene  # noqa: E402
 SCENE_WRITERS = {
     "cfg1": scenegen.config1,
     "cfg2": lambda d: scenegen.config2(d, "green"),
+    "cfg3": lambda d: scenegen.config3(d),
 }
 
 
