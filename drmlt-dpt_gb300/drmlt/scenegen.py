@@ -12,6 +12,7 @@ Workloads:
     Pinhole camera, fov 40 degrees.
   * ``config3``: the Lambertian box plus a rough-dielectric (Beckmann) sphere of
     528 smooth-shaded triangles, alpha U[0.05, 0.5] from the seed, IOR 1.5.
+  * ``config_lights``: config 3 with a point light (intensity 3) beside the area light.
 """
 from __future__ import annotations
 
@@ -149,7 +150,8 @@ class SceneOptions:
 
 def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int = 256,
                   phong: bool = False, options: SceneOptions | None = None,
-                  filename: str = "scene.xml", sphere: dict | None = None) -> str:
+                  filename: str = "scene.xml", sphere: dict | None = None,
+                  point_light: dict | None = None) -> str:
     """Writes the Cornell-box workload; returns the XML path."""
     os.makedirs(outdir, exist_ok=True)
     rng = np.random.default_rng(seed)
@@ -183,6 +185,10 @@ def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int =
     shapes.append('  <shape type="obj"><string name="filename" value="light.obj"/>'
                   '<bsdf type="diffuse"><rgb name="reflectance" value="0 0 0"/></bsdf>'
                   '<emitter type="area"><rgb name="radiance" value="15 15 15"/></emitter></shape>')
+    if point_light is not None:
+        shapes.append('  <emitter type="point"><point name="position" x="%.9g" y="%.9g" z="%.9g"/>'
+                      '<rgb name="intensity" value="%.9g %.9g %.9g"/></emitter>'
+                      % (*point_light["pos"], *point_light["intensity"]))
     sensor = ('  <sensor type="perspective">\n'
               '    <float name="fov" value="40"/>\n'
               '    <transform name="toWorld"><lookat origin="0, 0, 3.5" target="0, 0, 0" up="0, 1, 0"/></transform>\n'
@@ -219,3 +225,13 @@ def config3(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
     return write_cornell(outdir, seed=3, width=256, height=256, phong=False,
                          options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type=dr_type),
                          sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5))
+
+
+def config_lights(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
+    """Config 3 (seed 5) plus a point light of intensity 3 under the ceiling: area
+    light, point light and the rough-dielectric sphere together."""
+    alpha = float(np.random.default_rng(1005).uniform(0.05, 0.5))
+    return write_cornell(outdir, seed=5, width=256, height=256, phong=False,
+                         options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type=dr_type),
+                         sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5),
+                         point_light=dict(pos=(0.4, 0.75, 0.3), intensity=(3.0, 3.0, 3.0)))

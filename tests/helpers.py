@@ -22,6 +22,7 @@ SCENE_WRITERS = {
     "cfg1": scenegen.config1,
     "cfg2": lambda d: scenegen.config2(d, "green"),
     "cfg3": lambda d: scenegen.config3(d),
+    "cfgL": lambda d: scenegen.config_lights(d),
 }
 
 

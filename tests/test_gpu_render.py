@@ -23,7 +23,7 @@ from helpers import GOLDEN
 pytestmark = pytest.mark.gpu
 
 RENDERS = [("cfg1", "render", "green"), ("cfg2", "render_mira", "mira"), ("cfg2", "render_green", "green"),
-           ("cfg1", "render_accmap", "green"), ("cfg3", "render", "green")]
+           ("cfg1", "render_accmap", "green"), ("cfg3", "render", "green"), ("cfgL", "render", "green")]
 SINGLE_STAGE = [("cfg1", "render_h2mc", "h2mc"), ("cfg1", "render_mcmc", "mcmc")]
 
 
@@ -46,6 +46,8 @@ def _scene(cfg, dr_type, root, name="render"):
         return scenegen.config1(d, spp=16)
     if cfg == "cfg3":
         return scenegen.config3(d, spp=16)
+    if cfg == "cfgL":
+        return scenegen.config_lights(d, spp=16)
     return scenegen.config2(d, dr_type, spp=1)
 
 
