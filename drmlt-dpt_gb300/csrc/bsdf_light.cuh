@@ -369,6 +369,83 @@ DEV int light_tri(const SceneView &s, const Light &L, int lPrim) {
     return s.shapes[L.shape].triOffset + lPrim;
 }
 
+// ---------------------------------------------------------------- environment light
+// EnvLight (src/envlight.cpp:24-240) on an image with its EnvmapSampleInfo.
+DEV V3 env_at(const SceneView &s, int x, int y) {
+    // Image3::At (src/image.h:27-32) indexes y * width + x without wrapping: col + 1
+    // past the last column reads the next row's first pixel. Indexes past the
+    // image's end (undefined in the reference) are clamped to the last pixel.
+    const int i = min(y * s.envW + x, s.envW * s.envH - 1);
+    return ld3(s.envImg + 3 * i);
+}
+DEV V3 env_rep_at(const SceneView &s, int x, int y) {  // Image3::RepAt (src/image.h:33-38)
+    int yy = y % s.envH, xx = x % s.envW;
+    if (yy < 0) yy += s.envH;
+    if (xx < 0) xx += s.envW;
+    return ld3(s.envImg + 3 * (yy * s.envW + xx));
+}
+DEV float env_row_weight(const SceneView &s, int row) {
+    return __ldg(s.envRowW + (row < 0 ? 0 : (row > s.envH - 1 ? s.envH - 1 : row)));
+}
+DEV V3 xform3(const float *m, const V3 &v) {
+    return V3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+              m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+// uToIndex of SampleDirection: lower_bound over cdf[0..size], index clamped to
+// [0, size-1], u rescaled to the cell.
+DEV int env_u_to_index(const float *cdf, int size, float &u) {
+    int lo = 0, hi = size + 1;  // first index with cdf[i] >= u
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid) < u) lo = mid + 1; else hi = mid;
+    }
+    const int index = min(max(lo - 1, 0), size - 1);
+    const float c0 = __ldg(cdf + index);
+    u = (u - c0) / (__ldg(cdf + index + 1) - c0);
+    return index;
+}
+// SampleDirection (src/envlight.cpp:120-169). lPrim: the sampled pixel.
+DEV void env_sample_direction(const SceneView &s, float u0, float u1, V3 &dirToLight, V3 &value, float &pdf,
+                              int &lPrim) {
+    const int row = env_u_to_index(s.envCdfRows, s.envH, u1);
+    const int col = env_u_to_index(s.envCdfCols + row * (s.envW + 1), s.envW, u0);
+    lPrim = row * s.envW + col;
+    const float t0 = tent(u0), t1 = tent(u1);
+    const float phi = (float(col) + t0 + 0.5f) * s.envPix[0];
+    const float theta = (float(row) + t1 + 0.5f) * s.envPix[1];
+    float sinPhi, cosPhi, sinTheta, cosTheta;
+    sinPhi = sinf(phi);
+    cosPhi = cosf(phi);
+    sinTheta = sinf(theta);
+    cosTheta = cosf(theta);
+    dirToLight = xform3(s.envToWorld, V3(sinPhi * sinTheta, cosTheta, -cosPhi * sinTheta));
+    const float dx1 = t0, dx2 = 1.0f - t0, dy1 = t1, dy2 = 1.0f - t1;
+    const V3 value1 = env_at(s, col, row) * dx2 * dy2 + env_at(s, col + 1, row) * dx1 * dy2;
+    const V3 value2 = env_at(s, col, row + 1) * dx2 * dy1 + env_at(s, col + 1, row + 1) * dx1 * dy1;
+    value = value1 + value2;
+    pdf = (luminance(value1) * env_row_weight(s, row) + luminance(value2) * env_row_weight(s, row + 1)) *
+          s.envNorm / fmaxf(fabsf(sinTheta), 1e-7f);
+}
+DEV float env_position_pdf(const SceneView &s) { return kInvPi / sq(s.bsRadius); }
+
+// EnvLight::Emission (src/envlight.cpp:193-222).
+DEV void env_emission(const SceneView &s, const Light &L, const V3 &dirToLight, V3 &emission, float &directPdf,
+                      float &emissionPdf) {
+    const V3 d = xform3(s.envToLight, dirToLight);
+    const float uvx = atan2f(d.x, -d.z) * kInvTwoPi * float(s.envW) - 0.5f;
+    const float uvy = acosf(d.y) * kInvPi * float(s.envH) - 0.5f;
+    const int col = int(floorf(uvx));
+    const int row = int(floorf(uvy));
+    const float dx1 = uvx - float(col), dx2 = 1.0f - dx1, dy1 = uvy - float(row), dy2 = 1.0f - dy1;
+    const V3 value1 = env_rep_at(s, col, row) * dx2 * dy2 + env_rep_at(s, col + 1, row) * dx1 * dy2;
+    const V3 value2 = env_rep_at(s, col, row + 1) * dx2 * dy1 + env_rep_at(s, col + 1, row + 1) * dx1 * dy1;
+    emission = (value1 + value2) * L.samplingWeight;
+    const float sinTheta = sqrtf(1.0f - sq(d.y));
+    directPdf = (luminance(value1) * env_row_weight(s, row) + luminance(value2) * env_row_weight(s, row + 1)) *
+                s.envNorm / fmaxf(fabsf(sinTheta), 1e-7f);
+    emissionPdf = directPdf * env_position_pdf(s);
+}
+
 // AreaLight::SampleDirect (src/arealight.cpp:29-57).
 DEV bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &pos, float r0, float r1,
                              V3 &dirToLight, float &dist, V3 &contrib, float &cosAtLight,
@@ -391,6 +468,16 @@ DEV bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &po
         }
         return false;
     }
+    if (L.type == kLightEnv) {  // EnvLight::SampleDirect (src/envlight.cpp:171-191)
+        V3 value;
+        int lp;
+        env_sample_direction(s, r0, r1, dirToLight, value, directPdf, lp);
+        dist = INFINITY;
+        contrib = value * (1.0f / directPdf) * L.samplingWeight;
+        cosAtLight = 1.0f;
+        emissionPdf = directPdf * env_position_pdf(s);
+        return true;
+    }
     // PointLight::SampleDirect (src/pointlight.cpp): delta light at a position.
     const V3 lp(L.pos[0], L.pos[1], L.pos[2]);
     dirToLight = lp - pos;
@@ -408,6 +495,10 @@ DEV bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &po
 DEV void light_emission(const SceneView &s, int li, const V3 &dirToLight, const V3 &normalOnLight, V3 &emission,
                         float &directPdf, float &emissionPdf) {
     const Light &L = s.lights[li];
+    if (L.type == kLightEnv) {
+        env_emission(s, L, dirToLight, emission, directPdf, emissionPdf);
+        return;
+    }
     const float cosAtLight = -dot(normalOnLight, dirToLight);
     if (L.type == kLightArea && cosAtLight > 0.0f) {
         emission = V3(L.emission[0], L.emission[1], L.emission[2]);
@@ -431,6 +522,21 @@ DEV void light_emit(const SceneView &s, int li, int lPrim, float p0, float p1, f
         emission = V3(L.emission[0], L.emission[1], L.emission[2]);
         emissionPdf = 1.0f / (4.0f * kPi);
         cosAtLight = directPdf = 1.0f;
+        return;
+    }
+    if (L.type == kLightEnv) {  // EnvLight::Emit (src/envlight.cpp:224-247)
+        int lp;
+        env_sample_direction(s, d0, d1, dir, emission, directPdf, lp);
+        emission = emission * L.samplingWeight;
+        dir = -dir;
+        float ox, oy;
+        concentric_disc(p0, p1, ox, oy);
+        V3 b0, b1;
+        coordinate_system(dir, b0, b1);
+        const V3 perp = ox * b0 + oy * b1;
+        org = V3(s.bsCenter[0], s.bsCenter[1], s.bsCenter[2]) + (perp - dir) * s.bsRadius;
+        cosAtLight = 1.0f;
+        emissionPdf = directPdf * env_position_pdf(s);
         return;
     }
     V3 normal;

@@ -161,6 +161,14 @@ DEV void splat(float *film, int W, int H, float sx, float sy, float r, float g, 
     atomicAdd(px + 2, b);
 }
 
+// WeightedSplat (src/integrators/delayed/delayed.cpp:255-265): weight times the
+// stored splat, skipped when Eigen's isZero() holds for the product.
+DEV void weighted_splat(float *film, int W, int H, const float *sp, float w) {
+    const V3 v(w * sp[2], w * sp[3], w * sp[4]);
+    if (is_zero(v)) return;
+    splat(film, W, H, sp[0], sp[1], v.x, v.y, v.z);
+}
+
 // Block-aggregated statistics: one global atomic per counter per block.
 struct StatAcc {
     unsigned c[kNumStats];

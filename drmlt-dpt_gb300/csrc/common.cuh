@@ -50,7 +50,11 @@ template <class T> HD Vec3<T> cross(const Vec3<T> &a, const Vec3<T> &b) {
 template <class T> HD T sq(const T &x) { return x * x; }
 template <class T> HD T length_sq(const Vec3<T> &v) { return sq(v.x) + sq(v.y) + sq(v.z); }
 HD float luminance(const V3 &v) { return v.x * 0.212671f + v.y * 0.715160f + v.z * 0.072169f; }
-HD bool is_zero(const V3 &v) { return v.x == 0.0f && v.y == 0.0f && v.z == 0.0f; }
+// Eigen's DenseBase::isZero() with its default precision for float
+// (NumTraits<float>::dummy_precision() = 1e-5): every |component| <= 1e-5. The
+// reference rejects BSDF values and splats with this test (src/path.cpp:215,
+// 556, 651, 751, 889, 908, 1454; src/integrators/delayed/delayed.cpp:260).
+HD bool is_zero(const V3 &v) { return fabsf(v.x) <= 1e-5f && fabsf(v.y) <= 1e-5f && fabsf(v.z) <= 1e-5f; }
 HD float max_coeff(const V3 &v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
 HD bool all_finite(const V3 &v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
 HD float length(const V3 &v) { return sqrtf(v.x * v.x + v.y * v.y + v.z * v.z); }
@@ -74,6 +78,27 @@ HD void coordinate_system(const V3 &n, V3 &b1, V3 &b2) {
     const float b = -n.x * n.y * a;
     b1 = V3(1.0f - sq(n.x) * a, b, -n.x);
     b2 = V3(b, 1.0f - sq(n.y) * a, -n.y);
+}
+
+// Tent of src/utils.h:261-267 (as written there: 1 - sqrt(2u) below one half).
+HD float tent(float u) { return u < 0.5f ? 1.0f - sqrtf(2.0f * u) : sqrtf(2.0f * (u - 0.5f)) - 1.0f; }
+
+// SampleConcentricDisc of src/sampling.h:48-67.
+HD void concentric_disc(float u0, float u1, float &x, float &y) {
+    const float r1 = 2.0f * u0 - 1.0f;
+    const float r2 = 2.0f * u1 - 1.0f;
+    float phi, r;
+    if (r1 == 0.0f || r2 == 0.0f) {
+        r = phi = 0.0f;
+    } else if (sq(r1) > sq(r2)) {
+        r = r1;
+        phi = kPiOverFour * (r2 / r1);
+    } else {
+        r = r2;
+        phi = kPiOverTwo - (r1 / r2) * kPiOverFour;
+    }
+    x = r * cosf(phi);
+    y = r * sinf(phi);
 }
 
 // Spherical direction parameterisation of src/sampling.h:7-40.
@@ -190,6 +215,15 @@ struct SceneView {
     float lightWeightSum;
     float bsCenter[3];
     float bsRadius;
+    // environment light (EnvLight + EnvmapSampleInfo, src/envlight.cpp:24-81); envLight < 0: none
+    const float *envImg;      // envW x envH RGB, row-major from the top row (Image3 layout)
+    const float *envCdfRows;  // envH + 1
+    const float *envCdfCols;  // envH x (envW + 1)
+    const float *envRowW;     // envH: sin((y + 0.5) pi / envH)
+    int envLight, envW, envH;
+    float envNorm;            // 1 / (rowSum * pixelSize.x * pixelSize.y)
+    float envPix[2];          // pixelSize: 2 pi / envW, pi / envH
+    float envToWorld[9], envToLight[9];  // upper-left 3x3 of toWorld and its inverse
     Camera cam;
     Options opt;
 };

@@ -61,6 +61,47 @@ void piecewise_constant(const std::vector<float> &f, std::vector<float> &cdf, fl
     }
 }
 
+// CreateEnvmapSampleInfo (src/envlight.cpp:24-71) in single precision, with
+// the reference's accumulation order: per-row luminance CDFs over the columns,
+// a row CDF weighted by sin(theta) of the row centre, and the normalisation of
+// the sampled pdf. Returns false when the image has no finite positive weight.
+bool envmap_sample_info(const float *rgb, int width, int height, std::vector<float> &cdfRows,
+                        std::vector<float> &cdfCols, std::vector<float> &rowWeights, float &normalization,
+                        float pixelSize[2]) {
+    const float pi = 3.14159265358979323846f;
+    cdfCols.assign(size_t(width + 1) * height, 0.0f);
+    cdfRows.assign(height + 1, 0.0f);
+    rowWeights.assign(height, 0.0f);
+    size_t colPos = 0, rowPos = 0;
+    float rowSum = 0.0f;
+    cdfRows[rowPos++] = 0.0f;
+    for (int y = 0; y < height; y++) {
+        float colSum = 0.0f;
+        cdfCols[colPos++] = 0.0f;
+        for (int x = 0; x < width; x++) {
+            const float *v = rgb + 3 * (size_t(y) * width + x);
+            colSum += v[0] * 0.212671f + v[1] * 0.715160f + v[2] * 0.072169f;
+            cdfCols[colPos++] = colSum;
+        }
+        const float norm = 1.0f / colSum;
+        for (int x = 1; x < width; x++) cdfCols[colPos - x - 1] *= norm;
+        cdfCols[colPos - 1] = 1.0f;
+        const float weight = std::sin((float(y) + 0.5f) * pi / float(height));
+        rowWeights[y] = weight;
+        rowSum += colSum * weight;
+        cdfRows[rowPos++] = rowSum;
+    }
+    const float norm = 1.0f / rowSum;
+    for (int y = 1; y < height; y++) cdfRows[rowPos - y - 1] *= norm;
+    cdfRows[rowPos - 1] = 1.0f;
+    if (rowSum == 0.0f || !std::isfinite(rowSum)) return false;
+    const float twoPi = 2.0f * pi;
+    normalization = 1.0f / (rowSum * (twoPi / float(width)) * (pi / float(height)));
+    pixelSize[0] = twoPi / float(width);
+    pixelSize[1] = float(3.14159265358979323846 / double(height));
+    return true;
+}
+
 struct Renderer {
     drmlt_options opt{};
     SceneView sv{};
@@ -243,6 +284,8 @@ struct Renderer {
         // lights, light pick distribution and per-area-light triangle CDFs
         std::vector<Light> lights(sd->num_lights);
         std::vector<float> lightFunc(sd->num_lights), lightTriCdf;
+        std::vector<float> envImg, envCdfRows, envCdfCols, envRowW;
+        sv.envLight = -1;
         float weightSum = 0.0f;
         for (int i = 0; i < sd->num_lights; i++) {
             const drmlt_light &in = sd->lights[i];
@@ -278,8 +321,37 @@ struct Renderer {
                 L.numTris = sh.numTris;
                 L.invTotalArea = 1.0f / total;
                 lightTriCdf.insert(lightTriCdf.end(), cdf.begin(), cdf.end());
+            } else if (in.type == DRMLT_LIGHT_ENV) {
+                if (sv.envLight >= 0) return fail(DRMLT_E_ARG, "at most one environment light");
+                if (!in.env_rgb || in.env_width < 1 || in.env_height < 1)
+                    return fail(DRMLT_E_ARG, "environment light needs an image");
+                const size_t npix = size_t(in.env_width) * in.env_height;
+                envImg.assign(in.env_rgb, in.env_rgb + 3 * npix);
+                if (!envmap_sample_info(envImg.data(), in.env_width, in.env_height, envCdfRows, envCdfCols,
+                                        envRowW, sv.envNorm, sv.envPix))
+                    return fail(DRMLT_E_ARG, "invalid environment map");
+                // toWorld's upper-left 3x3 and, for toLight = Invert(toWorld), its inverse
+                const float *m = in.to_world;
+                const double a00 = m[0], a01 = m[1], a02 = m[2], a10 = m[4], a11 = m[5], a12 = m[6], a20 = m[8],
+                             a21 = m[9], a22 = m[10];
+                const double det = a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) +
+                                   a02 * (a10 * a21 - a11 * a20);
+                if (!(std::fabs(det) > 0.0)) return fail(DRMLT_E_ARG, "environment toWorld is singular");
+                const double inv[9] = {(a11 * a22 - a12 * a21) / det, (a02 * a21 - a01 * a22) / det,
+                                       (a01 * a12 - a02 * a11) / det, (a12 * a20 - a10 * a22) / det,
+                                       (a00 * a22 - a02 * a20) / det, (a02 * a10 - a00 * a12) / det,
+                                       (a10 * a21 - a11 * a20) / det, (a01 * a20 - a00 * a21) / det,
+                                       (a00 * a11 - a01 * a10) / det};
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) {
+                        sv.envToWorld[3 * r + c] = m[4 * r + c];
+                        sv.envToLight[3 * r + c] = float(inv[3 * r + c]);
+                    }
+                sv.envLight = i;
+                sv.envW = in.env_width;
+                sv.envH = in.env_height;
             } else if (in.type != DRMLT_LIGHT_POINT) {
-                return fail(DRMLT_E_ARG, "only area and point lights are supported yet");
+                return fail(DRMLT_E_ARG, "unknown light type");
             }
         }
         std::vector<float> lightCdf;
@@ -308,6 +380,17 @@ struct Renderer {
         if ((rc = up(&dLightCdf, lightCdf.data(), lightCdf.size()))) return rc;
         if ((rc = up(&dLightFunc, lightFunc.data(), lightFunc.size()))) return rc;
         if ((rc = up(&dLightTriCdf, lightTriCdf.data(), lightTriCdf.size()))) return rc;
+        if (sv.envLight >= 0) {
+            float *dEnv[4];
+            if ((rc = up(&dEnv[0], envImg.data(), envImg.size()))) return rc;
+            if ((rc = up(&dEnv[1], envCdfRows.data(), envCdfRows.size()))) return rc;
+            if ((rc = up(&dEnv[2], envCdfCols.data(), envCdfCols.size()))) return rc;
+            if ((rc = up(&dEnv[3], envRowW.data(), envRowW.size()))) return rc;
+            sv.envImg = dEnv[0];
+            sv.envCdfRows = dEnv[1];
+            sv.envCdfCols = dEnv[2];
+            sv.envRowW = dEnv[3];
+        }
         sv.tris = dTris;
         sv.triN = dTriN;
         sv.triP = dTriP;

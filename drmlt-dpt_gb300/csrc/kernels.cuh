@@ -396,11 +396,11 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
         const int W = p.s.cam.width, H = p.s.cam.height;
         if (!p.accMap) {
             if (cur.valid && wc > 0.0f && cur.hasSplat)
-                splat(p.d.film, W, H, cur.splat[0], cur.splat[1], wc * cur.splat[2], wc * cur.splat[3], wc * cur.splat[4]);
+                weighted_splat(p.d.film, W, H, cur.splat, wc);
             if (w1 > 0.0f && F.hasSplat)
-                splat(p.d.film, W, H, F.splat[0], F.splat[1], w1 * F.splat[2], w1 * F.splat[3], w1 * F.splat[4]);
+                weighted_splat(p.d.film, W, H, F.splat, w1);
             if (w2 > 0.0f && S.hasSplat)
-                splat(p.d.film, W, H, S.splat[0], S.splat[1], w2 * S.splat[2], w2 * S.splat[3], w2 * S.splat[4]);
+                weighted_splat(p.d.film, W, H, S.splat, w2);
         }
         // accept / swap (delayed.cpp:563-606)
         int *perm = p.d.perm + 3 * i;

@@ -511,8 +511,9 @@ DEV void generate_path_bidir(const SceneView &s, int minDepth, int maxDepth, R &
         cp.wi = -dir;
         if (hit) convert_mis(s, d, -1, org, dir, cp);
         if (d + 1 >= minDepth) {
-            const int light = hit ? area_light_of_tri(s, tri) : -1;
+            const int light = hit ? area_light_of_tri(s, tri) : s.envLight;  // GetHitLight
             if (light >= 0) {
+                if (!hit) v.tri = -1;  // a path that ends on the environment light
                 if (s.opt.useLightCoordinateSampling && d > 1 && s.lights[light].type == kLightArea)
                     light_coordinate_convert(s, f.cam[d - 1], tri, org, cp);
                 Emit e;
@@ -621,8 +622,9 @@ DEV bool generate_subpath(const SceneView &s, int camLength, int lgtLength, R &r
         cp.wi = -dir;
         if (hit) convert_mis(s, d, -1, org, dir, cp);
         if (d + 2 >= camLength && lgtLength == 0) {
-            const int light = hit ? area_light_of_tri(s, tri) : -1;
+            const int light = hit ? area_light_of_tri(s, tri) : s.envLight;
             if (light < 0) return false;
+            if (!hit) v.tri = -1;
             if (d > 1 && s.lights[light].type == kLightArea)
                 light_coordinate_convert(s, f.cam[d - 1], tri, org, cp);
             if (!handle_hit_light(s, d, light, dir, f.screen[0], f.screen[1], cp, e)) return false;
@@ -739,8 +741,9 @@ DEV bool perturb_path(const SceneView &s, const PathRec &in, const float *offset
         cp.wi = -dir;
         if (hit) convert_mis(s, d, -1, org, dir, cp);
         if (d == nc - 1 && l == 0) {
-            const int light = hit ? area_light_of_tri(s, tri) : -1;
+            const int light = hit ? area_light_of_tri(s, tri) : s.envLight;
             if (light < 0) return false;
+            if (!hit) out.tri[vi] = -1;  // the path ends on the environment light
             return handle_hit_light(s, d, light, dir, sx, sy, cp, e);
         }
         if (!hit) return false;
@@ -802,15 +805,17 @@ DEV void generate_path_direct(const SceneView &s, int px, int py, int minDepth, 
         Isect isect;
         int tri = -1;
         const bool hit = intersect(s, org, dir, minT, maxT, tri, isect);
-        const int light = hit ? area_light_of_tri(s, tri) : -1;
+        const int light = hit ? area_light_of_tri(s, tri) : s.envLight;
         if (light >= 0 && d + 1 >= minDepth) {
             V3 emission;
             float directPdf, emissionPdf;
             light_emission(s, light, dir, isect.shadingNormal, emission, directPdf, emissionPdf);
             if (emission.x + emission.y + emission.z > 0.0f) {
-                const float distSq = dist_sq(org, isect.position);
-                const float cosTheta = -dot(dir, isect.shadingNormal);
-                directPdf *= (distSq / cosTheta);
+                if (hit) {
+                    const float distSq = dist_sq(org, isect.position);
+                    const float cosTheta = -dot(dir, isect.shadingNormal);
+                    directPdf *= (distSq / cosTheta);
+                }
                 V3 contrib = cmul(throughput, emission);
                 if (d > 0) contrib = contrib * mis_weight(lastBsdfPdf, directPdf * pick_light_prob(s, light));
                 const float score = luminance(contrib);

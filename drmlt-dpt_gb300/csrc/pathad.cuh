@@ -78,6 +78,21 @@ HD HyperDual exp(const HyperDual &x) {
     const float e = expf(x.v);
     return chain(x, e, e, e);
 }
+// atan2(y, x) with its first and second partial derivatives.
+HD HyperDual atan2(const HyperDual &y, const HyperDual &x) {
+    const float r2 = x.v * x.v + y.v * y.v;
+    const float ir2 = 1.0f / r2;
+    const float fy = x.v * ir2, fx = -y.v * ir2;
+    const float ir4 = ir2 * ir2;
+    const float fyy = -2.0f * x.v * y.v * ir4, fxx = -fyy, fxy = (y.v * y.v - x.v * x.v) * ir4;
+    return HyperDual(atan2f(y.v, x.v), fy * y.a + fx * x.a, fy * y.b + fx * x.b,
+                     fy * y.ab + fx * x.ab + fyy * y.a * y.b + fxx * x.a * x.b + fxy * (y.a * x.b + x.a * y.b));
+}
+HD HyperDual acos(const HyperDual &x) {
+    const float q = 1.0f - x.v * x.v;
+    const float iq = 1.0f / sqrtf(q);
+    return chain(x, acosf(x.v), -iq, -x.v * iq / q);
+}
 HD HyperDual fabs(const HyperDual &x) { return x.v >= 0.0f ? x : -x; }
 HD HyperDual fmax(const HyperDual &x, float c) { return x.v >= c ? x : HyperDual(c); }
 HD float sqrt(float x) { return sqrtf(x); }
@@ -86,6 +101,8 @@ HD float cos(float x) { return cosf(x); }
 HD float log(float x) { return logf(x); }
 HD float exp(float x) { return expf(x); }
 HD float fabs(float x) { return fabsf(x); }
+HD float atan2(float y, float x) { return atan2f(y, x); }
+HD float acos(float x) { return acosf(x); }
 HD float fmax(float x, float c) { return fmaxf(x, c); }
 HD float val(const HyperDual &x) { return x.v; }
 HD float val(float x) { return x; }
@@ -455,6 +472,86 @@ DEV void ad_sample_primary(const Camera &c, const T &sx, const T &sy, TV3<T> &or
     dir = ad_xform_vector(c.camToWorld, d);
 }
 
+// ---------------------------------------------------------------- environment light (AD)
+// The forms of src/envlight.cpp:249-400 on the pixel the value part selects:
+// the cell's CDF bounds, image values and row weights are constants and the
+// derivatives flow through the cell-local coordinates. Image lookups use the
+// primal's indexing (Image3::At for sampling, RepAt for emission) and the
+// unwrapped column / row of the primal, so f is the primal's contribution;
+// the light's sampling weight is kept as the primal keeps it.
+template <class T>
+HD T ad_tent(const T &u) { return val(u) < 0.5f ? 1.0f - sqrt(2.0f * u) : sqrt(2.0f * (u - 0.5f)) - 1.0f; }
+
+template <class T>
+DEV void ad_env_sample_direction(const SceneView &s, const T &u0, const T &u1, TV3<T> &dirToLight, TV3<T> &value,
+                                 T &pdf) {
+    float a = val(u0), b = val(u1);
+    const int row = env_u_to_index(s.envCdfRows, s.envH, b);
+    const float *cc = s.envCdfCols + row * (s.envW + 1);
+    const int col = env_u_to_index(cc, s.envW, a);
+    const float cr0 = __ldg(s.envCdfRows + row), cr1 = __ldg(s.envCdfRows + row + 1);
+    const float cc0 = __ldg(cc + col), cc1 = __ldg(cc + col + 1);
+    const T t0 = ad_tent<T>((u0 - cc0) / (cc1 - cc0));
+    const T t1 = ad_tent<T>((u1 - cr0) / (cr1 - cr0));
+    const T phi = (t0 + float(col) + 0.5f) * s.envPix[0];
+    const T theta = (t1 + float(row) + 0.5f) * s.envPix[1];
+    const T sinPhi = sin(phi), cosPhi = cos(phi), sinTheta = sin(theta), cosTheta = cos(theta);
+    const TV3<T> d(sinPhi * sinTheta, cosTheta, -cosPhi * sinTheta);
+    const float *m = s.envToWorld;
+    dirToLight = TV3<T>(m[0] * d.x + m[1] * d.y + m[2] * d.z, m[3] * d.x + m[4] * d.y + m[5] * d.z,
+                        m[6] * d.x + m[7] * d.y + m[8] * d.z);
+    const T dx1 = t0, dx2 = 1.0f - t0, dy1 = t1, dy2 = 1.0f - t1;
+    const TV3<T> value1 = tv<T>(env_at(s, col, row)) * (dx2 * dy2) + tv<T>(env_at(s, col + 1, row)) * (dx1 * dy2);
+    const TV3<T> value2 =
+        tv<T>(env_at(s, col, row + 1)) * (dx2 * dy1) + tv<T>(env_at(s, col + 1, row + 1)) * (dx1 * dy1);
+    value = value1 + value2;
+    pdf = (tlum(value1) * env_row_weight(s, row) + tlum(value2) * env_row_weight(s, row + 1)) * s.envNorm /
+          fmax(fabs(sinTheta), 1e-7f);
+}
+
+template <class T>
+DEV void ad_env_emission(const SceneView &s, const Light &L, const TV3<T> &dirToLight, TV3<T> &emission,
+                         T &directPdf, T &emissionPdf) {
+    const float *m = s.envToLight;
+    const TV3<T> d(m[0] * dirToLight.x + m[1] * dirToLight.y + m[2] * dirToLight.z,
+                   m[3] * dirToLight.x + m[4] * dirToLight.y + m[5] * dirToLight.z,
+                   m[6] * dirToLight.x + m[7] * dirToLight.y + m[8] * dirToLight.z);
+    const T uvx = atan2(d.x, -d.z) * kInvTwoPi * float(s.envW) - 0.5f;
+    const T uvy = acos(d.y) * kInvPi * float(s.envH) - 0.5f;
+    const int col = int(floorf(val(uvx)));
+    const int row = int(floorf(val(uvy)));
+    const T dx1 = uvx - float(col), dx2 = 1.0f - dx1, dy1 = uvy - float(row), dy2 = 1.0f - dy1;
+    const TV3<T> value1 =
+        tv<T>(env_rep_at(s, col, row)) * (dx2 * dy2) + tv<T>(env_rep_at(s, col + 1, row)) * (dx1 * dy2);
+    const TV3<T> value2 =
+        tv<T>(env_rep_at(s, col, row + 1)) * (dx2 * dy1) + tv<T>(env_rep_at(s, col + 1, row + 1)) * (dx1 * dy1);
+    emission = (value1 + value2) * L.samplingWeight;
+    // EmissionEnvLight's clamp against infinite derivatives at the poles (src/envlight.cpp:353)
+    const T sinTheta = sqrt(fmax(1.0f - d.y * d.y, 1e-6f));
+    directPdf = (tlum(value1) * env_row_weight(s, row) + tlum(value2) * env_row_weight(s, row + 1)) * s.envNorm /
+                fmax(fabs(sinTheta), 1e-7f);
+    emissionPdf = directPdf * env_position_pdf(s);
+}
+
+template <class T>
+HD void ad_concentric_disc(const T &u0, const T &u1, T &x, T &y) {
+    const T r1 = 2.0f * u0 - 1.0f;
+    const T r2 = 2.0f * u1 - 1.0f;
+    T r, phi;
+    if (val(r1) == 0.0f || val(r2) == 0.0f) {
+        r = T(0.0f);
+        phi = T(0.0f);
+    } else if (val(r1) * val(r1) > val(r2) * val(r2)) {
+        r = r1;
+        phi = kPiOverFour * (r2 / r1);
+    } else {
+        r = r2;
+        phi = kPiOverTwo - (r1 / r2) * kPiOverFour;
+    }
+    x = r * cos(phi);
+    y = r * sin(phi);
+}
+
 // BSDFSampling<adjoint, false> (AD, src/path.cpp:2671-2762).
 template <class T, bool adjoint>
 DEV void ad_bsdf_sampling(const SceneView &s, int tri, const T &r0, const T &r1, float disc, bool useAbs,
@@ -522,6 +619,19 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
             cosLight = d.z;
             emissionPdf = d.z * kInvPi * L.invTotalArea;
             directPdf = T(L.invTotalArea);
+        } else if (L.type == kLightEnv) {  // EmitEnvLight (AD)
+            TV3<T> value;
+            ad_env_sample_direction(s, d0, d1, dir, value, directPdf);
+            lp.throughput = value * L.samplingWeight;
+            dir = -dir;
+            T ox, oy;
+            ad_concentric_disc(p0, p1, ox, oy);
+            TV3<T> b0, b1;
+            tframe(dir, b0, b1);
+            const TV3<T> perp = ox * b0 + oy * b1;
+            org = tv<T>(V3(s.bsCenter[0], s.bsCenter[1], s.bsCenter[2])) + (perp - dir) * s.bsRadius;
+            cosLight = T(1.0f);
+            emissionPdf = directPdf * env_position_pdf(s);
         } else {  // EmitPointLight (AD)
             org = tv<T>(V3(L.pos[0], L.pos[1], L.pos[2]));
             const T scaledTheta = kTwoPi * d0;
@@ -603,6 +713,22 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
         for (int d = 0; d < nc; d++) {
             const int vi = nl + d;
             const int tri = r.tri[vi];
+            if (d == nc - 1 && l == 0 && tri < 0) {
+                // the camera ray leaves the scene: ConvertMISLightHit leaves the MIS
+                // terms as they are, HandleHitLight with EmissionEnvLight (AD)
+                const Light &L = s.lights[s.envLight];
+                TV3<T> emission;
+                T directPdf, emissionPdf;
+                ad_env_emission(s, L, dir, emission, directPdf, emissionPdf);
+                cp.throughput = cmul(cp.throughput, emission);
+                const float pick = pick_light_prob(s, s.envLight);
+                directPdf = directPdf * pick;
+                emissionPdf = emissionPdf * pick;
+                const T wCamera = tmis(directPdf) * cp.prev + tmis(emissionPdf) * cp.cur;
+                cp.throughput = cp.throughput * (1.0f / (1.0f + wCamera));
+                contrib = cp.throughput;
+                break;
+            }
             ad_intersect(s, tri, org, dir, cp.isect);
             cp.wi = -dir;
             if (d == nc - 1 && l == 0) {
@@ -650,6 +776,12 @@ DEV T ad_eval_path(const SceneView &s, const PathRec &r, const T *u) {
                         const TV3<T> E = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2]));
                         lightContrib = TV3<T>(E.x / directPdf, E.y / directPdf, E.z / directPdf);
                         emissionPdf = L.invTotalArea * cosAtLight * kInvPi;
+                    } else if (L.type == kLightEnv) {  // SampleDirectEnvLight
+                        TV3<T> value;
+                        ad_env_sample_direction(s, r0, r1, dirToLight, value, directPdf);
+                        lightContrib = value * (1.0f / directPdf) * L.samplingWeight;
+                        cosAtLight = T(1.0f);
+                        emissionPdf = directPdf * env_position_pdf(s);
                     } else {
                         dirToLight = tv<T>(V3(L.pos[0], L.pos[1], L.pos[2])) - cp.isect.position;
                         const T distSq = dot(dirToLight, dirToLight);

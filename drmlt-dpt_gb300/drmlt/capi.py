@@ -34,7 +34,8 @@ class Bsdf(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("type", C.c_int32), ("shape", C.c_int32), ("emission", F3), ("pos", F3),
-                ("sampling_weight", C.c_float)]
+                ("sampling_weight", C.c_float), ("env_rgb", C.POINTER(C.c_float)),
+                ("env_width", C.c_int32), ("env_height", C.c_int32), ("to_world", F16)]
 
 
 class SceneDesc(C.Structure):

@@ -1,8 +1,9 @@
 """Scene front end: the reference's scene XML subset + OBJ meshes -> drmlt_scene_desc.
 
 Mirrors ParseScene / ParseSceneNode (src/parsescene.cpp:566-613) for
-<sensor type="perspective">, <shape type="obj"> with diffuse / phong / twosided
-BSDFs and area <emitter>, point <emitter>, and the <dpt> option block
+<sensor type="perspective">, <shape type="obj"> with diffuse / phong /
+roughdielectric / twosided BSDFs and area <emitter>, point and envmap (PFM
+image) <emitter>s, and the <dpt> option block
 (ParseDptOptions, src/parsescene.cpp:505-564). Camera matrices follow
 Camera::Camera (src/camera.cpp:11-28) and the transform helpers of
 src/transform.cpp, computed in double and rounded to float.
@@ -219,6 +220,20 @@ def load_obj(path: str, to_world: np.ndarray):
     return positions, normals
 
 
+def read_pfm(path: str) -> np.ndarray:
+    """A PFM image as H x W x 3 float32, top row first (Image3's layout: the
+    file stores rows bottom to top; a one-channel file is replicated to RGB as
+    Image3::Image3 does, src/image.cpp:5-43)."""
+    with open(path, "rb") as f:
+        magic = f.readline().strip()
+        w, h = map(int, f.readline().split())
+        scale = float(f.readline())
+        ch = 3 if magic == b"PF" else 1
+        data = np.frombuffer(f.read(4 * w * h * ch), "<f4" if scale < 0 else ">f4").reshape(h, w, ch)
+    img = np.ascontiguousarray(data[::-1], np.float32)
+    return np.repeat(img, 3, axis=2) if ch == 1 else img
+
+
 # ---------------------------------------------------------------- scene
 @dataclass
 class SceneData:
@@ -233,6 +248,7 @@ class SceneData:
     camera: dict
     options: DptOptions
     path: str
+    env_images: list = field(default_factory=list)  # keeps the envmap pixels behind drmlt_light.env_rgb
 
     @property
     def width(self):
@@ -294,6 +310,7 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
     bsdfs, lights = [], []
     pos_l, nor_l = [], []
     first, count, sb, sl = [], [], [], []
+    env_images = []
     ntri = 0
     for ch in root:
         if ch.tag == "dpt":
@@ -369,13 +386,35 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
                     elif e.get("name") == "intensity":
                         L.emission[:] = _vec3(e.get("value"))
                 lights.append(L)
+            elif ch.get("type") == "envmap":  # src/parsescene.cpp:477-498
+                L = capi.Light()
+                L.type = capi.LIGHT_ENV
+                L.shape = -1
+                L.sampling_weight = 1.0
+                to_world = np.eye(4)
+                fname = None
+                for e in ch:
+                    if e.get("name") == "filename":
+                        fname = e.get("value")
+                    elif e.get("name") == "samplingWeight":
+                        L.sampling_weight = float(e.get("value"))
+                    elif e.get("name") == "toWorld" and e.tag == "transform":
+                        to_world = parse_transform(e)
+                if fname is None:
+                    raise ValueError("envmap without filename")
+                img = read_pfm(os.path.join(base, fname))
+                env_images.append(img)
+                L.env_rgb = img.ctypes.data_as(C.POINTER(C.c_float))
+                L.env_height, L.env_width = img.shape[0], img.shape[1]
+                L.to_world[:] = to_world.astype(np.float32).ravel().tolist()
+                lights.append(L)
             else:
                 raise ValueError("unsupported emitter %r" % ch.get("type"))
     if cam is None:
         raise ValueError("scene has no sensor")
     return SceneData(np.concatenate(pos_l), np.concatenate(nor_l), np.asarray(first, np.int32),
                      np.asarray(count, np.int32), np.asarray(sb, np.int32), np.asarray(sl, np.int32),
-                     bsdfs, lights, cam, options, xml_path)
+                     bsdfs, lights, cam, options, xml_path, env_images)
 
 
 def camera_matrices(cam: dict) -> dict:
@@ -427,9 +466,12 @@ class SceneDescHolder:
         d.far_clip = sd.camera["far"]
         d.width = sd.camera["width"]
         d.height = sd.camera["height"]
-        lo = self.pos.reshape(-1, 3).min(0)
-        hi = self.pos.reshape(-1, 3).max(0)
-        c = 0.5 * (lo + hi)
+        # BSphere(BBox) (src/bounds.h:30-33) in single precision
+        lo = self.pos.reshape(-1, 3).min(0).astype(np.float32)
+        hi = self.pos.reshape(-1, 3).max(0).astype(np.float32)
+        c = np.float32(0.5) * (lo + hi)
+        e = hi - lo
         d.bsphere_center[:] = c.tolist()
-        d.bsphere_radius = float(np.linalg.norm(hi - c))
+        d.bsphere_radius = float(np.float32(0.5) * np.sqrt(np.float32(e[0] * e[0] + e[1] * e[1] + e[2] * e[2])))
+        self.sd = sd
         self.desc = d

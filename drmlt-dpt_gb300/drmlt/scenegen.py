@@ -13,6 +13,8 @@ Workloads:
   * ``config3``: the Lambertian box plus a rough-dielectric (Beckmann) sphere of
     528 smooth-shaded triangles, alpha U[0.05, 0.5] from the seed, IOR 1.5.
   * ``config_lights``: config 3 with a point light (intensity 3) beside the area light.
+  * ``config_env``: config 3 without its ceiling under an 8 x 4 environment map
+    (PFM, rotated 30 degrees about y) next to the area light.
 """
 from __future__ import annotations
 
@@ -148,16 +150,39 @@ class SceneOptions:
         return "  <dpt>\n%s\n  </dpt>\n" % body
 
 
+def write_pfm(path: str, img: np.ndarray) -> None:
+    """An H x W x 3 image (top row first) as a little-endian PFM (rows stored bottom to top)."""
+    img = np.asarray(img, np.float32)
+    h, w, _ = img.shape
+    with open(path, "wb") as f:
+        f.write(b"PF\n%d %d\n-1\n" % (w, h))
+        f.write(np.ascontiguousarray(img[::-1]).astype("<f4").tobytes())
+
+
+def env_image(width: int = 8, height: int = 4) -> np.ndarray:
+    """A sky-like environment map: colours per row band brightening along x.
+    Column 0 and the bottom row are black, so the importance sampler never
+    picks the last column or row and the reference's unwrapped image lookups
+    (src/envlight.cpp:159-160) stay inside the image."""
+    bands = np.array([[0.6, 0.8, 1.2], [0.9, 0.9, 0.8], [0.45, 0.4, 0.3], [0.3, 0.3, 0.3]])
+    img = np.zeros((height, width, 3), np.float32)
+    for y in range(height - 1):
+        for x in range(1, width):
+            img[y, x] = bands[min(y, len(bands) - 1)] * (0.6 + 0.6 * x / (width - 1))
+    return img
+
+
 def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int = 256,
                   phong: bool = False, options: SceneOptions | None = None,
                   filename: str = "scene.xml", sphere: dict | None = None,
-                  point_light: dict | None = None) -> str:
+                  point_light: dict | None = None, env: dict | None = None,
+                  ceiling: bool = True) -> str:
     """Writes the Cornell-box workload; returns the XML path."""
     os.makedirs(outdir, exist_ok=True)
     rng = np.random.default_rng(seed)
     options = options or SceneOptions()
     shapes = []
-    names = list(_WALLS) + list(_BOXES)
+    names = [n for n in _WALLS if ceiling or n != "ceiling"] + list(_BOXES)
     for name in names:
         quads = [_WALLS[name]] if name in _WALLS else _box_quads(*_BOXES[name])
         _write_obj(os.path.join(outdir, name + ".obj"), quads)
@@ -189,6 +214,11 @@ def write_cornell(outdir: str, *, seed: int = 1, width: int = 256, height: int =
         shapes.append('  <emitter type="point"><point name="position" x="%.9g" y="%.9g" z="%.9g"/>'
                       '<rgb name="intensity" value="%.9g %.9g %.9g"/></emitter>'
                       % (*point_light["pos"], *point_light["intensity"]))
+    if env is not None:
+        write_pfm(os.path.join(outdir, "env.pfm"), env["image"])
+        shapes.append('  <emitter type="envmap"><string name="filename" value="env.pfm"/>'
+                      '<transform name="toWorld"><rotate y="1" angle="%.9g"/></transform></emitter>'
+                      % env.get("angle", 0.0))
     sensor = ('  <sensor type="perspective">\n'
               '    <float name="fov" value="40"/>\n'
               '    <transform name="toWorld"><lookat origin="0, 0, 3.5" target="0, 0, 0" up="0, 1, 0"/></transform>\n'
@@ -235,3 +265,14 @@ def config_lights(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
                          options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type=dr_type),
                          sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5),
                          point_light=dict(pos=(0.4, 0.75, 0.3), intensity=(3.0, 3.0, 3.0)))
+
+
+def config_env(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
+    """Config 3 (seed 6) without its ceiling, lit by the area light and an 8 x 4
+    environment map rotated 30 degrees about y; the camera sees the map past
+    the box's edges."""
+    alpha = float(np.random.default_rng(1006).uniform(0.05, 0.5))
+    return write_cornell(outdir, seed=6, width=256, height=256, phong=False,
+                         options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type=dr_type),
+                         sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5),
+                         env=dict(image=env_image(), angle=30.0), ceiling=False)

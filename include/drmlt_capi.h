@@ -62,6 +62,13 @@ typedef struct drmlt_light {
     float emission[3];   /* area: radiance, point: intensity */
     float pos[3];        /* point light position */
     float sampling_weight;
+    /* environment light (EnvLight, src/envlight.h; at most one per scene): the
+     * envmap image as env_width x env_height RGB floats, row-major from the top
+     * row (the reference's Image3 layout), and toWorld as a row-major 4x4 whose
+     * upper-left 3x3 rotates directions (src/envlight.cpp:73-81). */
+    const float *env_rgb;
+    int32_t env_width, env_height;
+    float to_world[16];
 } drmlt_light;
 
 /* Triangles are listed shape by shape (shape k owns a contiguous range).

@@ -8,6 +8,7 @@
 //   re-intersection                                  src/trianglemesh.cpp:30-79,187-236
 //   Lambertian / Phong BSDFs                         src/lambertian.cpp, src/phong.cpp:21-167
 //   area / point lights                              src/arealight.cpp:29-102, src/pointlight.cpp
+//   environment light                                src/envlight.cpp:24-247
 //   camera                                           src/camera.cpp:38-75
 //   GeneratePathBidir / GenerateSubpath              src/path.cpp:978-1269
 //   PerturbPathBidir                                 src/path.cpp:1480-1628
@@ -56,7 +57,10 @@ static inline float sq(float x) { return x * x; }
 static inline float lensq(V3 a) { return sq(a.x) + sq(a.y) + sq(a.z); }
 static inline V3 norm(V3 a) { float il = 1.0f / std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); return mul(a, il); }
 static inline float lum(V3 a) { return a.x * 0.212671f + a.y * 0.715160f + a.z * 0.072169f; }
-static inline bool iszero(V3 a) { return a.x == 0 && a.y == 0 && a.z == 0; }
+// Eigen's isZero() at its default float precision 1e-5, the test the reference
+// applies to BSDF values and splats (src/path.cpp:556, 651, 751, 889, 908, 1454;
+// delayed.cpp:260).
+static inline bool iszero(V3 a) { return std::fabs(a.x) <= 1e-5f && std::fabs(a.y) <= 1e-5f && std::fabs(a.z) <= 1e-5f; }
 static inline float maxc(V3 a) { return std::max(a.x, std::max(a.y, a.z)); }
 static inline float mis(float x) { return x * x; }
 static inline float modulo1(float a) { float r = std::fmod(a, 1.0f); return r < 0 ? r + 1.0f : r; }
@@ -86,6 +90,12 @@ struct Scene {
     float s2c[16], c2s[16], c2w[16], w2c[16], dist, nearc, farc;
     int W, H;
     drmlt_options opt;
+    V3 bsC;
+    float bsR;
+    // environment light: image (top row first), EnvmapSampleInfo, toWorld / toLight 3x3
+    int envL, envW, envH;
+    std::vector<float> envImg, envRows, envCols, envRowW;
+    float envNorm, envPix[2], envW2L[9], envL2W[9];
 };
 
 static void piecewise(const std::vector<float> &f, std::vector<float> &cdf, float &fi) {
@@ -400,9 +410,65 @@ static int pick_light(const Scene &s, float u, float &prob) {
     return id;
 }
 static float pick_prob(const Scene &s, int li) { return s.lights[li].w / s.lightWeightSum; }
+// ---------------------------------------------------------------- environment light
+static float tent(float u) { return u < 0.5f ? 1.0f - std::sqrt(2.0f * u) : std::sqrt(2.0f * (u - 0.5f)) - 1.0f; }
+static V3 env_px(const Scene &s, int i) { return mk(s.envImg[3 * i], s.envImg[3 * i + 1], s.envImg[3 * i + 2]); }
+// Image3::At: unwrapped y * width + x (the last pixel stands in past the end).
+static V3 env_at(const Scene &s, int x, int y) { return env_px(s, std::min(y * s.envW + x, s.envW * s.envH - 1)); }
+static V3 env_rep(const Scene &s, int x, int y) {
+    const int yy = ((y % s.envH) + s.envH) % s.envH, xx = ((x % s.envW) + s.envW) % s.envW;
+    return env_px(s, yy * s.envW + xx);
+}
+static float env_rw(const Scene &s, int row) { return s.envRowW[std::min(std::max(row, 0), s.envH - 1)]; }
+static V3 rot3(const float *m, V3 v) {
+    return mk(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z, m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+// uToIndex (src/envlight.cpp:128-133): std::lower_bound over cdf[0..n].
+static int env_index(const float *cdf, int n, float &u) {
+    const int e = int(std::lower_bound(cdf, cdf + n + 1, u) - cdf);
+    const int i = std::min(std::max(e - 1, 0), n - 1);
+    u = (u - cdf[i]) / (cdf[i + 1] - cdf[i]);
+    return i;
+}
+static void env_sample_dir(const Scene &s, float u0, float u1, V3 &dir, V3 &val, float &pdf) {
+    const int row = env_index(s.envRows.data(), s.envH, u1);
+    const int col = env_index(s.envCols.data() + row * (s.envW + 1), s.envW, u0);
+    const float t0 = tent(u0), t1 = tent(u1);
+    const float phi = (float(col) + t0 + 0.5f) * s.envPix[0], th = (float(row) + t1 + 0.5f) * s.envPix[1];
+    const float sp = std::sin(phi), cp = std::cos(phi), st = std::sin(th), ct = std::cos(th);
+    dir = rot3(s.envL2W, mk(sp * st, ct, -cp * st));
+    const V3 v1 = add(mul(mul(env_at(s, col, row), 1.0f - t0), 1.0f - t1), mul(mul(env_at(s, col + 1, row), t0), 1.0f - t1));
+    const V3 v2 = add(mul(mul(env_at(s, col, row + 1), 1.0f - t0), t1), mul(mul(env_at(s, col + 1, row + 1), t0), t1));
+    val = add(v1, v2);
+    pdf = (lum(v1) * env_rw(s, row) + lum(v2) * env_rw(s, row + 1)) * s.envNorm / std::max(std::fabs(st), 1e-7f);
+}
+static float env_pos_pdf(const Scene &s) { return INV_PI / sq(s.bsR); }
+static void env_emission(const Scene &s, const Light &L, V3 dirToLight, V3 &E, float &dp, float &ep) {
+    const V3 d = rot3(s.envW2L, dirToLight);
+    const float ux = std::atan2(d.x, -d.z) * INV_TWO_PI * float(s.envW) - 0.5f;
+    const float uy = std::acos(d.y) * INV_PI * float(s.envH) - 0.5f;
+    const int col = int(std::floor(ux)), row = int(std::floor(uy));
+    const float dx1 = ux - float(col), dy1 = uy - float(row);
+    const V3 v1 = add(mul(mul(env_rep(s, col, row), 1.0f - dx1), 1.0f - dy1), mul(mul(env_rep(s, col + 1, row), dx1), 1.0f - dy1));
+    const V3 v2 = add(mul(mul(env_rep(s, col, row + 1), 1.0f - dx1), dy1), mul(mul(env_rep(s, col + 1, row + 1), dx1), dy1));
+    E = mul(add(v1, v2), L.w);
+    const float st = std::sqrt(1.0f - sq(d.y));
+    dp = (lum(v1) * env_rw(s, row) + lum(v2) * env_rw(s, row + 1)) * s.envNorm / std::max(std::fabs(st), 1e-7f);
+    ep = dp * env_pos_pdf(s);
+}
+
 static bool sample_direct(const Scene &s, int li, int prim, V3 pos, float r0, float r1, V3 &dir, float &dist, V3 &c,
                           float &cosL, float &dpdf, float &epdf) {
     const Light &L = s.lights[li];
+    if (L.type == DRMLT_LIGHT_ENV) {
+        V3 val;
+        env_sample_dir(s, r0, r1, dir, val, dpdf);
+        dist = INFINITY;
+        c = mul(mul(val, 1.0f / dpdf), L.w);
+        cosL = 1.0f;
+        epdf = dpdf * env_pos_pdf(s);
+        return true;
+    }
     if (L.type == DRMLT_LIGHT_AREA) {
         V3 p, n;
         tri_sample(s, ltri(s, li, prim), r0, r1, p, n);
@@ -509,6 +575,24 @@ static void emit_light(const Scene &s, float pick, int li, int prim, const float
         cosL = z;
         ep = z * INV_PI * L.invArea;
         dpd = L.invArea;
+    } else if (L.type == DRMLT_LIGHT_ENV) {
+        V3 val;
+        env_sample_dir(s, dp[0], dp[1], d, val, dpd);
+        ps.T = mul(val, L.w);
+        d = neg(d);
+        // SampleConcentricDisc (src/sampling.h:48-67)
+        const float r1 = 2.0f * pp[0] - 1.0f, r2 = 2.0f * pp[1] - 1.0f;
+        float r = 0.0f, phi = 0.0f;
+        if (r1 != 0.0f && r2 != 0.0f) {
+            if (sq(r1) > sq(r2)) { r = r1; phi = (0.25f * PI) * (r2 / r1); }
+            else { r = r2; phi = 0.5f * PI - (r1 / r2) * (0.25f * PI); }
+        }
+        V3 b1, b2;
+        frame(d, b1, b2);
+        const V3 perp = add(mul(b1, r * std::cos(phi)), mul(b2, r * std::sin(phi)));
+        o = add(s.bsC, mul(sub(perp, d), s.bsR));
+        cosL = 1.0f;
+        ep = dpd * env_pos_pdf(s);
     } else {
         o = L.pos;
         const float th = TWO_PI * dp[0], ph = PI * dp[1];
@@ -619,10 +703,19 @@ static bool direct(const Scene &s, int cd, const St &ps, float sx, float sy, flo
 }
 static bool hit_light(const Scene &s, int cd, int li, V3 d, float sx, float sy, const St &ps, Em &e) {
     const Light &L = s.lights[li];
-    const float cosL = -dot(ps.is.ns, d);
-    if (!(L.type == DRMLT_LIGHT_AREA && cosL > 0)) return false;
-    float dp = L.invArea, ep = cosL * dp * INV_PI;
-    V3 c = cmul(ps.T, L.E);
+    float dp, ep;
+    V3 E;
+    if (L.type == DRMLT_LIGHT_ENV) {
+        env_emission(s, L, d, E, dp, ep);
+        if (!(E.x + E.y + E.z > 0)) return false;
+    } else {
+        const float cosL = -dot(ps.is.ns, d);
+        if (!(L.type == DRMLT_LIGHT_AREA && cosL > 0)) return false;
+        dp = L.invArea;
+        ep = cosL * dp * INV_PI;
+        E = L.E;
+    }
+    V3 c = cmul(ps.T, E);
     if (cd > 0) {
         const float pk = pick_prob(s, li);
         dp *= pk;
@@ -772,8 +865,9 @@ static void gen_bidir(const Scene &s, int minD, int maxD, R &rng, Full &f, Sink 
         cp.wi = neg(d);
         if (hit) conv_mis(s, k, -1, o, d, cp);
         if (k + 1 >= minD) {
-            const int li = hit ? light_of(s, tri) : -1;
+            const int li = hit ? light_of(s, tri) : s.envL;
             if (li >= 0) {
+                if (!hit) v.tri = -1;
                 if (s.opt.use_light_coordinate_sampling && k > 1 && s.lights[li].type == DRMLT_LIGHT_AREA)
                     lc_convert(s, f.cm[k - 1], tri, o, cp);
                 Em e;
@@ -861,8 +955,9 @@ static bool gen_subpath(const Scene &s, int camL, int lgtL, R &rng, drmlt_path &
         cp.wi = neg(d);
         if (hit) conv_mis(s, k, -1, o, d, cp);
         if (k + 2 >= camL && lgtL == 0) {
-            const int li = hit ? light_of(s, tri) : -1;
+            const int li = hit ? light_of(s, tri) : s.envL;
             if (li < 0) return false;
+            if (!hit) v.tri = -1;
             if (k > 1 && s.lights[li].type == DRMLT_LIGHT_AREA) lc_convert(s, f.cm[k - 1], tri, o, cp);
             if (!hit_light(s, k, li, d, f.screen[0], f.screen[1], cp, e)) return false;
             make_rec(f, camL, 0, rec);
@@ -956,7 +1051,8 @@ static bool perturb(const Scene &s, const drmlt_path &in, const float *off, J &j
         cp.wi = neg(d);
         if (hit) conv_mis(s, q, -1, o, d, cp);
         if (q == nc - 1 && l == 0) {
-            const int li = hit ? light_of(s, tri) : -1;
+            const int li = hit ? light_of(s, tri) : s.envL;
+            if (!hit) out.tri[vi] = -1;  // the path ends on the environment light
             return li >= 0 && hit_light(s, q, li, d, sx, sy, cp, e);
         }
         if (!hit) return false;
@@ -1010,11 +1106,21 @@ static void gen_direct(const Scene &s, int px, int py, int minD, int maxD, R &rn
         Isect is;
         int tri = -1;
         const bool hit = intersect(s, o, d, t0, t1, tri, is);
-        const int li = hit ? light_of(s, tri) : -1;
+        const int li = hit ? light_of(s, tri) : s.envL;
         if (li >= 0 && k + 1 >= minD) {
             const Light &L = s.lights[li];
-            const float cosL = -dot(is.ns, d);
-            if (L.type == DRMLT_LIGHT_AREA && cosL > 0) {
+            const float cosL = hit ? -dot(is.ns, d) : 0.0f;
+            if (L.type == DRMLT_LIGHT_ENV) {
+                V3 E;
+                float dp, ep;
+                env_emission(s, L, d, E, dp, ep);
+                if (E.x + E.y + E.z > 0) {
+                    V3 c = cmul(T, E);
+                    if (k > 0) c = mul(c, 1.0f / (1.0f + sq((dp * pick_prob(s, li)) / lastPdf)));
+                    Em e;
+                    if (fin(e, 2 + k, 0, sx, sy, c, 1.0f)) sink(e);
+                }
+            } else if (L.type == DRMLT_LIGHT_AREA && cosL > 0) {
                 float dp = L.invArea * (lensq(sub(o, is.p)) / (-dot(d, is.ns)));
                 V3 c = cmul(T, L.E);
                 if (k > 0) c = mul(c, 1.0f / (1.0f + sq((dp * pick_prob(s, li)) / lastPdf)));

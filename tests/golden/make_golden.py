@@ -44,6 +44,7 @@ CONFIGS = {
     "cfg2": (lambda d: scenegen.config2(d, "green"), 8, dict(bidir=100, subpath=200, direct=100, tech=100, perturb=6)),
     "cfg3": (lambda d: scenegen.config3(d), 5, dict(bidir=200, subpath=300, direct=200, tech=200, perturb=6)),
     "cfgL": (lambda d: scenegen.config_lights(d), 5, dict(bidir=200, subpath=300, direct=200, tech=200, perturb=6)),
+    "cfgE": (lambda d: scenegen.config_env(d), 5, dict(bidir=200, subpath=300, direct=200, tech=250, perturb=6)),
 }
 
 # full renders: (output suffix, scene writer with the render's spp, derivative depth)
@@ -55,6 +56,7 @@ RENDERS = {
              ("render_accmap", lambda d: scenegen.config1(d, spp=16, acceptance_map=True), 5)],
     "cfg3": [("render", lambda d: scenegen.config3(d, spp=16), 5)],
     "cfgL": [("render", lambda d: scenegen.config_lights(d, spp=16), 5)],
+    "cfgE": [("render", lambda d: scenegen.config_env(d, spp=16), 5)],
     "cfg2": [("render_mira", lambda d: scenegen.config2(d, "mira", spp=1), 8),
              ("render_green", lambda d: scenegen.config2(d, "green", spp=1), 8)],
 }

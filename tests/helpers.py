@@ -23,6 +23,7 @@ SCENE_WRITERS = {
     "cfg2": lambda d: scenegen.config2(d, "green"),
     "cfg3": lambda d: scenegen.config3(d),
     "cfgL": lambda d: scenegen.config_lights(d),
+    "cfgE": lambda d: scenegen.config_env(d),
 }
 
 
@@ -90,3 +91,60 @@ def rel_err(a, b, floor=1e-30):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+def ss_rtol(p: dict, base: float = 1e-4) -> float:
+    """Tolerance for a contribution's ss score (ls times the primary-sample
+    Jacobian). An absolute-parameter vertex contributes |sin(pi u1)| of its
+    direction's spherical coordinates (src/path.cpp:623-642); near the poles
+    that factor amplifies the last-ulp differences of a float direction by
+    about 1 / sin^2, so the tolerance widens with it."""
+    s = [abs(np.sin(np.pi * v["bsdfRnd"][1])) for v in p["lgtSurf"] + p["camSurf"] if v["useAbs"]]
+    m = min(s) if s else 1.0
+    return max(base, 1e-6 / max(m * m, 1e-12))
+
+
+def env_light_index(sd) -> int:
+    for i, L in enumerate(sd.lights):
+        if L.type == capi.LIGHT_ENV:
+            return i
+    return -1
+
+
+def chad_env_defect(rec: dict, env: int) -> bool:
+    """Technique paths where the chad-generated function is not the reference's
+    own primal on the environment light, so chad's f and derivatives are not
+    a reference for them:
+      * paths ending on the environment light whose chad log f differs from
+        the log of the reference's primal ss score: EmissionEnvLight
+        (src/envlight.cpp:330-357) takes the cell coordinates of the wrapped
+        pixel index, which are off by the image width or height wherever the
+        unwrapped column or row is negative;
+      * paths emitted by the environment light whose disc sample falls in the
+        |2 u0 - 1| > |2 u1 - 1| half: the generated SampleConcentricDisc
+        (src/sampling.h:70-97) evaluates its last branch there.
+    """
+    p = rec["path"]
+    if env < 0:
+        return False
+    if p["lgtDepth"] == 0 and p["camSurf"] and p["camSurf"][-1]["shape"] < 0:
+        lf = rec["logf"]
+        return lf is None or abs(lf - np.log(rec["contrib"][0]["ss"])) > 1e-4 * max(1.0, abs(lf))
+    if p["lgtDepth"] >= 2 and p["lgtLight"] == env:
+        r1, r2 = 2.0 * p["lgtPos"][0] - 1.0, 2.0 * p["lgtPos"][1] - 1.0
+        return r1 != 0.0 and r2 != 0.0 and r1 * r1 > r2 * r2
+    return False
+
+
+def chad_hessian_consistent(rec: dict) -> bool:
+    """Whether chad's Hessian is the derivative of chad's own gradient: within
+    2% of the central differences of that gradient (fixture field `fdHess`,
+    h = 1e-3, itself accurate to a few 0.1%) and symmetric to 1e-3. It is not
+    for light paths connected to the camera (c = 1), for some rough-dielectric
+    paths, and on the direction rows of some environment-emitted paths."""
+    d = rec["dim"]
+    hr = np.array(rec["hess"]).reshape(d, d)
+    hfd = np.array(rec["fdHess"]).reshape(d, d)
+    top = max(np.max(np.abs(hfd)), 1e-6)
+    return (rec["path"]["camDepth"] != 1 and np.max(np.abs(hr - hfd)) <= 2e-2 * top
+            and np.max(np.abs(hr - hr.T)) <= 1e-3 * max(np.max(np.abs(hr)), 1e-6))

@@ -21,8 +21,8 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 pytestmark = pytest.mark.gpu
 
-CFGS = ["cfg1", "cfg2", "cfg3", "cfgL"]
-MAX_DEPTH = {"cfg1": 5, "cfg2": 8, "cfg3": 5, "cfgL": 5}
+CFGS = ["cfg1", "cfg2", "cfg3", "cfgL", "cfgE"]
+MAX_DEPTH = {"cfg1": 5, "cfg2": 8, "cfg3": 5, "cfgL": 5, "cfgE": 5}
 
 
 @pytest.fixture(scope="module")

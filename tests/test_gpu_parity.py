@@ -11,11 +11,11 @@ each test bounds that fraction explicitly.
 import numpy as np
 import pytest
 
-from helpers import golden, path_record, rel_err
+from helpers import chad_env_defect, chad_hessian_consistent, env_light_index, golden, path_record, rel_err, ss_rtol
 
 pytestmark = pytest.mark.gpu
 
-CFGS = ["cfg1", "cfg2", "cfg3", "cfgL"]
+CFGS = ["cfg1", "cfg2", "cfg3", "cfgL", "cfgE"]
 
 
 def _lum(c):
@@ -33,13 +33,13 @@ def _first_tri(r):
     return r.scene.shape_first_tri
 
 
-def _cmp_contrib(mine, ref, tol=1e-4):
+def _cmp_contrib(mine, ref, tol=1e-4, ss_tol=1e-4):
     ok = True
     ok &= np.allclose(mine["screen"], ref["screen"], atol=2e-5, rtol=0)
     ok &= bool(np.all(rel_err(mine["rgb"], ref["contrib"], 1e-12) < tol) or
                np.allclose(mine["rgb"], ref["contrib"], rtol=tol, atol=1e-9))
     ok &= bool(rel_err(mine["ls"], ref["ls"], 1e-12) < tol)
-    ok &= bool(rel_err(mine["ss"], ref["ss"], 1e-12) < tol or (ref["ss"] == 0 and mine["ss"] == 0))
+    ok &= bool(rel_err(mine["ss"], ref["ss"], 1e-12) < ss_tol or (ref["ss"] == 0 and mine["ss"] == 0))
     return ok
 
 
@@ -54,14 +54,9 @@ def test_bootstrap_sampler_replay(renderers, cfg):
     for i, rec in enumerate(recs):
         ref = {(c["camDepth"], c["lightDepth"]): c for c in rec["contribs"]}
         mine = {(int(tech[i, k, 0]), int(tech[i, k, 1])): ct[i, k] for k in range(cnt[i])}
-        # extra, negligible contributions where the reference emits none (the
-        # rough-dielectric scene; the oracle shows the same) are not mismatches
-        top = max([_lum(c["contrib"]) for c in ref.values()] + [1e-30])
-        extra = set(mine) - set(ref)
-        negligible = all(_lum(mine[k]["rgb"]) <= max(1e-3 * top, 1e-9) for k in extra)
-        good = cons[i] == rec["consumed"] and set(ref) <= set(mine) and negligible
+        good = cons[i] == rec["consumed"] and set(ref) == set(mine)
         if good:
-            good = all(_cmp_contrib(mine[k], ref[k]) for k in ref)
+            good = all(_cmp_contrib(mine[k], ref[k], ss_tol=ss_rtol(rec["path"])) for k in ref)
         bad += 0 if good else 1
     assert bad <= max(1, len(recs) // 50), "%d / %d bootstrap samples differ" % (bad, len(recs))
 
@@ -81,7 +76,7 @@ def test_large_step_sampler_replay(renderers, cfg):
         good = cons[i] == rec["consumed"] and cnt[i] == len(rec["contribs"])
         if good and cnt[i]:
             nvalid += 1
-            good = _cmp_contrib(ct[i, 0], rec["contribs"][0])
+            good = _cmp_contrib(ct[i, 0], rec["contribs"][0], ss_tol=ss_rtol(rec["path"]))
             exp = path_record(rec["path"], rec["camLength"], rec["lgtLength"], _first_tri(r))
             L = rec["camLength"] + rec["lgtLength"] - 1
             nv = (rec["lgtLength"] - 1 if rec["lgtLength"] > 1 else 0) + rec["camLength"] - 1
@@ -89,7 +84,7 @@ def test_large_step_sampler_replay(renderers, cfg):
             good = good and np.allclose(pth[i]["u"][:2 * L], exp["u"][:2 * L], atol=2e-5)
             good = good and np.array_equal(pth[i]["disc"][:nv], exp["disc"][:nv])
         bad += 0 if good else 1
-    assert nvalid > len(recs) // 10
+    assert nvalid > len(recs) // 20
     assert bad <= max(1, len(recs) // 50), "%d / %d large steps differ" % (bad, len(recs))
 
 
@@ -133,13 +128,11 @@ def test_small_step_perturbation(renderers, cfg):
     nvalid = 0
     for i, (rec, pt) in enumerate(refs):
         dim = rec["dim"]
-        if ct[i]["valid"] and not pt["contribs"] and ct[i]["ls"] <= 1e-6 * rec["contrib"][0]["ls"]:
-            continue  # extra, negligible contribution (see the bootstrap test)
         good = np.allclose(out[i]["u"][:dim], pt["ypos"], atol=2e-6)
         good = good and bool(ct[i]["valid"]) == (len(pt["contribs"]) == 1)
         if good and ct[i]["valid"]:
             nvalid += 1
-            good = _cmp_contrib(ct[i], pt["contribs"][0])
+            good = _cmp_contrib(ct[i], pt["contribs"][0], ss_tol=ss_rtol(pt["path"]))
         bad += 0 if good else 1
     assert nvalid > len(refs) // 4
     assert bad <= max(1, len(refs) // 50), "%d / %d perturbations differ" % (bad, len(refs))
@@ -151,12 +144,14 @@ def test_path_derivatives_vs_chad(renderers, cfg):
 
     Tolerances: f 1e-4, gradient and Hessian 1e-3 relative to the largest
     reference entry. Exception: where chad's Hessian is not the derivative of
-    chad's own gradient -- light paths connected to the camera (technique c = 1,
-    ConnectToCamera), and paths where chad's Hessian is more than 2% away from
-    the central differences of its gradient (fixture field `fdHess`, h = 1e-3;
-    some rough-dielectric paths) -- the CUDA Hessian (the exact Hessian of the
-    same function) is compared with those differences instead, at the
-    differences' own accuracy (2e-2, Frobenius), or with chad (1e-3).
+    chad's own gradient (helpers.chad_hessian_consistent: light paths connected
+    to the camera, some rough-dielectric and environment-emitted paths) the
+    CUDA Hessian (the exact Hessian of the same function) is compared with the
+    central differences of chad's gradient instead, at the differences' own
+    accuracy (2e-2, Frobenius), or with chad (1e-3). Paths on which chad's
+    function is not the reference's primal (helpers.chad_env_defect) are left
+    to the comparison with the oracle's FP64 derivatives; paths ending on the
+    environment light must have f = log of the reference's primal ss (1e-4).
     """
     recs = [rec for rec in _need(cfg, "tech") if rec["haveDerv"] and not rec["scrubbed"]
             and rec["contrib"][0]["ss"] > 1e-15]
@@ -172,9 +167,18 @@ def test_path_derivatives_vs_chad(renderers, cfg):
     us = np.array(us)
     logf = r.path_eval(paths, us)
     g, h = r.path_grad_hess(paths, us)
-    bad_fg, bad_h, n_cam = [], [], 0
+    env = env_light_index(r.scene)
+    bad_fg, bad_h, n_cam, n_defect = [], [], 0, 0
     for i, rec in enumerate(recs):
         d = rec["dim"]
+        p = rec["path"]
+        if env >= 0 and p["lgtDepth"] == 0 and p["camSurf"][-1]["shape"] < 0:
+            lss = np.log(rec["contrib"][0]["ss"])
+            if abs(logf[i] - lss) > 1e-4 * max(1.0, abs(lss)):
+                bad_fg.append((i, "primal", logf[i], lss))
+        if chad_env_defect(rec, env):
+            n_defect += 1
+            continue
         gr = np.array(rec["grad"])
         hr = np.array(rec["hess"]).reshape(d, d)
         gm = g[i, :d]
@@ -184,8 +188,7 @@ def test_path_derivatives_vs_chad(renderers, cfg):
         if not (e_f < 1e-4 and e_g < 1e-3):
             bad_fg.append((i, e_f, e_g))
         hfd = np.array(rec["fdHess"]).reshape(d, d)
-        chad_consistent = np.max(np.abs(hr - hfd)) <= 2e-2 * max(np.max(np.abs(hfd)), 1e-6)
-        if rec["path"]["camDepth"] == 1 or not chad_consistent:
+        if not chad_hessian_consistent(rec):
             # either reference may be off here: chad's Hessian, or the float
             # differences where they straddle a kink; accept agreement with either
             n_cam += 1
@@ -198,6 +201,7 @@ def test_path_derivatives_vs_chad(renderers, cfg):
             if e_h > 1e-3:
                 bad_h.append((i, "chad", e_h))
     tol = max(1, len(recs) // 50)
+    assert n_defect <= 0.2 * len(recs), n_defect
     assert len(bad_fg) <= tol, "f/gradient mismatches: %s" % bad_fg[:5]
     assert len(bad_h) <= max(tol, n_cam // 20), "Hessian mismatches: %s" % bad_h[:10]
 

@@ -7,11 +7,11 @@ import sys
 import numpy as np
 import pytest
 
-from helpers import REPO, golden, path_record, scene_xml
+from helpers import REPO, chad_env_defect, chad_hessian_consistent, env_light_index, golden, path_record, scene_xml, ss_rtol
 
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
-CFGS = ["cfg1", "cfg2", "cfg3", "cfgL"]
+CFGS = ["cfg1", "cfg2", "cfg3", "cfgL", "cfgE"]
 
 
 @pytest.fixture(scope="module")
@@ -37,28 +37,18 @@ def lum(c):
 @pytest.mark.parametrize("cfg", CFGS)
 def test_oracle_bootstrap_sampler(oracles, cfg):
     """Same techniques, contributions (1e-4) and consumed uniforms as the
-    reference. On the rough-dielectric scene the restatement emits, in a few
-    samples, extra contributions where the reference emits none; they are
-    allowed when each is below 1e-3 of the sample's largest contribution
-    (luminance) or below 1e-9, and at most 6% of the samples have one."""
+    reference; ss to the conditioning of its spherical Jacobians (ss_rtol)."""
     recs = golden(cfg, "bidir")
     o = oracles(cfg)
     cnt, tech, ct, _, cons = o.replay(0, [r["uniforms"] for r in recs])
-    n_extra = 0
     for i, rec in enumerate(recs):
         ref = {(c["camDepth"], c["lightDepth"]): c for c in rec["contribs"]}
         mine = {(int(tech[i, k, 0]), int(tech[i, k, 1])): ct[i, k] for k in range(cnt[i])}
         assert cons[i] == rec["consumed"], i
-        assert set(ref) <= set(mine), i
-        extra = set(mine) - set(ref)
-        if extra:
-            n_extra += 1
-            top = max([lum(c["contrib"]) for c in ref.values()] + [1e-30])
-            assert all(lum(mine[k]["rgb"]) <= 1e-3 * top or lum(mine[k]["rgb"]) <= 1e-9 for k in extra), (i, extra)
+        assert set(ref) == set(mine), i
         for k, c in ref.items():
             np.testing.assert_allclose(mine[k]["rgb"], c["contrib"], rtol=1e-4, atol=1e-12)
-            np.testing.assert_allclose(mine[k]["ss"], c["ss"], rtol=1e-4, atol=1e-30)
-    assert n_extra <= 0.06 * len(recs), n_extra
+            np.testing.assert_allclose(mine[k]["ss"], c["ss"], rtol=ss_rtol(rec["path"]), atol=1e-30)
 
 
 @pytest.mark.parametrize("cfg", CFGS)
@@ -84,9 +74,6 @@ def test_oracle_direct_pass(oracles, cfg):
                                       [r["pixel"][1] for r in recs], 8)
     for i, rec in enumerate(recs):
         assert cons[i] == rec["consumed"], i
-        if cnt[i] > len(rec["contribs"]):  # extra negligible contributions (see the bootstrap test)
-            assert all(lum(ct[i, k]["rgb"]) <= 1e-9 for k in range(len(rec["contribs"]), cnt[i])), i
-            continue
         assert cnt[i] == len(rec["contribs"]), i
         for k, c in enumerate(rec["contribs"]):
             np.testing.assert_allclose(ct[i, k]["rgb"], c["contrib"], rtol=1e-4, atol=1e-12)
@@ -109,11 +96,6 @@ def test_oracle_perturbation(oracles, cfg):
     out, ct = o.perturb(np.array(paths), np.array(offs))
     n_early = 0
     for i, (rec, pt) in enumerate(refs):
-        if ct[i]["valid"] and not pt["contribs"]:
-            # an extra, negligible contribution (see the bootstrap test); the
-            # reference's perturbation stopped part-way, so its positions differ
-            assert ct[i]["ls"] <= 1e-6 * rec["contrib"][0]["ls"], i
-            continue
         if not ct[i]["valid"] and not pt["contribs"] and not np.allclose(out[i]["u"][:rec["dim"]], pt["ypos"], atol=2e-6):
             # both rejected, but stopped at different vertices (the positions of a
             # rejected proposal are never used); bounded below
@@ -122,7 +104,7 @@ def test_oracle_perturbation(oracles, cfg):
         np.testing.assert_allclose(out[i]["u"][:rec["dim"]], pt["ypos"], atol=2e-6)
         assert bool(ct[i]["valid"]) == (len(pt["contribs"]) == 1), i
         if ct[i]["valid"]:
-            np.testing.assert_allclose(ct[i]["ss"], pt["contribs"][0]["ss"], rtol=1e-4, atol=1e-30)
+            np.testing.assert_allclose(ct[i]["ss"], pt["contribs"][0]["ss"], rtol=ss_rtol(pt["path"]), atol=1e-30)
     assert n_early <= 0.005 * len(refs), n_early
 
 
@@ -141,28 +123,39 @@ def test_oracle_derivatives(oracles, cfg):
     """Forward-over-reverse (FP64 tape) vs chad and vs FP64 central differences (h = 1e-4).
 
     Gradient vs chad 1e-3 everywhere. Hessian vs chad 1e-3 wherever chad's
-    Hessian is the derivative of chad's own gradient: not for light paths
-    connected to the camera (c = 1), and not where it is more than 2% away from
-    the central differences of that gradient (fixture field `fdHess`; some
-    rough-dielectric paths); there only the check below applies. Hessian vs FP64 differences 1e-3
+    Hessian is the derivative of chad's own gradient (chad_hessian_consistent);
+    elsewhere only the check below applies. Hessian vs FP64 differences 1e-3
     on at least 90% of paths (differences straddling a branch of the path
-    function are not derivatives)."""
+    function are not derivatives).
+
+    Environment light: paths that end on it have f = log of the reference's
+    primal ss score (1e-4); chad is compared only where it is the reference's
+    primal too (chad_env_defect), the other paths rely on the differences."""
     o = oracles(cfg)
     recs, P, U = _deriv_records(cfg, o)
+    env = env_light_index(o.scene)
     f, gfd, hfd = o.fd_derivs(P, U, 1e-4)
+    _, gfd6, _ = o.fd_derivs(P, U, 1e-6)  # gradient differences closer in (Tent's kink at 0.5)
     g, h = o.tape_derivs(P, U.astype(np.float32))
-    n_fd_ok = 0
+    n_fd_ok = n_defect = 0
     for i, r in enumerate(recs):
         d = r["dim"]
+        p = r["path"]
+        if env >= 0 and p["lgtDepth"] == 0 and p["camSurf"][-1]["shape"] < 0:
+            assert abs(f[i] - np.log(r["contrib"][0]["ss"])) <= 1e-4 * max(1.0, abs(f[i])), i
+        if np.max(np.abs(h[i, :d * d] - hfd[i, :d * d])) <= 1e-3 * np.max(np.abs(hfd[i, :d * d])):
+            n_fd_ok += 1
+        if chad_env_defect(r, env):
+            n_defect += 1
+            assert np.max(np.abs(g[i, :d] - gfd6[i, :d])) <= 1e-3 * np.max(np.abs(gfd6[i, :d])), i
+            continue
         assert abs(f[i] - r["logf"]) <= 1e-4 * max(1.0, abs(r["logf"])), i
         assert np.max(np.abs(g[i, :d] - r["grad"])) <= 1e-3 * np.max(np.abs(r["grad"])), i
         hr = np.array(r["hess"])
-        hfc = np.array(r["fdHess"])
-        if r["path"]["camDepth"] != 1 and np.max(np.abs(hr - hfc)) <= 2e-2 * np.max(np.abs(hfc)):
+        if chad_hessian_consistent(r):
             assert np.max(np.abs(h[i, :d * d] - hr)) <= 1e-3 * np.max(np.abs(hr)), i
-        if np.max(np.abs(h[i, :d * d] - hfd[i, :d * d])) <= 1e-3 * np.max(np.abs(hfd[i, :d * d])):
-            n_fd_ok += 1
     assert n_fd_ok >= 0.9 * len(recs), (n_fd_ok, len(recs))
+    assert n_defect <= 0.2 * len(recs), n_defect
 
 
 @pytest.mark.parametrize("cfg", CFGS)
