@@ -10,6 +10,12 @@ chain state resident in HBM; `e2e` is the same metric through the public C ABI
 from host buffers (scene upload, prepass, direct pass, K steps, film readback).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload config2|config4|config5]
+
+--workload config4 / config5 run the large procedural scenes of
+drmlt/procedural.py instead (3.0 M / 8.0 M triangles, max depth 12, 65536 /
+262144 chains; scene built in memory). Their CPU legs are not run: the
+oracle's brute-force intersector costs O(triangles) per ray.
 
 Under torchrun (N > 1) every rank renders its own shard of chains (different
 random streams) and the films are summed; chains are independent, so there is
@@ -107,6 +113,23 @@ def write_workload(tmp: str, spp: int = 64) -> str:
                                   options=scenegen.SceneOptions(maxdepth=8, numchains=16384, spp=spp, type="mira"))
 
 
+LARGE = {
+    "config4": ("drmlt-h2mc-displaced-sphere-3.0Mtris-env-point-1024x1024-depth12-65536chains-mira", "config4"),
+    "config5": ("drmlt-h2mc-caustic-heightfield-8.0Mtris-2048x2048-depth12-262144chains-mira", "config5"),
+}
+
+
+def load_workload(name: str, tmp: str):
+    """(scene data, XML path or None, workload label) of a bench workload."""
+    from drmlt import procedural
+    from drmlt import scene as dscene
+    if name == "config2":
+        xml = write_workload(tmp)
+        return dscene.load_scene(xml), xml, WORKLOAD
+    label, fn = LARGE[name]
+    return getattr(procedural, fn)(), None, label
+
+
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
 # HBM). A Slot is 328 B, the per-chain scratch 128 B (both asserted in
 # csrc/chain.cuh), a stored FP64 Gaussian 5008 B.
@@ -125,14 +148,15 @@ def run_ours(args, world, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     tmp = tempfile.mkdtemp()
-    xml = write_workload(tmp)
-    sd = dscene.load_scene(xml)
+    sd, xml, label = load_workload(args.workload, tmp)
+    N = sd.options.numChains
     seed = 0x1234ABCD + 7919 * rank
 
     # ---- device-timed throughput (chain state resident in HBM)
     r = Renderer(sd, device=local, seed=seed)
     r.direct()
     r.prepass()
+    lanes, dwarps = r.autotune(8)  # launch shape for this scene (drmlt_autotune)
     r.run(args.warmup)
     prof, prof_mut = r.profile(max(1, min(8, args.steps)))  # per-stage CUDA-event times (serialised)
     torch.cuda.synchronize()
@@ -167,31 +191,33 @@ def run_ours(args, world, rank, local):
     t0 = time.perf_counter()
     r2 = Renderer(sd, device=local, seed=seed + 1)
     r2.prepass()
-    e_done = r2.run(args.steps)
+    r2.autotune(8)
+    r2.run(args.steps)
     film = r2.film()
     e2e_s = time.perf_counter() - t0
+    e_done = r2.stats()["mutations"]  # the autotuner's iterations included
     r2.close()
     scene_bytes = sd.positions.nbytes + sd.normals.nbytes + 64 * 4
-    e2e = {"value": done / e2e_s * world, "unit": "mutations/s", "h2d_bytes_per_step": scene_bytes // args.steps,
+    e2e = {"value": e_done / e2e_s * world, "unit": "mutations/s", "h2d_bytes_per_step": scene_bytes // args.steps,
            "d2h_bytes_per_step": film.nbytes // args.steps}
 
     # ---- roofline of the dominant stage kernel
     hbm, peak_kind = _peaks()
     stage_bytes = {
-        "stage1": 16384 * (2 * SLOT_B + SCRATCH_B),
-        "stage2": 16384 * (2 * SLOT_B + SCRATCH_B),
-        "finish": 16384 * (3 * SLOT_B + SCRATCH_B),
+        "stage1": N * (2 * SLOT_B + SCRATCH_B),
+        "stage2": N * (2 * SLOT_B + SCRATCH_B),
+        "finish": N * (3 * SLOT_B + SCRATCH_B),
         "derivs_x": 0, "derivs_z": 0, "gauss_x": 0, "gauss_z": 0,
     }
-    iters = max(1, prof_mut // 16384)
+    iters = max(1, prof_mut // N)
     dom = max(prof, key=prof.get)
     per_launch_ms = prof[dom] / iters
     # derivative / Gaussian stages: bytes = path records read + grad/Hessian or Gaussian written per listed chain
     if dom.startswith("derivs"):
-        listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // 16384)) if stats["mutations"] else 1
+        listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // N)) if stats["mutations"] else 1
         stage_bytes[dom] = listed * (SLOT_B + 4 * (24 + 576))
     if dom.startswith("gauss"):
-        listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // 16384)) if stats["mutations"] else 1
+        listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // N)) if stats["mutations"] else 1
         stage_bytes[dom] = listed * (4 * (24 + 576) + GAUSS_B)
     achieved = stage_bytes[dom] / (per_launch_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -201,14 +227,21 @@ def run_ours(args, world, rank, local):
     out = None
     if rank == 0:
         relmse = time_to_relmse(sd, local) if not args.no_relmse else None
-        cpu = cpu_baseline_sample(xml) if not args.no_cpu else None
+        if xml is None:
+            cpu = {"value": None, "unit": "mutations/s", "cores": 0, "kind": "port",
+                   "sample": "not run: the oracle's brute-force intersector costs O(triangles) per ray"}
+        else:
+            cpu = cpu_baseline_sample(xml) if not args.no_cpu else None
+        gb = (3 * SLOT_B + 3 * GAUSS_B + SCRATCH_B) * N / 1e9
         out = {
             "metric": METRIC, "value": value, "unit": "mutations/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "chains": 16384, "width": 1024, "height": 1024, "max_depth": 8,
-                       "dr_type": "mira", "mutations_per_step": 16384 * world,
-                       "l2": "chain state (3 slots + 3 FP64 Gaussians per chain, 0.27 GB) exceeds L2"},
+            "config": {"workload": label, "chains": N, "width": sd.width, "height": sd.height,
+                       "max_depth": sd.options.maxDepth, "triangles": int(len(sd.positions)),
+                       "dr_type": sd.options.type, "mutations_per_step": N * world,
+                       "launch_shape": {"chains_per_warp": lanes, "derivative_warps": dwarps, "autotuned": True},
+                       "l2": "chain state (3 slots + 3 FP64 Gaussians per chain, %.2f GB) exceeds L2" % gb},
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
@@ -250,11 +283,13 @@ def time_to_relmse(sd, device, target=0.01, ref_spp=64):
     t0 = time.perf_counter()
     r.direct()
     r.prepass()
+    direct_img = r.film().astype(np.float64)  # before any chain iteration: the direct pass alone
+    r.autotune(8)
     setup_s = time.perf_counter() - t0
-    direct_img = r.film().astype(np.float64)
     total = r.total_iterations()
-    done, run_s, hit, checkpoints = 0, 0.0, None, []
-    step = 8
+    done = r.stats()["mutations"] // sd.options.numChains  # the autotuner's iterations (part of setup_s)
+    run_s, hit, checkpoints = 0.0, None, []
+    step = max(8, done)
     while done < total:
         n = min(step, total - done)
         r.run(n)
@@ -318,6 +353,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE measurement")
+    ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"])
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":

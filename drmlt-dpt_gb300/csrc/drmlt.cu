@@ -473,21 +473,36 @@ struct Renderer {
         const int minDepth = std::max(opt.min_depth, 3);
         const int ns = opt.num_init_samples;
         if (ns <= 0) return fail(DRMLT_E_ARG, "num_init_samples must be positive");
-        const int cap = ns * 8;
-        BootRecord *dRec;
+        // Contribution records: 8 per bootstrap path first; the kernel counts every
+        // contribution, so an overflowing pass is rerun once (same streams, same
+        // records) with the exact count.
+        long long cap = (long long)ns * 8;
+        BootRecord *dRec = nullptr;
         int *dCount;
         int rc;
-        if ((rc = dalloc(&dRec, size_t(cap)))) return rc;
+        int hc[2] = {0, 0};
         if ((rc = dalloc(&dCount, 2))) return rc;
-        CK(cudaMemsetAsync(dCount, 0, 2 * sizeof(int), stream));
-        k_bootstrap<<<(ns + 127) / 128, 128, 0, stream>>>(sv, bootSeed, ns, minDepth, opt.max_depth, dRec, dCount, cap,
-                                                          dCount + 1);
-        CK(cudaGetLastError());
-        int hc[2];
-        CK(cudaMemcpyAsync(hc, dCount, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        if (hc[1]) {
+        for (int attempt = 0; attempt < 2; attempt++) {
+            if (cap > (1ll << 31) - 1) {
+                cudaFree(dCount);
+                return fail(DRMLT_E_OVERFLOW, "bootstrap contribution count exceeds 2^31");
+            }
+            if ((rc = dalloc(&dRec, size_t(cap)))) {
+                cudaFree(dCount);
+                return rc;
+            }
+            CK(cudaMemsetAsync(dCount, 0, 2 * sizeof(int), stream));
+            k_bootstrap<<<(ns + 127) / 128, 128, 0, stream>>>(sv, bootSeed, ns, minDepth, opt.max_depth, dRec, dCount,
+                                                              int(cap), dCount + 1);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(hc, dCount, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            if (!hc[1]) break;
             cudaFree(dRec);
+            dRec = nullptr;
+            cap = (long long)(unsigned)hc[0] + 1;
+        }
+        if (hc[1]) {
             cudaFree(dCount);
             return fail(DRMLT_E_OVERFLOW, "bootstrap contribution buffer overflow");
         }
@@ -723,6 +738,61 @@ struct Renderer {
         return DRMLT_OK;
     }
 
+    // Launch-shape autotuner: times `per` real iterations under each candidate
+    // number of chains per warp in the per-chain stage kernels, keeps the
+    // fastest, then does the same for the number of warps sharing one chain's
+    // derivatives. The timed iterations are part of the render: the launch shape
+    // never changes which steps the chains take. Stops early when the render
+    // has fewer than `per` iterations left.
+    int autotune(int per, int *lanesOut, int *warpsOut) {
+        if (!prepassDone) return fail(DRMLT_E_STATE, "autotune before prepass");
+        if (per < 1) return fail(DRMLT_E_ARG, "autotune needs at least one iteration per candidate");
+        static const int kLanes[] = {2, 4, 8, 16, 32};
+        static const int kWarps[] = {1, 2, 4};
+        int bestL = params().lanes, bestW = params().derivWarps;
+        float bestMs = INFINITY;
+        auto trial = [&](int lanes, int warps, float &ms) -> int {
+            ms = -1.0f;
+            if (total_iterations() - iterDone < per) return DRMLT_OK;
+            opt.stage_lanes = lanes;
+            opt.deriv_warps = warps;
+            if (graph) {
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+            }
+            if (int rc = run(per, nullptr)) return rc;
+            ms = lastRunMs / float(per);
+            return DRMLT_OK;
+        };
+        float ms;
+        for (int L : kLanes) {
+            if (int rc = trial(L, bestW, ms)) return rc;
+            if (ms < 0.0f) break;
+            if (ms < bestMs) {
+                bestMs = ms;
+                bestL = L;
+            }
+        }
+        for (int w : kWarps) {
+            if (w == bestW) continue;
+            if (int rc = trial(bestL, w, ms)) return rc;
+            if (ms < 0.0f) break;
+            if (ms < bestMs) {
+                bestMs = ms;
+                bestW = w;
+            }
+        }
+        opt.stage_lanes = bestL;
+        opt.deriv_warps = bestW;
+        if (graph) {
+            cudaGraphExecDestroy(graph);
+            graph = nullptr;
+        }
+        if (lanesOut) *lanesOut = bestL;
+        if (warpsOut) *warpsOut = bestW;
+        return DRMLT_OK;
+    }
+
     int film(float *rgb) {
         const size_t n = size_t(W) * H * 3;
         std::vector<float> ind(n), dir(n);
@@ -773,6 +843,7 @@ void drmlt_default_options(drmlt_options *o) {
     o->chain_groups = 0;
     o->stage_lanes = 0;
     o->deriv_warps = 0;
+    o->autotune = 1;
     o->smem_carveout = -1;
 }
 
@@ -820,7 +891,17 @@ int drmlt_render(void *handle) {
     if (rc) return rc;
     rc = r->prepass(nullptr);
     if (rc) return rc;
-    return r->run(r->total_iterations(), nullptr);
+    // autotune on renders long enough that its 7 candidate runs are a small part
+    if (r->opt.autotune && r->total_iterations() >= 64 * 8) {
+        rc = r->autotune(8, nullptr, nullptr);
+        if (rc) return rc;
+    }
+    return r->run(r->total_iterations() - r->iterDone, nullptr);
+}
+
+int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes, int *deriv_warps) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    return static_cast<Renderer *>(handle)->autotune(iterations_per_candidate, stage_lanes, deriv_warps);
 }
 
 int drmlt_get_film(void *handle, float *rgb) {

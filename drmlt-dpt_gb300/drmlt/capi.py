@@ -61,7 +61,7 @@ class Options(C.Structure):
                 ("use_light_coordinate_sampling", C.c_int32), ("max_derivative_depth", C.c_int32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("use_graph", C.c_int32),
                 ("chain_groups", C.c_int32), ("stage_lanes", C.c_int32), ("deriv_warps", C.c_int32),
-                ("smem_carveout", C.c_int32)]
+                ("smem_carveout", C.c_int32), ("autotune", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -107,6 +107,7 @@ _SIGS = {
     "drmlt_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "drmlt_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "drmlt_kernel_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "drmlt_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "drmlt_profile": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int64)]),
     "drmlt_total_iterations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "drmlt_path_eval": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),

@@ -112,6 +112,13 @@ class Renderer:
         capi.check(capi.lib().drmlt_kernel_launches(self.handle, C.byref(n)))
         return n.value
 
+    def autotune(self, iterations_per_candidate: int = 8):
+        """drmlt_autotune: (chains per warp, derivative warps) it settled on."""
+        lanes, warps = C.c_int(), C.c_int()
+        capi.check(capi.lib().drmlt_autotune(self.handle, int(iterations_per_candidate), C.byref(lanes),
+                                             C.byref(warps)))
+        return lanes.value, warps.value
+
     STAGES = ("stage1", "derivs_x", "gauss_x", "stage2", "derivs_z", "gauss_z", "finish")
 
     def profile(self, iterations: int):

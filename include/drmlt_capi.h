@@ -123,6 +123,8 @@ typedef struct drmlt_options {
     int32_t deriv_warps;          /* warps sharing one chain's Hessian entries, 1..4 (0 = 2) */
     int32_t smem_carveout;        /* shared-memory carveout (percent) for every chain-loop kernel,
                                      -1 = the driver's choice per kernel */
+    int32_t autotune;             /* drmlt_render picks stage_lanes / deriv_warps with drmlt_autotune
+                                     (default 1; renders of fewer than 512 iterations are not tuned) */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
@@ -194,6 +196,14 @@ int drmlt_get_stats(void *handle, drmlt_stats *stats);
 int drmlt_last_run_ms(void *handle, float *ms);
 /* Kernels launched by drmlt_run on this handle so far (all chain groups). */
 int drmlt_kernel_launches(void *handle, int64_t *n);
+
+/* Launch-shape autotuner (after drmlt_prepass): runs `iterations_per_candidate`
+ * iterations of the render under each candidate chains-per-warp count of the
+ * per-chain stage kernels (2, 4, 8, 16, 32) and then each derivative team size
+ * (1, 2, 4 warps), timed with CUDA events, and keeps the fastest pair (written
+ * to the outputs, which may be NULL). The iterations count toward the render;
+ * the launch shape does not change the chains' steps. */
+int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes, int *deriv_warps);
 
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
  * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,

@@ -137,6 +137,26 @@ def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
         np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
 
 
+def test_autotuner_keeps_the_chains(built_lib, scene_root):
+    """drmlt_autotune runs real iterations under each candidate launch shape and
+    settles on one of them; the render is the one an untuned render gives
+    (same counters, film equal up to the order of the splat additions)."""
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
+    with Renderer(sd, num_chains=4096) as a, Renderer(sd, num_chains=4096) as b:
+        a.prepass()
+        lanes, warps = a.autotune(2)
+        assert lanes in (2, 4, 8, 16, 32) and warps in (1, 2, 4)
+        tuned = a.stats()["mutations"] // 4096
+        assert tuned == 2 * 7
+        a.run(30 - tuned)
+        b.prepass()
+        b.run(30)
+        assert a.stats() == b.stats()
+        np.testing.assert_allclose(a.film(), b.film(), rtol=1e-4, atol=1e-6)
+
+
 @pytest.mark.parametrize("cfg,name,integrator", SINGLE_STAGE)
 def test_single_stage_integrators_match_reference(built_lib, scene_root, cfg, name, integrator):
     """integrator=h2mc (H2MC small step with uniform mixing, h2mc.cpp:200-240,
