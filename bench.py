@@ -127,7 +127,8 @@ def load_workload(name: str, tmp: str):
         xml = write_workload(tmp)
         return dscene.load_scene(xml), xml, WORKLOAD
     label, fn = LARGE[name]
-    return getattr(procedural, fn)(), None, label
+    # enough samples per pixel that the autotuner, warm-up and timed steps fit in one render
+    return getattr(procedural, fn)(spp=64 if name == "config4" else 32), None, label
 
 
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
@@ -171,6 +172,7 @@ def run_ours(args, world, rank, local):
     dev_ms = r.last_run_ms()
     torch.cuda.synchronize()
     stats = r.stats()
+    rays = ray_roofline(r, _peaks()[0]) if rank == 0 else None
     r.close()
     if world > 1:
         t = torch.tensor([dev_ms], device="cuda")
@@ -226,7 +228,13 @@ def run_ours(args, world, rank, local):
 
     out = None
     if rank == 0:
-        relmse = time_to_relmse(sd, local) if not args.no_relmse else None
+        relmse = relmse_plain = None
+        if not args.no_relmse:
+            ref_spp = 256
+            ref = render_reference(sd, local, ref_spp)
+            spp = 64 if args.workload == "config2" else 128
+            relmse = time_to_relmse(sd, local, ref, ref_spp, spp=spp)
+            relmse_plain = time_to_relmse(sd, local, ref, ref_spp, spp=spp, plain=True)
         if xml is None:
             cpu = {"value": None, "unit": "mutations/s", "cores": 0, "kind": "port",
                    "sample": "not run: the oracle's brute-force intersector costs O(triangles) per ray"}
@@ -245,7 +253,9 @@ def run_ours(args, world, rank, local):
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
+            "rays": rays,
             "time_to_relmse": relmse,
+            "time_to_relmse_plain": relmse_plain,
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "wall_s_timed_region": wall,
@@ -258,33 +268,63 @@ def run_ours(args, world, rank, local):
     return out
 
 
+def ray_roofline(r, hbm_gbs, n_rays=1 << 21, repeats=10):
+    """Rays/s of the BVH traversal kernel alone on the workload's scene
+    (drmlt_ray_benchmark) and the bytes it visits: nodes fetched x 64 B +
+    triangles tested x 48 B per pass over the kernel's event-timed duration,
+    against the HBM peak (the upper levels of the tree sit in L2, so the
+    fraction can exceed what DRAM alone delivers)."""
+    out = {}
+    for kind in r.RAY_KINDS:
+        b = r.ray_benchmark(kind, n_rays, repeats)
+        sec = b["ms"] * 1e-3
+        gbs = (64.0 * b["nodes"] + 48.0 * b["tris"]) / sec / 1e9
+        out[kind] = {"rays_per_s": b["rays"] / sec, "ms_per_pass": b["ms"], "rays": int(b["rays"]),
+                     "nodes_per_ray": b["nodes"] / max(b["rays"], 1), "tris_per_ray": b["tris"] / max(b["rays"], 1),
+                     "visited_gbs": gbs, "frac_of_hbm": gbs / hbm_gbs}
+    return out
+
+
 def rel_mse(img, ref):
     """Mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2)."""
     return float(np.mean((img - ref) ** 2 / (ref * ref + 1e-2)))
 
 
-def time_to_relmse(sd, device, target=0.01, ref_spp=64):
+# The plain per-stage-launch GPU drop-in: the same kernels launched one stage
+# at a time on one stream without CUDA graphs, one chain per lane in the
+# per-chain kernels, one warp per chain's derivatives, no launch autotuning.
+PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, deriv_warps=1)
+
+
+def render_reference(sd, device, spp):
+    from drmlt.integrator import Renderer
+    r = Renderer(sd, device=device, seed=0xBADC0FFE, spp=spp)
+    r.render()
+    img = r.film().astype(np.float64)
+    r.close()
+    return img
+
+
+def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False):
     """Seconds of GPU rendering until the image is within relMSE `target` of a
-    long render (ref_spp samples per pixel, different random streams) of the
-    same scene: the direct-lighting pass, the prepass and the chain-loop device
-    time up to the first checkpoint (doubling iteration counts) that meets the
-    target. Partial images scale the indirect film by total / done iterations."""
+    long render (`ref`, ref_spp samples per pixel, other random streams) of the
+    same scene: the direct-lighting pass, the prepass (and the autotuner's
+    iterations) plus the chain-loop device time up to the first checkpoint
+    (iteration counts growing by 1.25x) that meets the target. Partial images
+    scale the indirect film by total / done iterations. plain=True runs the
+    plain per-stage-launch configuration (PLAIN) without autotuning."""
     from drmlt.integrator import Renderer
 
-    def render_ref():
-        r = Renderer(sd, device=device, seed=0xBADC0FFE, spp=ref_spp)
-        r.render()
-        img = r.film().astype(np.float64)
-        r.close()
-        return img
-
-    ref = render_ref()
-    r = Renderer(sd, device=device, seed=0x5EED1234)
+    kw = dict(PLAIN) if plain else {}
+    if spp:
+        kw["spp"] = spp
+    r = Renderer(sd, device=device, seed=0x5EED1234, **kw)
     t0 = time.perf_counter()
     r.direct()
     r.prepass()
     direct_img = r.film().astype(np.float64)  # before any chain iteration: the direct pass alone
-    r.autotune(8)
+    if not plain:
+        r.autotune(8)
     setup_s = time.perf_counter() - t0
     total = r.total_iterations()
     done = r.stats()["mutations"] // sd.options.numChains  # the autotuner's iterations (part of setup_s)
@@ -297,15 +337,16 @@ def time_to_relmse(sd, device, target=0.01, ref_spp=64):
         done += n
         img = direct_img + (r.film().astype(np.float64) - direct_img) * (total / done)
         e = rel_mse(img, ref)
-        checkpoints.append([done, round(setup_s + run_s, 4), e])
+        checkpoints.append([done, round(setup_s + run_s, 4), round(e, 6)])
         if e <= target:
             hit = setup_s + run_s
             break
-        step = done
+        step = max(8, done // 4)
     r.close()
     return {"value": hit, "unit": "s", "target_relmse": target, "reference": "%d spp GPU render" % ref_spp,
             "setup_s": setup_s, "iterations": done, "spp_equivalent": done * sd.options.numChains /
-            (sd.width * sd.height), "checkpoints": checkpoints}
+            (sd.width * sd.height), "mutations_per_s": done * sd.options.numChains / max(run_s, 1e-9),
+            "checkpoints": checkpoints}
 
 
 def cpu_baseline_sample(xml: str, seconds: float = 15.0):

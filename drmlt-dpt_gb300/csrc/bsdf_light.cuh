@@ -181,7 +181,7 @@ DEV bool rough_dielectric_sample(const Bsdf &b, const V3 &wi, const V3 &normal, 
 // Lambertian::Evaluate (src/lambertian.cpp:15-38), Phong::Evaluate (src/phong.cpp:21-62),
 // RoughDielectric::Evaluate / EvaluateAdjoint (src/roughdielectric.cpp:126-144).
 template <bool adjoint = false>
-DEV void bsdf_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &wo, BsdfOut &o) {
+DEV_SHARED void bsdf_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &wo, BsdfOut &o) {
     if (b.type == kBsdfRoughDielectric) {
         rough_dielectric_evaluate<adjoint>(b, wi, normal, wo, o);
         return;
@@ -227,7 +227,7 @@ DEV void bsdf_evaluate(const Bsdf &b, const V3 &wi, const V3 &normal, const V3 &
 // Lambertian::Sample (src/lambertian.cpp:56-90), Phong::Sample (src/phong.cpp:64-147),
 // RoughDielectric::Sample / SampleAdjoint (src/roughdielectric.cpp:256-282).
 template <bool adjoint = false>
-DEV bool bsdf_sample(const Bsdf &b, const V3 &wi, const V3 &normal, float r0, float r1, float uDiscrete,
+DEV_SHARED bool bsdf_sample(const Bsdf &b, const V3 &wi, const V3 &normal, float r0, float r1, float uDiscrete,
                      V3 &wo, BsdfOut &o) {
     if (b.type == kBsdfRoughDielectric) return rough_dielectric_sample<adjoint>(b, wi, normal, r0, r1, uDiscrete, wo, o);
     float cosWi = dot(wi, normal);
@@ -405,7 +405,7 @@ DEV int env_u_to_index(const float *cdf, int size, float &u) {
     return index;
 }
 // SampleDirection (src/envlight.cpp:120-169). lPrim: the sampled pixel.
-DEV void env_sample_direction(const SceneView &s, float u0, float u1, V3 &dirToLight, V3 &value, float &pdf,
+DEV_SHARED void env_sample_direction(const SceneView &s, float u0, float u1, V3 &dirToLight, V3 &value, float &pdf,
                               int &lPrim) {
     const int row = env_u_to_index(s.envCdfRows, s.envH, u1);
     const int col = env_u_to_index(s.envCdfCols + row * (s.envW + 1), s.envW, u0);
@@ -429,7 +429,7 @@ DEV void env_sample_direction(const SceneView &s, float u0, float u1, V3 &dirToL
 DEV float env_position_pdf(const SceneView &s) { return kInvPi / sq(s.bsRadius); }
 
 // EnvLight::Emission (src/envlight.cpp:193-222).
-DEV void env_emission(const SceneView &s, const Light &L, const V3 &dirToLight, V3 &emission, float &directPdf,
+DEV_SHARED void env_emission(const SceneView &s, const Light &L, const V3 &dirToLight, V3 &emission, float &directPdf,
                       float &emissionPdf) {
     const V3 d = xform3(s.envToLight, dirToLight);
     const float uvx = atan2f(d.x, -d.z) * kInvTwoPi * float(s.envW) - 0.5f;
@@ -447,7 +447,7 @@ DEV void env_emission(const SceneView &s, const Light &L, const V3 &dirToLight, 
 }
 
 // AreaLight::SampleDirect (src/arealight.cpp:29-57).
-DEV bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &pos, float r0, float r1,
+DEV_SHARED bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &pos, float r0, float r1,
                              V3 &dirToLight, float &dist, V3 &contrib, float &cosAtLight,
                              float &directPdf, float &emissionPdf) {
     const Light &L = s.lights[li];
@@ -492,7 +492,7 @@ DEV bool light_sample_direct(const SceneView &s, int li, int lPrim, const V3 &po
 }
 
 // AreaLight::Emission (src/arealight.cpp:59-76).
-DEV void light_emission(const SceneView &s, int li, const V3 &dirToLight, const V3 &normalOnLight, V3 &emission,
+DEV_SHARED void light_emission(const SceneView &s, int li, const V3 &dirToLight, const V3 &normalOnLight, V3 &emission,
                         float &directPdf, float &emissionPdf) {
     const Light &L = s.lights[li];
     if (L.type == kLightEnv) {
@@ -512,7 +512,7 @@ DEV void light_emission(const SceneView &s, int li, const V3 &dirToLight, const 
 }
 
 // AreaLight::Emit (src/arealight.cpp:78-102).
-DEV void light_emit(const SceneView &s, int li, int lPrim, float p0, float p1, float d0, float d1, V3 &org,
+DEV_SHARED void light_emit(const SceneView &s, int li, int lPrim, float p0, float p1, float d0, float d1, V3 &org,
                     V3 &dir, V3 &emission, float &cosAtLight, float &emissionPdf, float &directPdf) {
     const Light &L = s.lights[li];
     if (L.type == kLightPoint) {  // PointLight::Emit (src/pointlight.cpp:58-72)

@@ -8,6 +8,9 @@
 #include <cuda_runtime.h>
 
 #define DEV __device__ __forceinline__
+// Called from many sites of the large per-chain kernels: kept out of line so
+// that one copy of the code serves every call site (instruction-cache footprint).
+#define DEV_SHARED static __device__ __noinline__
 #define HD __host__ __device__ __forceinline__
 
 namespace drmlt {

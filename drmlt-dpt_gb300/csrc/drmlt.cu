@@ -738,22 +738,26 @@ struct Renderer {
         return DRMLT_OK;
     }
 
-    // Launch-shape autotuner: times `per` real iterations under each candidate
-    // number of chains per warp in the per-chain stage kernels, keeps the
-    // fastest, then does the same for the number of warps sharing one chain's
-    // derivatives. The timed iterations are part of the render: the launch shape
-    // never changes which steps the chains take. Stops early when the render
-    // has fewer than `per` iterations left.
+    // Launch-shape autotuner: after `per` untimed iterations (past the first
+    // iterations' transient), times `per` real iterations under each candidate
+    // number of chains per warp in the per-chain stage kernels, in two passes
+    // of opposite order so that a drift of the iteration cost over the render
+    // cancels, keeps the fastest, then does the same for the number of warps
+    // sharing one chain's derivatives. The iterations are part of the render:
+    // the launch shape never changes which steps the chains take. Stops early
+    // when the render runs out of iterations.
     int autotune(int per, int *lanesOut, int *warpsOut) {
         if (!prepassDone) return fail(DRMLT_E_STATE, "autotune before prepass");
         if (per < 1) return fail(DRMLT_E_ARG, "autotune needs at least one iteration per candidate");
         static const int kLanes[] = {2, 4, 8, 16, 32};
         static const int kWarps[] = {1, 2, 4};
         int bestL = params().lanes, bestW = params().derivWarps;
-        float bestMs = INFINITY;
+        bool out = false;  // ran out of iterations
         auto trial = [&](int lanes, int warps, float &ms) -> int {
-            ms = -1.0f;
-            if (total_iterations() - iterDone < per) return DRMLT_OK;
+            if (total_iterations() - iterDone < per) {
+                out = true;
+                return DRMLT_OK;
+            }
             opt.stage_lanes = lanes;
             opt.deriv_warps = warps;
             if (graph) {
@@ -761,26 +765,36 @@ struct Renderer {
                 graph = nullptr;
             }
             if (int rc = run(per, nullptr)) return rc;
-            ms = lastRunMs / float(per);
+            ms += lastRunMs;
             return DRMLT_OK;
         };
-        float ms;
-        for (int L : kLanes) {
-            if (int rc = trial(L, bestW, ms)) return rc;
-            if (ms < 0.0f) break;
-            if (ms < bestMs) {
-                bestMs = ms;
-                bestL = L;
+        float warm = 0.0f;
+        if (int rc = trial(bestL, bestW, warm)) return rc;
+        // chains per warp
+        float tl[5] = {0, 0, 0, 0, 0};
+        for (int pass = 0; pass < 2 && !out; pass++)
+            for (int k = 0; k < 5 && !out; k++) {
+                const int i = pass == 0 ? k : 4 - k;
+                if (int rc = trial(kLanes[i], bestW, tl[i])) return rc;
             }
+        if (!out) {
+            int bi = 0;
+            for (int i = 1; i < 5; i++)
+                if (tl[i] < tl[bi]) bi = i;
+            bestL = kLanes[bi];
         }
-        for (int w : kWarps) {
-            if (w == bestW) continue;
-            if (int rc = trial(bestL, w, ms)) return rc;
-            if (ms < 0.0f) break;
-            if (ms < bestMs) {
-                bestMs = ms;
-                bestW = w;
+        // derivative warps
+        float tw[3] = {0, 0, 0};
+        for (int pass = 0; pass < 2 && !out; pass++)
+            for (int k = 0; k < 3 && !out; k++) {
+                const int i = pass == 0 ? k : 2 - k;
+                if (int rc = trial(bestL, kWarps[i], tw[i])) return rc;
             }
+        if (!out) {
+            int bi = 0;
+            for (int i = 1; i < 3; i++)
+                if (tw[i] < tw[bi]) bi = i;
+            bestW = kWarps[bi];
         }
         opt.stage_lanes = bestL;
         opt.deriv_warps = bestW;
@@ -891,8 +905,8 @@ int drmlt_render(void *handle) {
     if (rc) return rc;
     rc = r->prepass(nullptr);
     if (rc) return rc;
-    // autotune on renders long enough that its 7 candidate runs are a small part
-    if (r->opt.autotune && r->total_iterations() >= 64 * 8) {
+    // autotune on renders long enough that its 17 runs of 8 iterations are a small part
+    if (r->opt.autotune && r->total_iterations() >= 1024) {
         rc = r->autotune(8, nullptr, nullptr);
         if (rc) return rc;
     }

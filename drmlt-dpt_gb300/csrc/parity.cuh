@@ -348,3 +348,46 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
 }
 
 }  // extern "C"
+
+// ============================================================================ ray-casting benchmark
+#include "raybench.cuh"
+
+extern "C" {
+
+int drmlt_ray_benchmark(void *handle, int kind, int n_rays, int repeats, float *ms_per_pass, double *counts) {
+    if (!handle || !ms_per_pass || !counts) return fail(DRMLT_E_ARG, "null argument");
+    if (kind < 0 || kind > 2 || n_rays <= 0 || repeats <= 0) return fail(DRMLT_E_ARG, "bad ray benchmark shape");
+    Renderer *r = static_cast<Renderer *>(handle);
+    const int n = n_rays;
+    int rc;
+    DevBuf<float4> org, dir;
+    DevBuf<int> hit;
+    DevBuf<unsigned long long> cnt;
+    if ((rc = org.alloc(n)) || (rc = dir.alloc(n)) || (rc = hit.alloc(n)) || (rc = cnt.alloc(3))) return rc;
+    const int nb = (n + 127) / 128;
+    k_rays_setup<<<nb, 128>>>(r->sv, kind, n, r->opt.seed ^ 0xBE7Cull, org.p, dir.p);
+    CK(cudaMemset(cnt.p, 0, 3 * sizeof(unsigned long long)));
+    const int anyHit = kind == 2;
+    k_rays_trace<true><<<nb, 128>>>(r->sv, anyHit, n, org.p, dir.p, hit.p, cnt.p);
+    k_rays_trace<false><<<nb, 128>>>(r->sv, anyHit, n, org.p, dir.p, hit.p, cnt.p);
+    CK(cudaGetLastError());
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0));
+    for (int k = 0; k < repeats; k++) k_rays_trace<false><<<nb, 128>>>(r->sv, anyHit, n, org.p, dir.p, hit.p, cnt.p);
+    CK(cudaEventRecord(e1));
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    unsigned long long h[3];
+    if ((rc = cnt.get(h, 3))) return rc;
+    *ms_per_pass = ms / float(repeats);
+    for (int k = 0; k < 3; k++) counts[k] = double(h[k]);
+    return DRMLT_OK;
+}
+
+}  // extern "C"

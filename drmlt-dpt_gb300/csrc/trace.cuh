@@ -44,9 +44,11 @@ DEV bool slab(const V3 &o, const V3 &inv, float lx, float ly, float lz, float hx
 }
 
 // Traverses the BVH. anyHit: stop at the first hit in (tmin, tmax).
-// Returns the global triangle index of the closest hit or -1.
-template <bool anyHit>
-DEV int traverse(const SceneView &s, const V3 &o, const V3 &d, float tmin, float tmax) {
+// Returns the global triangle index of the closest hit or -1. kCount: adds the
+// nodes fetched and triangles tested to *nodes / *tests (the ray benchmark).
+template <bool anyHit, bool kCount = false>
+DEV_SHARED int traverse(const SceneView &s, const V3 &o, const V3 &d, float tmin, float tmax, unsigned *nodes = nullptr,
+                 unsigned *tests = nullptr) {
     const float tiny = 1e-20f;
     const V3 inv(1.0f / (fabsf(d.x) > tiny ? d.x : copysignf(tiny, d.x)),
                  1.0f / (fabsf(d.y) > tiny ? d.y : copysignf(tiny, d.y)),
@@ -58,6 +60,7 @@ DEV int traverse(const SceneView &s, const V3 &o, const V3 &d, float tmin, float
     float tbest = tmax;
     for (int iter = 0; iter < (1 << 20); iter++) {
         const BvhNode n = s.nodes[node];
+        if (kCount) ++*nodes;
         int next[2];
         int nn = 0;
         float te0, te1;
@@ -71,6 +74,7 @@ DEV int traverse(const SceneView &s, const V3 &o, const V3 &d, float tmin, float
             if (count[c] > 0) {
                 for (int k = 0; k < count[c]; k++) {
                     const Tri tri = s.tris[child[c] + k];
+                    if (kCount) ++*tests;
                     const float t = hit_triangle(o, d, tri.p0, tri.e1, tri.e2);
                     if (t > tmin && t <= tbest && t < INFINITY) {
                         best = __float_as_int(tri.p0.w);

@@ -119,6 +119,16 @@ class Renderer:
                                              C.byref(warps)))
         return lanes.value, warps.value
 
+    RAY_KINDS = ("primary", "bounce", "shadow")
+
+    def ray_benchmark(self, kind: str, n_rays: int = 1 << 20, repeats: int = 10) -> dict:
+        """drmlt_ray_benchmark: ms per pass, rays traced, nodes fetched, triangles tested."""
+        ms = C.c_float()
+        counts = np.zeros(3, np.float64)
+        capi.check(capi.lib().drmlt_ray_benchmark(self.handle, self.RAY_KINDS.index(kind), int(n_rays), int(repeats),
+                                                  C.byref(ms), counts.ctypes.data))
+        return {"ms": ms.value, "rays": counts[0], "nodes": counts[1], "tris": counts[2]}
+
     STAGES = ("stage1", "derivs_x", "gauss_x", "stage2", "derivs_z", "gauss_z", "finish")
 
     def profile(self, iterations: int):

@@ -226,7 +226,7 @@ def config4(seed: int = 4, spp: int = 16, dr_type: str = "mira", width: int = 10
                      bsdfs, [Le, Lp], cam, _options(12, chains, spp, dr_type), [env])
 
 
-def config5(seed: int = 5, spp: int = 4, dr_type: str = "mira", width: int = 2048, height: int = 2048,
+def config5(seed: int = 5, spp: int = 16, dr_type: str = "mira", width: int = 2048, height: int = 2048,
             chains: int = 262144, grid: int = 2000, acceptance_map: bool = False) -> SceneData:
     def fbm(X, Z):
         h = np.zeros_like(X)

@@ -124,7 +124,7 @@ typedef struct drmlt_options {
     int32_t smem_carveout;        /* shared-memory carveout (percent) for every chain-loop kernel,
                                      -1 = the driver's choice per kernel */
     int32_t autotune;             /* drmlt_render picks stage_lanes / deriv_warps with drmlt_autotune
-                                     (default 1; renders of fewer than 512 iterations are not tuned) */
+                                     (default 1; renders of fewer than 1024 iterations are not tuned) */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
@@ -197,12 +197,14 @@ int drmlt_last_run_ms(void *handle, float *ms);
 /* Kernels launched by drmlt_run on this handle so far (all chain groups). */
 int drmlt_kernel_launches(void *handle, int64_t *n);
 
-/* Launch-shape autotuner (after drmlt_prepass): runs `iterations_per_candidate`
- * iterations of the render under each candidate chains-per-warp count of the
- * per-chain stage kernels (2, 4, 8, 16, 32) and then each derivative team size
- * (1, 2, 4 warps), timed with CUDA events, and keeps the fastest pair (written
- * to the outputs, which may be NULL). The iterations count toward the render;
- * the launch shape does not change the chains' steps. */
+/* Launch-shape autotuner (after drmlt_prepass): after one untimed run of
+ * `iterations_per_candidate` iterations, times that many iterations of the
+ * render under each candidate chains-per-warp count of the per-chain stage
+ * kernels (2, 4, 8, 16, 32), in two passes of opposite order, then each
+ * derivative team size (1, 2, 4 warps) the same way (CUDA events), and keeps
+ * the fastest pair (written to the outputs, which may be NULL): 17 runs in all.
+ * The iterations count toward the render; the launch shape does not change the
+ * chains' steps. */
 int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes, int *deriv_warps);
 
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
@@ -248,6 +250,15 @@ int drmlt_replay(void *handle, int mode, const float *tapes, const int32_t *tape
  * org/dir: n x 3 floats. Writes the global triangle index (-1 = miss) and hit t. */
 int drmlt_trace_rays(void *handle, const float *org, const float *dir, float tmin, float tmax, int n, int any_hit,
                      int32_t *tri, float *t);
+
+/* Ray-casting benchmark on the scene BVH (no reference counterpart): n_rays
+ * device-generated rays of one kind -- 0 primary camera rays (closest hit),
+ * 1 diffuse bounce rays from their first hits (closest hit), 2 shadow rays of
+ * length 2 from the same hits (any hit) -- traced `repeats` times by a kernel
+ * timed on its own with CUDA events. Writes the mean milliseconds per pass and
+ * counts[3] = rays traced, BVH nodes fetched (64 B each) and triangles tested
+ * (48 B each) in one pass. */
+int drmlt_ray_benchmark(void *handle, int kind, int n_rays, int repeats, float *ms_per_pass, double *counts);
 
 /* ComputeGaussian (drsmallstep.cpp:219-266) in FP64: returns mean (MAX_DIM),
  * invCov and cov (MAX_DIM^2 each, row-major) and logDet per input. */

@@ -236,3 +236,19 @@ def test_compute_gaussian_vs_reference(renderers, cfg):
         worst.append(max(e_ic, e_cv, e_m, e_ld))
     worst = np.array(worst)
     assert np.mean(worst < 1e-3) >= 0.98, "Gaussian mismatch: max %g" % worst.max()
+
+
+@pytest.mark.parametrize("kind", ["primary", "bounce", "shadow"])
+def test_ray_benchmark_counts(renderers, kind):
+    """drmlt_ray_benchmark traces every generated ray and fetches at least the
+    root node per ray; primary rays of the open-front box all start at the
+    camera, bounce and shadow rays only from first hits."""
+    r = renderers("cfg1")
+    n = 1 << 16
+    b = r.ray_benchmark(kind, n, repeats=2)
+    assert b["ms"] > 0.0
+    if kind == "primary":
+        assert b["rays"] == n
+    else:
+        assert 0.5 * n <= b["rays"] <= n
+    assert b["nodes"] >= b["rays"] and b["tris"] > 0

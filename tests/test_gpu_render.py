@@ -149,10 +149,10 @@ def test_autotuner_keeps_the_chains(built_lib, scene_root):
         lanes, warps = a.autotune(2)
         assert lanes in (2, 4, 8, 16, 32) and warps in (1, 2, 4)
         tuned = a.stats()["mutations"] // 4096
-        assert tuned == 2 * 7
-        a.run(30 - tuned)
+        assert tuned == 2 * 17
+        a.run(40 - tuned)
         b.prepass()
-        b.run(30)
+        b.run(40)
         assert a.stats() == b.stats()
         np.testing.assert_allclose(a.film(), b.film(), rtol=1e-4, atol=1e-6)
 
