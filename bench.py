@@ -131,6 +131,15 @@ def load_workload(name: str, tmp: str):
     return getattr(procedural, fn)(spp=64 if name == "config4" else 32), None, label
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each chain-loop
+# kernel per iteration (both chain groups), from `ncu --set full` captures of
+# the same kernels on these workloads; None where not captured.
+NCU_TRAFFIC = {
+    "config2": {"stage1": 2 * 3.44e6, "derivs_x": 2 * 0.63e6, "gauss_x": 2 * 0.85e6, "stage2": 2 * 1.65e6,
+                "derivs_z": 2 * 0.67e6, "gauss_z": 2 * 2.30e6, "finish": 2 * 5.33e6},
+    "config4": {"stage1": 2 * 145.7e6},
+}
+
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
 # HBM). A Slot is 328 B, the per-chain scratch 128 B (both asserted in
 # csrc/chain.cuh), a stored FP64 Gaussian 5008 B.
@@ -223,7 +232,7 @@ def run_ours(args, world, rank, local):
         stage_bytes[dom] = listed * (4 * (24 + 576) + GAUSS_B)
     achieved = stage_bytes[dom] / (per_launch_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+            "frac": achieved / hbm, "traffic": NCU_TRAFFIC.get(args.workload, {}).get(dom), "peak_kind": peak_kind,
             "stage_ms_per_iteration": {k: v / iters for k, v in prof.items()}}
 
     out = None

@@ -259,3 +259,32 @@ def config5(seed: int = 5, spp: int = 16, dr_type: str = "mira", width: int = 20
     opts.acceptanceMap = acceptance_map
     return _assemble([(GV, GF, None, 0, -1), (SV, SF, SN, 1, -1), (LV, LF, flat(LV, [0.0, -1.0, 0.0]), 2, 0)],
                      bsdfs, [La], cam, opts)
+
+
+def main(argv=None):
+    """Renders a few chain-loop iterations of a procedural scene (and optionally
+    one ray-benchmark pass) -- a small driver for profiling runs:
+    python -m drmlt.procedural config4 --iterations 4 --lanes 4 --warps 4 --rays bounce"""
+    import argparse
+    from .integrator import Renderer
+    ap = argparse.ArgumentParser()
+    ap.add_argument("scene", choices=["config4", "config5"])
+    ap.add_argument("--iterations", type=int, default=4)
+    ap.add_argument("--lanes", type=int, default=0, help="chains per warp (0: library default)")
+    ap.add_argument("--warps", type=int, default=0, help="derivative warps per chain (0: library default)")
+    ap.add_argument("--graph", type=int, default=0, help="replay iterations as CUDA graphs")
+    ap.add_argument("--rays", default="", choices=["", "primary", "bounce", "shadow"])
+    a = ap.parse_args(argv)
+    sd = globals()[a.scene]()
+    r = Renderer(sd, seed=77, use_graph=a.graph, stage_lanes=a.lanes, deriv_warps=a.warps)
+    r.prepass()
+    r.run(a.iterations)
+    out = {"mutations": r.stats()["mutations"]}
+    if a.rays:
+        out["rays"] = r.ray_benchmark(a.rays, 1 << 21, 1)
+    r.close()
+    print(out)
+
+
+if __name__ == "__main__":
+    main()
