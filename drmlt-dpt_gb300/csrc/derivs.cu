@@ -38,17 +38,25 @@ __device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, 
     }
 }
 
-// A team of p.derivWarps warps per listed chain shares its Hessian entries.
+// A team of p.derivWarps warps per listed chain shares its Hessian entries. The
+// grid is sized for the GPU: team t takes list entries t, t + teams, ...
 __global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int w = gw / p.derivWarps;
+    const int teams = (gridDim.x * blockDim.x >> 5) / p.derivWarps;
     const int n = p.d.counters[which == 0 ? 0 : 1];
-    if (w >= n) return;
-    const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
-    const Slot &st = slot_of(p.d, chain, which);
-    derivs_for_path(p.s, st.rec, st.ss, p.maxDerv, p.d.grad + size_t(w) * kMaxDim,
-                    p.d.hess + size_t(w) * kMaxDim * kMaxDim, (gw % p.derivWarps) * 32 + (threadIdx.x & 31),
-                    32 * p.derivWarps);
+    for (int w = gw / p.derivWarps; w < n; w += teams) {
+        const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
+        const Slot &st = slot_of(p.d, chain, which);
+        derivs_for_path(p.s, st.rec, st.ss, p.maxDerv, p.d.grad + size_t(w) * kMaxDim,
+                        p.d.hess + size_t(w) * kMaxDim * kMaxDim, (gw % p.derivWarps) * 32 + (threadIdx.x & 31),
+                        32 * p.derivWarps);
+    }
+}
+
+int derivs_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_derivs, 128, 0) != cudaSuccess) n = 1;
+    return n > 0 ? n : 1;
 }
 
 __global__ void __launch_bounds__(128) k_gradhess_paths(SceneView s, const PathRec *paths, const float *u, int n,

@@ -16,5 +16,7 @@ void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s);
 void launch_gradhess_paths(const SceneView &s, const PathRec *paths, const float *u, int n, float *grad,
                            float *hess, cudaStream_t st);
 cudaError_t set_derivs_carveout(int percent);
+// Resident blocks of the derivative kernel per SM (its grid-stride grid).
+int derivs_blocks_per_sm();
 
 }  // namespace drmlt

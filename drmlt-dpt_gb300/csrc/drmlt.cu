@@ -122,6 +122,7 @@ struct Renderer {
     int *dIters = nullptr;  // per chain group: its current iteration
     // chain groups, each stepped on its own stream
     int G = 1, chunk = 0;
+    int gaussGrid = 1, derivsGrid = 1;  // blocks of the list-driven kernels (grid-stride over their lists)
     std::vector<cudaStream_t> gstreams;
     std::vector<cudaEvent_t> gevents;
     unsigned long long bootSeed = 0;
@@ -206,6 +207,17 @@ struct Renderer {
             return fail(DRMLT_E_CUDA, "no CUDA device available");
         CK(cudaSetDevice(opt.device));
         if (int rc = gauss_kernels_setup()) return rc;
+        {
+            // grids of the list-driven kernels: four times as many blocks as the GPU
+            // holds at once (lists that long are rare; shorter lists keep one entry
+            // per block, scheduled dynamically, without thousands of idle blocks)
+            int sms = 0, perSm = 0;
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opt.device));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_gauss, 32 * kGaussTeamWarps,
+                                                             gauss_smem_bytes(std::min(2 * opt.max_depth, kMaxDim))));
+            gaussGrid = std::max(1, 4 * sms * std::max(perSm, 1));
+            derivsGrid = std::max(1, 4 * sms * derivs_blocks_per_sm());
+        }
         if (opt.smem_carveout >= 0) {
             // one shared-memory carveout for every chain-loop kernel, so that
             // kernels of different stages can share an SM
@@ -600,8 +612,8 @@ struct Renderer {
         const RunParams p = params(g);
         const int nb = (p.N + kStageBlock - 1) / kStageBlock;
         const int nbS = sparse_blocks(p.N, p.lanes);
-        const int nbWarp = (p.N * 32 * p.derivWarps + 127) / 128;
-        const int nbG = p.N;  // one block per listed chain; blocks past the list exit
+        const int nbWarp = std::min((p.N * 32 * p.derivWarps + 127) / 128, derivsGrid);
+        const int nbG = std::min(p.N, gaussGrid);
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
         switch (k) {
             case 0:

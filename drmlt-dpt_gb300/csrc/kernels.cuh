@@ -183,11 +183,7 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
 constexpr int kGaussTeamWarps = 4;
 inline size_t gauss_smem_bytes(int maxDim) { return size_t(gauss_smem_doubles(maxDim)) * sizeof(double); }
 
-__global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int which) {
-    extern __shared__ double gsm[];
-    const int w = blockIdx.x;
-    const int n = p.d.counters[which == 0 ? 0 : 1];
-    if (w >= n) return;
+DEV void gauss_for_entry(const RunParams &p, int which, int w, double *gsm) {
     const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
     Slot &st = slot_of(p.d, chain, which);
     const int dim = path_dim(st.rec.c, st.rec.l);
@@ -210,6 +206,18 @@ __global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int
         st.gaussInit = 1;
         if (kind != kGaussIsotropic) atomicAdd(&p.d.stats[kStatGauss], 1ull);
         if (kind == kGaussFp64Jacobi) atomicAdd(&p.d.stats[kStatGaussFallback], 1ull);
+    }
+}
+
+// The grid is sized for the GPU, not the list: each block takes list entries
+// blockIdx.x, blockIdx.x + gridDim.x, ... (the list's length is known only on
+// the device).
+__global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int which) {
+    extern __shared__ double gsm[];
+    const int n = p.d.counters[which == 0 ? 0 : 1];
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+        gauss_for_entry(p, which, w, gsm);
+        __syncthreads();  // the block's shared scratch is reused by its next entry
     }
 }
 
