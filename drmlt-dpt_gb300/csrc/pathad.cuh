@@ -89,7 +89,7 @@ HD HyperDual atan2(const HyperDual &y, const HyperDual &x) {
                      fy * y.ab + fx * x.ab + fyy * y.a * y.b + fxx * x.a * x.b + fxy * (y.a * x.b + x.a * y.b));
 }
 HD HyperDual acos(const HyperDual &x) {
-    const float q = 1.0f - x.v * x.v;
+    const float q = (1.0f - x.v) * (1.0f + x.v);  // 1 - x^2 without cancellation near |x| = 1
     const float iq = 1.0f / sqrtf(q);
     return chain(x, acosf(x.v), -iq, -x.v * iq / q);
 }
@@ -526,8 +526,10 @@ DEV void ad_env_emission(const SceneView &s, const Light &L, const TV3<T> &dirTo
     const TV3<T> value2 =
         tv<T>(env_rep_at(s, col, row + 1)) * (dx2 * dy1) + tv<T>(env_rep_at(s, col + 1, row + 1)) * (dx1 * dy1);
     emission = (value1 + value2) * L.samplingWeight;
-    // EmissionEnvLight's clamp against infinite derivatives at the poles (src/envlight.cpp:353)
-    const T sinTheta = sqrt(fmax(1.0f - d.y * d.y, 1e-6f));
+    // EmissionEnvLight's clamp against infinite derivatives at the poles
+    // (src/envlight.cpp:353); 1 - y^2 as (1 - y)(1 + y), which keeps its digits
+    // (and its second derivative) in single precision as |y| approaches 1
+    const T sinTheta = sqrt(fmax((1.0f - d.y) * (1.0f + d.y), 1e-6f));
     directPdf = (tlum(value1) * env_row_weight(s, row) + tlum(value2) * env_row_weight(s, row + 1)) * s.envNorm /
                 fmax(fabs(sinTheta), 1e-7f);
     emissionPdf = directPdf * env_position_pdf(s);

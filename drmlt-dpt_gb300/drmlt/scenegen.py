@@ -276,3 +276,58 @@ def config_env(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
                          options=SceneOptions(maxdepth=5, numchains=4096, spp=spp, type=dr_type),
                          sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5),
                          env=dict(image=env_image(), angle=30.0), ceiling=False)
+
+
+def _write_mesh_obj(path, V, F, N):
+    lines = ["v %.9g %.9g %.9g" % tuple(v) for v in V]
+    lines += ["vn %.9g %.9g %.9g" % tuple(n) for n in N]
+    lines += ["f %d//%d %d//%d %d//%d" % (a + 1, a + 1, b + 1, b + 1, c + 1, c + 1) for a, b, c in F]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def config4_small(outdir: str, spp: int = 4, dr_type: str = "mira") -> str:
+    """Config 4 in miniature, written as scene XML + OBJ: the displaced geodesic
+    sphere at frequency 6 (720 triangles, rough dielectric, alpha from the seed)
+    over a 12 x 12 Phong ground grid (288 triangles), the 2 x 1 constant
+    environment map and the point light of intensity 50; 256 x 256, max depth
+    12 (paths of up to 24 primary dimensions), 4096 chains."""
+    from . import procedural as P
+    os.makedirs(outdir, exist_ok=True)
+    seed = 4
+    rng = np.random.default_rng(seed)
+    V, F = P.geodesic_sphere(6)
+    V = V * (1.0 + 0.05 * P.gradient_noise(3.0 * V, seed))[:, None]
+    _write_mesh_obj(os.path.join(outdir, "sphere.obj"), V, F, P._vertex_normals(V, F))
+    GV, GF = P._grid(12, 6.0, -1.08)
+    _write_mesh_obj(os.path.join(outdir, "ground.obj"), GV, GF, np.tile([0.0, 1.0, 0.0], (len(GV), 1)))
+    alpha = float(rng.uniform(0.05, 0.5))
+    kd = rng.uniform(0.2, 0.8, 3)
+    expo = float(np.exp(rng.uniform(np.log(10.0), np.log(1000.0))))
+    ks = float(rng.uniform(0.1, 0.5))
+    write_pfm(os.path.join(outdir, "env.pfm"), np.ones((1, 2, 3), np.float32))
+    options = SceneOptions(maxdepth=12, numchains=4096, spp=spp, type=dr_type)
+    shapes = [
+        '  <shape type="obj"><string name="filename" value="sphere.obj"/>'
+        '<bsdf type="roughdielectric"><float name="alpha" value="%.9g"/>'
+        '<float name="intIOR" value="1.5"/><float name="extIOR" value="1"/></bsdf></shape>' % alpha,
+        '  <shape type="obj"><string name="filename" value="ground.obj"/>'
+        '<bsdf type="phong"><rgb name="diffuseReflectance" value="%.9g %.9g %.9g"/>'
+        '<rgb name="specularReflectance" value="%.9g %.9g %.9g"/><float name="exponent" value="%.9g"/></bsdf>'
+        '</shape>' % (*kd, ks, ks, ks, expo),
+        '  <emitter type="envmap"><string name="filename" value="env.pfm"/></emitter>',
+        '  <emitter type="point"><point name="position" x="2" y="4" z="3"/>'
+        '<rgb name="intensity" value="50 50 50"/></emitter>',
+    ]
+    sensor = ('  <sensor type="perspective">\n'
+              '    <float name="fov" value="40"/>\n'
+              '    <transform name="toWorld"><lookat origin="0, 1.2, 5.5" target="0, -0.2, 0" up="0, 1, 0"/></transform>\n'
+              '    <film type="hdrfilm"><integer name="width" value="256"/><integer name="height" value="256"/>'
+              '<string name="filename" value="image.exr"/></film>\n'
+              '  </sensor>\n')
+    xml = ('<?xml version="1.0" encoding="utf-8"?>\n<scene version="0.5.0">\n'
+           + options.xml() + sensor + "\n".join(shapes) + "\n</scene>\n")
+    path = os.path.join(outdir, "scene.xml")
+    with open(path, "w") as f:
+        f.write(xml)
+    return path

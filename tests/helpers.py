@@ -24,6 +24,7 @@ SCENE_WRITERS = {
     "cfg3": lambda d: scenegen.config3(d),
     "cfgL": lambda d: scenegen.config_lights(d),
     "cfgE": lambda d: scenegen.config_env(d),
+    "cfg4s": lambda d: scenegen.config4_small(d),
 }
 
 

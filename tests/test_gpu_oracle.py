@@ -21,8 +21,11 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 pytestmark = pytest.mark.gpu
 
-CFGS = ["cfg1", "cfg2", "cfg3", "cfgL", "cfgE"]
-MAX_DEPTH = {"cfg1": 5, "cfg2": 8, "cfg3": 5, "cfgL": 5, "cfgE": 5}
+# cfg4s: config 4 in miniature (displaced rough-dielectric sphere, Phong ground,
+# constant environment map, point light) at max depth 12 -- paths of up to 24
+# primary dimensions; no reference fixtures (the oracle only)
+CFGS = ["cfg1", "cfg2", "cfg3", "cfgL", "cfgE", "cfg4s"]
+MAX_DEPTH = {"cfg1": 5, "cfg2": 8, "cfg3": 5, "cfgL": 5, "cfgE": 5, "cfg4s": 12}
 
 
 @pytest.fixture(scope="module")
@@ -47,7 +50,7 @@ def _random_large_steps(cfg, n, seed):
     L = rng.integers(3, MAX_DEPTH[cfg] + 1, n)
     cam = np.array([rng.integers(1, l + 2) for l in L], np.int32)
     lgt = (L + 1 - cam).astype(np.int32)
-    tapes = rng.random((n, 64), dtype=np.float32)
+    tapes = rng.random((n, 64 if MAX_DEPTH[cfg] <= 8 else 128), dtype=np.float32)
     tapes = np.minimum(tapes, np.float32(1.0 - 2 ** -24))
     return tapes, cam, lgt
 
@@ -55,8 +58,15 @@ def _random_large_steps(cfg, n, seed):
 _CACHE = {}
 
 
-def _valid_paths(cfg, renderers, oracles, n=4096):
+# random large steps per scene; in the open miniature config 4 under the
+# environment map only ~0.7% of random techniques contribute
+N_STEPS = {"cfg4s": 1 << 16}
+MIN_VALID = {"cfg4s": 1.0 / 400}
+
+
+def _valid_paths(cfg, renderers, oracles):
     """Random large-step paths traced by both sides; returns the ones both found valid and equal."""
+    n = N_STEPS.get(cfg, 4096)
     if cfg in _CACHE:
         return _CACHE[cfg]
     tapes, cam, lgt = _random_large_steps(cfg, n, 17)
@@ -76,7 +86,7 @@ def test_random_large_steps_vs_oracle(renderers, oracles, cfg):
     co, cto, po, so = o
     n = len(tapes)
     bad = int(np.sum((cg != co) | (sg != so)))
-    assert len(keep) > n // 20
+    assert len(keep) > n * MIN_VALID.get(cfg, 1.0 / 20)
     for i in keep:
         d = 2 * (pg[i]["c"] + pg[i]["l"] - 1)
         nv = pg[i]["c"] + pg[i]["l"] - 2
@@ -143,7 +153,11 @@ def test_random_derivatives_vs_fp64_oracle(renderers, oracles, cfg):
             bad_h.append(i)
     n = len(paths)
     assert n > 100
-    tol = max(2, n // 100)
+    # In the miniature config 4 a few deep paths graze the tessellated sphere
+    # from inside, where the single-precision path function itself is not smooth
+    # at the 1e-3 level (central differences of the FP32 gradient change sign
+    # with the step while the FP64 oracle's do not): up to 2% of paths there.
+    tol = max(2, n // (50 if cfg == "cfg4s" else 100))
     assert len(bad_f) <= tol, "log f: %d / %d" % (len(bad_f), n)
     assert len(bad_g) <= tol, "gradient: %d / %d" % (len(bad_g), n)
     assert len(bad_h) <= tol, "Hessian: %d / %d" % (len(bad_h), n)
