@@ -290,8 +290,10 @@ DEV double eigen_residuals(GaussSmem &sm, int n, bool skipR, const Team &tm) {
 //   X' = X + X E,  delta = 2 (|offdiag(X^T A X)|_F + |A|_F |R|_F).
 // T, E and X E are ~1e-7 and are formed in FP32 from a float copy of X; only
 // the residual sums and X + X E are FP64. A step is accepted when the FP64
-// residual of (X', lam~) is below 1e-11 |A|_F; at most two steps, then the
-// caller falls back to the FP64 polish. Leaves X and lam in sm.
+// residual of (X', lam~) is below 1e-11 |A|_F; at most three steps (a third
+// step certifies three quarters of the Gaussians the second leaves, at a fifth
+// of the polish's cost), then the caller falls back to the FP64 polish.
+// Leaves X and lam in sm.
 DEV bool refine_eigen_team(GaussSmem &sm, int n, double froA, const Team &tm) {
     const LaneGrid g(n, tm);
     const int ld = sm.ld;
@@ -302,7 +304,7 @@ DEV bool refine_eigen_team(GaussSmem &sm, int n, double froA, const Team &tm) {
     tm.sync();
     eigen_residuals(sm, n, false, tm);
     double *lamNew = sm.cs64;
-    for (int step = 0; step < 2; step++) {
+    for (int step = 0; step < 3; step++) {
         const float *X32 = sm.V32;
         const float *Z = sm.A32;
         // T = X^T Z
@@ -359,7 +361,7 @@ DEV bool refine_eigen_team(GaussSmem &sm, int n, double froA, const Team &tm) {
         // certificate: FP64 residual of the refined pairs (also the next step's Z)
         const double res = eigen_residuals(sm, n, true, tm);
         if (res <= tol2) return true;  // false for NaN
-        if (step == 1) break;
+        if (step == 2) break;
         if (g.j < n)
             for (int i = g.h; i < n; i += g.G) sm.V32[i * ld + g.j] = float(sm.X[i * ld + g.j]);
         // R for the refined X (FP64; Z is already in place)
