@@ -224,8 +224,8 @@ int drmlt_total_iterations(void *handle, int64_t *iterations);
 int drmlt_path_eval(void *handle, const drmlt_path *paths, const float *u, int n, float *logf);
 
 /* Backward pair of drmlt_path_eval: gradient (DRMLT_MAX_DIM stride) and Hessian
- * (DRMLT_MAX_DIM^2 stride, row-major) of log f, the PathFuncDerv call of
- * drsmallstep.cpp:128-158. */
+ * (DRMLT_MAX_DIM^2 stride per path; within it the dim x dim matrix row-major,
+ * dim = 2(c+l-1)) of log f, the PathFuncDerv call of drsmallstep.cpp:128-158. */
 int drmlt_path_grad_hess(void *handle, const drmlt_path *paths, const float *u, int n, float *grad,
                          float *hess);
 

@@ -252,3 +252,45 @@ def test_ray_benchmark_counts(renderers, kind):
     else:
         assert 0.5 * n <= b["rays"] <= n
     assert b["nodes"] >= b["rays"] and b["tris"] > 0
+
+
+def test_autograd_wrapper_matches_the_derivative_pair(renderers):
+    """drmlt.autograd: torch's first and second derivatives of log f through the
+    C-ABI pair equal drmlt_path_grad_hess's gradient and Hessian."""
+    import torch
+    from drmlt.autograd import path_log_f
+    recs = [rec for rec in _need("cfg2", "tech") if rec["dim"] == 8 and rec["contrib"][0]["ss"] > 1e-15][:16]
+    r = renderers("cfg2")
+    paths = np.array([path_record(rec["path"], rec["path"]["camDepth"], rec["path"]["lgtDepth"], _first_tri(r),
+                                  rec["pos"]) for rec in recs])
+    u = torch.tensor(np.array([rec["pos"] for rec in recs], np.float32), requires_grad=True)
+    f = path_log_f(r, paths, u)
+    uh = np.zeros((len(recs), 24), np.float32)
+    uh[:, :8] = u.detach().numpy()
+    g_ref, h_ref = r.path_grad_hess(paths, uh)
+    np.testing.assert_allclose(f.detach().numpy(), r.path_eval(paths, uh), rtol=1e-6)
+    (g,) = torch.autograd.grad(f.sum(), u, create_graph=True)
+    np.testing.assert_allclose(g.detach().numpy(), g_ref[:, :8], rtol=1e-6, atol=1e-6)
+    for i in range(8):
+        (hi,) = torch.autograd.grad(g[:, i].sum(), u, retain_graph=True)
+        np.testing.assert_allclose(hi.numpy(), h_ref.reshape(-1, 576)[:, :64].reshape(-1, 8, 8)[:, i, :],
+                                   rtol=1e-6, atol=1e-6)
+
+
+def test_create_rejects_bad_environment_lights(built_lib, scene_root):
+    """drmlt_create: at most one environment light, and it needs an image."""
+    import dataclasses
+    from drmlt import capi
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    from helpers import scene_xml
+    sd = dscene.load_scene(scene_xml("cfgE", scene_root))
+    env = [L for L in sd.lights if L.type == capi.LIGHT_ENV][0]
+    twice = dataclasses.replace(sd, lights=list(sd.lights) + [capi.Light.from_buffer_copy(env)])
+    with pytest.raises(Exception, match="at most one environment light"):
+        Renderer(twice)
+    empty = capi.Light.from_buffer_copy(env)
+    empty.env_width = 0
+    lights = [empty if L.type == capi.LIGHT_ENV else L for L in sd.lights]
+    with pytest.raises(Exception, match="environment light needs an image"):
+        Renderer(dataclasses.replace(sd, lights=lights))
