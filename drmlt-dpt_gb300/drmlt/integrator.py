@@ -249,9 +249,21 @@ class DRIntegrator(Integrator):
     """Delayed-rejection MLT (src/integrators/delayed/delayed.cpp)."""
 
 
+class H2MCIntegrator(Integrator):
+    """H2MC (src/integrators/h2mc.cpp) without its lens mutation."""
+
+
+class MCMCIntegrator(Integrator):
+    """Plain MMLT (src/integrators/mcmc.cpp) without its lens mutation."""
+
+
+_CLASSES = {"drmlt": DRIntegrator, "h2mc": H2MCIntegrator, "mcmc": MCMCIntegrator}
+
+
 def make_integrator(xml_path: str, **kw) -> Integrator:
-    """main()'s dispatch on the scene's integrator (src/main.cpp:104-120)."""
+    """main()'s dispatch on the scene's integrator (src/main.cpp:104-120); the
+    reference's `mc` path tracer is not part of this library."""
     sd = load_scene(xml_path)
-    if sd.options.integrator == "drmlt":
-        return DRIntegrator(sd, **kw)
-    raise NotImplementedError("integrator %r is not implemented on the GPU path yet" % sd.options.integrator)
+    if sd.options.integrator not in _CLASSES:
+        raise ValueError("Unknown integrator %r" % sd.options.integrator)
+    return _CLASSES[sd.options.integrator](sd, **kw)

@@ -1,7 +1,8 @@
-"""Scene front end: the reference's scene XML subset + OBJ meshes -> drmlt_scene_desc.
+"""Scene front end: the reference's scene XML subset + meshes -> drmlt_scene_desc.
 
 Mirrors ParseScene / ParseSceneNode (src/parsescene.cpp:566-613) for
-<sensor type="perspective">, <shape type="obj"> with diffuse / phong /
+<sensor type="perspective">, <shape type="obj"|"serialized"> (drmlt/meshio.py)
+with diffuse / phong /
 roughdielectric / twosided BSDFs and area <emitter>, point and envmap (PFM
 image) <emitter>s, and the <dpt> option block
 (ParseDptOptions, src/parsescene.cpp:505-564). Camera matrices follow
@@ -20,6 +21,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import capi
+from .meshio import load_obj, load_serialized  # noqa: F401  (load_obj re-exported)
 
 
 # ---------------------------------------------------------------- options
@@ -170,56 +172,6 @@ def parse_transform(node) -> np.ndarray:
     return t
 
 
-# ---------------------------------------------------------------- OBJ
-def load_obj(path: str, to_world: np.ndarray):
-    """ParseObj (src/parseobj.cpp): triangles (quads split 0-1-2, 0-2-3) with
-    their vertex positions and shading normals in world space."""
-    pos, nor = [], []
-    tris_p, tris_n = [], []
-    with open(path) as f:
-        for line in f:
-            tok = line.split()
-            if not tok or tok[0].startswith("#"):
-                continue
-            if tok[0] == "v":
-                w = float(tok[4]) if len(tok) > 4 else 1.0
-                pos.append([float(tok[1]) / w, float(tok[2]) / w, float(tok[3]) / w])
-            elif tok[0] == "vn":
-                n = np.array([float(tok[1]), float(tok[2]), float(tok[3])])
-                nor.append(n / np.linalg.norm(n))
-            elif tok[0] == "f":
-                idx = []
-                for t in tok[1:]:
-                    s = t.split("/")
-                    vi = int(s[0]) - 1
-                    ni = int(s[2]) - 1 if len(s) > 2 and s[2] else -1
-                    idx.append((vi, ni))
-                faces = [(idx[0], idx[1], idx[2])]
-                if len(idx) == 4:
-                    faces.append((idx[0], idx[2], idx[3]))
-                for fc in faces:
-                    tris_p.append([v for v, _ in fc])
-                    tris_n.append([n for _, n in fc])
-    P = np.asarray(pos, np.float64)
-    P = (to_world @ np.c_[P, np.ones(len(P))].T).T
-    P = P[:, :3] / P[:, 3:4]
-    inv = np.linalg.inv(to_world)
-    Nn = (inv[:3, :3].T @ np.asarray(nor, np.float64).T).T if nor else np.zeros((0, 3))
-    T = len(tris_p)
-    positions = np.zeros((T, 3, 3), np.float32)
-    normals = np.zeros((T, 3, 3), np.float32)
-    for t in range(T):
-        for k in range(3):
-            positions[t, k] = P[tris_p[t][k]]
-        if all(n >= 0 for n in tris_n[t]):
-            for k in range(3):
-                normals[t, k] = Nn[tris_n[t][k]]
-        else:  # no normals in the file: geometric normal
-            e = np.cross(positions[t, 1] - positions[t, 0], positions[t, 2] - positions[t, 0])
-            normals[t, :] = e / np.linalg.norm(e)
-    return positions, normals
-
-
 def read_pfm(path: str) -> np.ndarray:
     """A PFM image as H x W x 3 float32, top row first (Image3's layout: the
     file stores rows bottom to top; a one-channel file is replicated to RGB as
@@ -331,11 +283,12 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
                         if fch.get("name") == "width": W = int(fch.get("value"))
                         elif fch.get("name") == "height": H = int(fch.get("value"))
             cam = dict(fov=fov, near=near, far=far, width=W, height=H, to_world=to_world)
-        elif ch.tag == "shape":
-            if ch.get("type") != "obj":
-                raise ValueError("only obj shapes are supported (got %r)" % ch.get("type"))
+        elif ch.tag == "shape":  # ParseShape (src/parsescene.cpp:190-300)
+            kind = ch.get("type")
+            if kind not in ("obj", "serialized"):
+                raise ValueError("Invalid shape %r (obj and serialized are supported)" % kind)
             bsdf = None
-            fname, to_world = None, np.eye(4)
+            fname, to_world, shape_index = None, np.eye(4), 0
             emitter = None
             for s in ch:
                 if s.tag == "bsdf" and bsdf is None:
@@ -344,11 +297,18 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
                     bsdf = bsdf_map[s.get("id")]
                 elif s.get("name") == "filename":
                     fname = s.get("value")
+                elif s.get("name") == "shapeIndex":
+                    shape_index = int(s.get("value"))
                 elif s.get("name") == "toWorld" and s.tag == "transform":
                     to_world = parse_transform(s)
+                elif s.get("name") == "toWorld" and s.tag == "animation":
+                    raise ValueError("animated toWorld (motion blur) is not supported")
                 elif s.tag == "emitter":
                     emitter = s
-            p, n = load_obj(os.path.join(base, fname), to_world)
+            if kind == "obj":
+                p, n = load_obj(os.path.join(base, fname), to_world)
+            else:
+                p, n = load_serialized(os.path.join(base, fname), shape_index, to_world)
             shape_id = len(first)
             first.append(ntri)
             count.append(len(p))

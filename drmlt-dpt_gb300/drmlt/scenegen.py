@@ -331,3 +331,81 @@ def config4_small(outdir: str, spp: int = 4, dr_type: str = "mira") -> str:
     with open(path, "w") as f:
         f.write(xml)
     return path
+
+
+def config_meshes(outdir: str) -> str:
+    """Mesh front-end check scene (no render intended): every loader branch of
+    the reference's ParseObj / LoadSerialized once, seeded.
+
+    shapes, in order:
+      0  OBJ without normals, ``v/vt`` corners with a texture seam, rotated and
+         non-uniformly scaled (vertex normals computed; seam vertices split);
+      1  OBJ quads with ``vn`` under a non-uniform scale (inverse-transpose
+         normals, not renormalised);
+      2  serialized v4, single precision, stored normals (shapeIndex 0);
+      3  serialized v4, double precision, no normals, uvs + colours, a
+         degenerate and obtuse triangles (shapeIndex 1);
+      4  serialized v4, single precision, normals + uvs (shapeIndex 2),
+         translated;
+      5  serialized v3, single precision, no normals (shapeIndex 1)."""
+    from . import procedural as P
+    from .meshio import write_serialized
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.default_rng(17)
+    V, F = P.geodesic_sphere(3)
+    V = V * (1.0 + 0.1 * P.gradient_noise(2.0 * V, 17))[:, None]
+    # texture coordinates split along x < 0 / x >= 0: corners of faces that
+    # straddle the split get their own vt per side
+    side = (V[F].mean(axis=1)[:, 0] >= 0).astype(np.int64)
+    lines = ["v %.9g %.9g %.9g" % tuple(v) for v in V]
+    lines += ["vt %.6g %.6g" % (0.25 + 0.5 * s, 0.5) for s in (0, 1)]
+    lines += ["f %d/%d %d/%d %d/%d" % (a + 1, s + 1, b + 1, s + 1, c + 1, s + 1) for (a, b, c), s in zip(F, side)]
+    with open(os.path.join(outdir, "noNormals.obj"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    qV = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0.2], [0, 1, 0], [2, 0, 0.3], [2, 1, 0]], np.float64)
+    qN = rng.normal(size=(6, 3))
+    lines = ["v %.9g %.9g %.9g" % tuple(v) for v in qV] + ["vn %.9g %.9g %.9g" % tuple(n) for n in qN]
+    lines += ["f 1//1 2//2 3//3 4//4", "f 2//2 5//5 6//6 3//3"]
+    with open(os.path.join(outdir, "quads.obj"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    gV, gF = P._grid(4, 1.0, 0.0)
+    gV = gV + rng.uniform(-0.2, 0.2, gV.shape) * [1, 0, 1]
+    gV[:, 1] = rng.uniform(-0.1, 0.1, len(gV))
+    gF = np.vstack([gF, [[0, 1, 2]]])  # a degenerate triangle (0, 1, 2 lie on one grid row)
+    gV[2] = 2 * gV[1] - gV[0]
+    sV, sF = P.geodesic_sphere(2)
+    meshes = [dict(positions=sV * 0.5, indices=sF, normals=sV, name="sphere"),
+              dict(positions=gV, indices=gF, uvs=gV[:, [0, 2]], colors=rng.uniform(size=gV.shape), name="grid"),
+              dict(positions=sV * [0.3, 0.6, 0.3], indices=sF, normals=sV * [2, 1, 2], uvs=sV[:, :2], name="egg")]
+    write_serialized(os.path.join(outdir, "meshes_v4_f.serialized"), [meshes[0], meshes[2]], version=4)
+    write_serialized(os.path.join(outdir, "meshes_v4_d.serialized"), [meshes[0], meshes[1]], version=4, double=True)
+    write_serialized(os.path.join(outdir, "meshes_v4_f3.serialized"), [meshes[1], meshes[1], meshes[2]], version=4)
+    write_serialized(os.path.join(outdir, "meshes_v3.serialized"),
+                     [meshes[2], dict(positions=gV * 0.7, indices=gF)], version=3)
+    diffuse = '<bsdf type="diffuse"><rgb name="reflectance" value="0.5 0.5 0.5"/></bsdf>'
+    shapes = [
+        ('obj', 'noNormals.obj', None, '<rotate x="0.3" y="1" z="0.2" angle="37"/><scale x="1.5" y="0.7" z="1.1"/>'),
+        ('obj', 'quads.obj', None, '<scale x="2" y="0.5" z="1"/><translate x="0.1" y="0" z="-0.3"/>'),
+        ('serialized', 'meshes_v4_f.serialized', 0, '<scale x="1" y="2" z="1"/>'),
+        ('serialized', 'meshes_v4_d.serialized', 1, '<rotate x="0" y="1" z="0" angle="20"/>'),
+        ('serialized', 'meshes_v4_f3.serialized', 2, '<translate x="0.5" y="0.2" z="0.1"/>'),
+        ('serialized', 'meshes_v3.serialized', 1, ''),
+    ]
+    body = []
+    for kind, fn, idx, xf in shapes:
+        extra = '' if idx is None else '<integer name="shapeIndex" value="%d"/>' % idx
+        body.append('  <shape type="%s"><string name="filename" value="%s"/>%s'
+                    '<transform name="toWorld">%s</transform>%s</shape>' % (kind, fn, extra, xf, diffuse))
+    body.append('  <emitter type="point"><point name="position" x="0" y="3" z="3"/>'
+                '<rgb name="intensity" value="10 10 10"/></emitter>')
+    sensor = ('  <sensor type="perspective">\n'
+              '    <float name="fov" value="40"/>\n'
+              '    <transform name="toWorld"><lookat origin="0, 0, 6" target="0, 0, 0" up="0, 1, 0"/></transform>\n'
+              '    <film type="hdrfilm"><integer name="width" value="64"/><integer name="height" value="64"/></film>\n'
+              '  </sensor>\n')
+    xml = ('<?xml version="1.0" encoding="utf-8"?>\n<scene version="0.5.0">\n'
+           + SceneOptions(maxdepth=3, numchains=64, spp=1).xml() + sensor + "\n".join(body) + "\n</scene>\n")
+    path = os.path.join(outdir, "scene.xml")
+    with open(path, "w") as f:
+        f.write(xml)
+    return path

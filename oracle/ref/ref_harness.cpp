@@ -16,11 +16,14 @@
 // the continuous offsets move the path.
 //
 // usage: ref_harness <scene.xml> <libdir> <maxDervDepth> <out.jsonl> <mode> <seed0> <count> [extra]
-//   mode = bidir | subpath | direct | tech
+//   mode = camera | bidir | subpath | direct | tech | mesh
+//   (mesh: every shape's triangles as loaded by ParseObj / LoadSerialized,
+//    src/parseobj.cpp:148-264, src/loadserialized.cpp:236-317)
 #include "parsescene.h"
 #include "path.h"
 #include "scene.h"
 #include "shape.h"
+#include "trianglemesh.h"
 #include "light.h"
 #include "camera.h"
 #include "gaussian.h"
@@ -337,6 +340,29 @@ void ModeTech(uint64_t seed0, int count, int nPerturb, const PathFuncLib &lib, i
     }
 }
 
+// Per shape: the world-space corner positions and shading normals of every
+// triangle, in TriMeshData index order.
+void ModeMesh() {
+    for (size_t i = 0; i < g_scene->objects.size(); i++) {
+        const TriangleMesh *m = dynamic_cast<const TriangleMesh *>(g_scene->objects[i].get());
+        if (m == nullptr) continue;
+        const TriMeshData &d = *m->data;
+        for (int pass = 0; pass < 2; pass++) {
+            fprintf(g_out, pass == 0 ? "{\"shape\":%d,\"p\":[" : "],\"n\":[", int(i));
+            const std::vector<Vector3> &v = pass == 0 ? d.position0 : d.normal0;
+            bool first = true;
+            for (const TriIndex &t : d.indices)
+                for (int k = 0; k < 3; k++)
+                    for (int c = 0; c < 3; c++) {
+                        if (!first) fputc(',', g_out);
+                        first = false;
+                        F(v[t.index[k]][c]);
+                    }
+        }
+        fprintf(g_out, "]}\n");
+    }
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -392,6 +418,8 @@ int main(int argc, char **argv) {
         ModeSubpath(seed0, count, scene->options->maxDepth);
     } else if (mode == "direct") {
         ModeDirect(seed0, count);
+    } else if (mode == "mesh") {
+        ModeMesh();
     } else if (mode == "tech") {
         if (chdir(libdir.c_str()) != 0) return 3;
         std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);

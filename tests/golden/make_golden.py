@@ -13,9 +13,12 @@ synthetic Cornell-box scenes of drmlt/scenegen.py and writes gzipped JSON lines:
   <cfg>_render*.json.gz   a full `dpt -d` render of the scene (the reference's
                           DRIntegrator::Render): its printed acceptance counters
                           and the final image averaged over 16 x 16 blocks
+  cfgM_mesh.jsonl.gz      every shape of drmlt/scenegen.py:config_meshes as the
+                          reference's ParseObj / LoadSerialized load it
 
 usage (in a container that has the reference at /root/reference):
   python tests/golden/make_golden.py [--render] [cfg1] [cfg2]   (--render: only the renders)
+  python tests/golden/make_golden.py --mesh                     (only cfgM_mesh)
 """
 from __future__ import annotations
 
@@ -133,8 +136,27 @@ def run(cfg: str):
         shutil.rmtree(tmp)
 
 
+def mesh():
+    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
+    tmp = tempfile.mkdtemp()
+    try:
+        xml = scenegen.config_meshes(os.path.join(tmp, "scene"))
+        out = os.path.join(tmp, "mesh.jsonl")
+        subprocess.check_call([HARNESS, xml, tmp, "5", out, "mesh", "0", "0"], stdout=subprocess.DEVNULL)
+        dst = os.path.join(HERE, "cfgM_mesh.jsonl.gz")
+        with open(out, "rb") as f, open(dst, "wb") as raw:
+            with gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as g:
+                shutil.copyfileobj(f, g)
+        print(dst, os.path.getsize(dst))
+    finally:
+        shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
     args = sys.argv[1:]
+    if "--mesh" in args:
+        mesh()
+        sys.exit(0)
     only_render = "--render" in args
     for c in [a for a in args if not a.startswith("--")] or ["cfg1"]:
         if not only_render:
