@@ -1,5 +1,6 @@
 """Builds libdrmlt.so in-tree for sm_103a (nvcc: the chain-loop translation unit, the
-path-derivative translation unit and the host BVH builder, compiled in parallel).
+path-derivative translation unit, the host BVH builder and the host image writer,
+compiled in parallel).
 
 usage: python drmlt-dpt_gb300/build.py [--force]
 """
@@ -40,7 +41,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     objs = []
     jobs = []
-    for src in ("drmlt.cu", "derivs.cu", "bvh.cpp"):
+    for src in ("drmlt.cu", "derivs.cu", "bvh.cpp", "image_io.cpp"):
         obj = os.path.join(LIBDIR, src + ".o")
         cmd = [NVCC] + ARCH + FLAGS + TU_FLAGS.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):

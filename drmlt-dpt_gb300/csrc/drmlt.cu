@@ -3,6 +3,7 @@
 #include "drmlt_capi.h"
 #include "kernels.cuh"
 #include "bvh.h"
+#include "errors.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -13,13 +14,17 @@
 using namespace drmlt;
 
 namespace {
-
 thread_local std::string g_error;
+}  // namespace
 
-int fail(int code, const std::string &msg) {
+int drmlt::set_error(int code, const char *msg) {
     g_error = msg;
     return code;
 }
+
+namespace {
+
+int fail(int code, const std::string &msg) { return set_error(code, msg.c_str()); }
 
 #define CK(call)                                                                                \
     do {                                                                                        \
@@ -835,6 +840,18 @@ struct Renderer {
         }
         return DRMLT_OK;
     }
+
+    int partial_film(float *rgb) {
+        const size_t n = size_t(W) * H * 3;
+        std::vector<float> ind(n);
+        unsigned long long h[kNumStats];
+        CK(cudaMemcpy(ind.data(), cv.film, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h, cv.stats, sizeof(h), cudaMemcpyDeviceToHost));
+        const unsigned long long work = h[kStatMutations];
+        const float factor = work > 0 ? float(double(W) * double(H) / double(work)) : 0.0f;
+        for (size_t i = 0; i < n; i++) rgb[i] = factor * ind[i];
+        return DRMLT_OK;
+    }
 };
 
 }  // namespace
@@ -933,6 +950,11 @@ int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes,
 int drmlt_get_film(void *handle, float *rgb) {
     if (!handle || !rgb) return fail(DRMLT_E_ARG, "null argument");
     return static_cast<Renderer *>(handle)->film(rgb);
+}
+
+int drmlt_get_partial_film(void *handle, float *rgb) {
+    if (!handle || !rgb) return fail(DRMLT_E_ARG, "null argument");
+    return static_cast<Renderer *>(handle)->partial_film(rgb);
 }
 
 int drmlt_get_stats(void *handle, drmlt_stats *st) {

@@ -104,6 +104,8 @@ _SIGS = {
     "drmlt_run": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "drmlt_render": (C.c_int, [C.c_void_p]),
     "drmlt_get_film": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "drmlt_get_partial_film": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "drmlt_write_exr": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_void_p]),
     "drmlt_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "drmlt_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "drmlt_kernel_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

@@ -8,6 +8,8 @@ on the GPU through the C ABI; this module only marshals arguments.
 """
 from __future__ import annotations
 
+import os
+import time
 import warnings
 
 import ctypes as C
@@ -147,6 +149,13 @@ class Renderer:
         capi.check(capi.lib().drmlt_get_film(self.handle, capi.ptr(out)))
         return out
 
+    def partial_film(self) -> np.ndarray:
+        """The indirect film scaled by pixels / mutations so far (the reference's
+        intermediate images, delayed.cpp:612-637)."""
+        out = np.zeros((self.scene.height, self.scene.width, 3), np.float32)
+        capi.check(capi.lib().drmlt_get_partial_film(self.handle, capi.ptr(out)))
+        return out
+
     def stats(self) -> dict:
         s = capi.Stats()
         capi.check(capi.lib().drmlt_get_stats(self.handle, C.byref(s)))
@@ -241,8 +250,62 @@ class Integrator:
         return self.renderer.prepass()
 
     def Render(self) -> np.ndarray:
-        self.renderer.render()
-        return self.renderer.film()
+        """The whole render (drmlt_render). With reportintervalseconds > 0 the
+        chain loop runs in slices and, like delayed.cpp:612-637, writes the
+        partial film to <partial dir>/<name>_<k>.exr once k intervals have
+        passed since the prepass, appending the elapsed seconds to
+        <name>_time.csv; the partial dir is <integrator>_partial (or
+        <output_name>_partial) beside the scene's output image."""
+        interval = self.scene.options.reportIntervalSeconds
+        r = self.renderer
+        if interval <= 0:
+            r.render()
+            return r.film()
+        r.direct()
+        r.prepass()
+        if r.options.autotune and r.total_iterations() >= 1024:
+            r.autotune(8)
+        base = self.output_name or self.scene.options.integrator
+        partial = os.path.join(os.path.dirname(self.output_path()), base + "_partial")
+        os.makedirs(partial, exist_ok=True)
+        t0, image_id, step = time.perf_counter(), 1, 8
+        while True:
+            t = time.perf_counter()
+            if r.run(step) == 0:
+                break
+            # slices of about a tenth of the interval keep the write times close to it
+            step = max(1, min(4 * step, int(step * 0.1 * interval / max(time.perf_counter() - t, 1e-6))))
+            elapsed = time.perf_counter() - t0
+            if elapsed >= interval * image_id:
+                write_image(os.path.join(partial, "%s_%d.exr" % (base, image_id)), r.partial_film())
+                with open(os.path.join(partial, base + "_time.csv"), "w" if image_id == 1 else "a") as f:
+                    f.write("%g,\n" % elapsed)
+                image_id += 1
+        return r.film()
+
+    def output_path(self) -> str:
+        """The scene's output image (the film's filename, default image.exr
+        beside the scene file, src/parsescene.cpp:149-160, 574)."""
+        return self.scene.camera.get("output") or os.path.join(os.path.dirname(os.path.abspath(self.scene.path)),
+                                                               "image.exr")
+
+    def write_image(self, path: str | None = None) -> str:
+        """WriteImage of the final film (src/main.cpp:130) to path or output_path()."""
+        path = path or self.output_path()
+        write_image(path, self.renderer.film())
+        return path
+
+
+def write_image(path: str, img: np.ndarray) -> None:
+    """WriteImage (src/image.cpp:45-58): .exr through the C ABI, .pfm as float PFM."""
+    if path.lower().endswith(".exr"):
+        from .exr import write_exr
+        write_exr(path, img)
+    elif path.lower().endswith(".pfm"):
+        from .scenegen import write_pfm
+        write_pfm(path, img)
+    else:
+        raise ValueError("%s: only .exr and .pfm output is supported" % path)
 
 
 class DRIntegrator(Integrator):

@@ -3,8 +3,8 @@
 Mirrors ParseScene / ParseSceneNode (src/parsescene.cpp:566-613) for
 <sensor type="perspective">, <shape type="obj"|"serialized"> (drmlt/meshio.py)
 with diffuse / phong /
-roughdielectric / twosided BSDFs and area <emitter>, point and envmap (PFM
-image) <emitter>s, and the <dpt> option block
+roughdielectric / twosided BSDFs and area <emitter>, point and envmap (EXR or
+PFM image) <emitter>s, and the <dpt> option block
 (ParseDptOptions, src/parsescene.cpp:505-564). Camera matrices follow
 Camera::Camera (src/camera.cpp:11-28) and the transform helpers of
 src/transform.cpp, computed in double and rounded to float.
@@ -186,6 +186,18 @@ def read_pfm(path: str) -> np.ndarray:
     return np.repeat(img, 3, axis=2) if ch == 1 else img
 
 
+def read_image(path: str) -> np.ndarray:
+    """Image3::Image3 (src/image.cpp:5-43) for the formats this front end
+    reads: OpenEXR (drmlt/exr.py) and PFM; H x W x 3 float32, top row first."""
+    low = path.lower()
+    if low.endswith(".exr"):
+        from .exr import read_exr
+        return read_exr(path)
+    if low.endswith(".pfm"):
+        return read_pfm(path)
+    raise ValueError("%s: only .exr and .pfm images are supported" % path)
+
+
 # ---------------------------------------------------------------- scene
 @dataclass
 class SceneData:
@@ -271,6 +283,7 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
             bsdf_map[ch.get("id")] = _parse_bsdf(ch)
         elif ch.tag == "sensor":
             fov, near, far, W, H = 45.0, 1e-2, 1000.0, 512, 512
+            output = os.path.join(base, "image.exr")  # src/parsescene.cpp:574
             to_world = np.eye(4)
             for s in ch:
                 n = s.get("name")
@@ -282,7 +295,8 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
                     for fch in s:
                         if fch.get("name") == "width": W = int(fch.get("value"))
                         elif fch.get("name") == "height": H = int(fch.get("value"))
-            cam = dict(fov=fov, near=near, far=far, width=W, height=H, to_world=to_world)
+                        elif fch.get("name") == "filename": output = os.path.join(base, fch.get("value"))
+            cam = dict(fov=fov, near=near, far=far, width=W, height=H, to_world=to_world, output=output)
         elif ch.tag == "shape":  # ParseShape (src/parsescene.cpp:190-300)
             kind = ch.get("type")
             if kind not in ("obj", "serialized"):
@@ -362,7 +376,7 @@ def load_scene(xml_path: str, honour_aniso_stddev: bool = False) -> SceneData:
                         to_world = parse_transform(e)
                 if fname is None:
                     raise ValueError("envmap without filename")
-                img = read_pfm(os.path.join(base, fname))
+                img = read_image(os.path.join(base, fname))
                 env_images.append(img)
                 L.env_rgb = img.ctypes.data_as(C.POINTER(C.c_float))
                 L.env_height, L.env_width = img.shape[0], img.shape[1]

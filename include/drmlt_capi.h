@@ -27,6 +27,7 @@ extern "C" {
 #define DRMLT_E_CUDA (-2)      /* CUDA error (device missing, launch failure, ...) */
 #define DRMLT_E_STATE (-3)     /* call out of order (e.g. run before prepass) */
 #define DRMLT_E_OVERFLOW (-4)  /* a fixed-capacity buffer overflowed */
+#define DRMLT_E_IO (-5)        /* a file could not be written */
 
 #define DRMLT_MAX_LEN 12           /* longest path (segments) a chain may hold */
 #define DRMLT_MAX_DIM 24           /* 2 * DRMLT_MAX_LEN */
@@ -191,6 +192,15 @@ int drmlt_render(void *handle);
 
 /* Final film (direct/directSpp + indirect/spp, delayed.cpp:681-685), W*H*3 floats. */
 int drmlt_get_film(void *handle, float *rgb);
+/* The film of the reference's intermediate images (delayed.cpp:612-637:
+ * BufferToFilm of the indirect buffer alone, scaled by numPixels / mutations
+ * done so far), W*H*3 floats; zeros before the first mutation. */
+int drmlt_get_partial_film(void *handle, float *rgb);
+/* WriteImage (src/image.cpp:45-58): a width x height RGB float image, rows top
+ * to bottom, to an OpenEXR file (scanline, HALF channels, no compression;
+ * floats rounded to nearest even half). Host only: needs no device.
+ * DRMLT_E_IO when the file cannot be written. */
+int drmlt_write_exr(const char *filename, int width, int height, const float *rgb);
 int drmlt_get_stats(void *handle, drmlt_stats *stats);
 /* Device time of the last drmlt_run in milliseconds (CUDA events). */
 int drmlt_last_run_ms(void *handle, float *ms);

@@ -181,3 +181,55 @@ def test_single_stage_integrators_match_reference(built_lib, scene_root, cfg, na
     H, W, _ = img.shape
     mb = img.reshape(8, H // 8, 8, W // 8, 3).mean(axis=(1, 3))
     assert (np.abs(mb - rb) / np.maximum(rb, 1e-3)).mean() < 0.06
+
+
+def test_partial_film_and_interval_images(built_lib, scene_root, monkeypatch):
+    """drmlt_get_partial_film is the indirect film scaled by pixels / mutations
+    done (the reference's intermediate images, delayed.cpp:612-637). A render
+    with reportintervalseconds writes them as <integrator>_partial/drmlt_<k>.exr
+    plus drmlt_time.csv and ends on the film of the render without slices; the
+    final image goes to the scene's output EXR."""
+    from drmlt import exr, scenegen
+    from drmlt import integrator as I
+    from drmlt import scene as dscene
+    d = os.path.join(scene_root, "partial_images")
+    sd = dscene.load_scene(scenegen.config1(d, spp=2, extra={"reportintervalseconds": "1"}))
+    assert sd.options.reportIntervalSeconds == 1
+    with I.Renderer(sd, num_chains=4096) as r:
+        r.direct()
+        r.prepass()
+        direct = r.film().astype(np.float64)
+        np.testing.assert_array_equal(r.partial_film(), 0.0)
+        r.run(5)
+        mutations = r.stats()["mutations"]
+        assert mutations == 5 * 4096
+        want = (r.film() - direct) * sd.options.spp * sd.width * sd.height / mutations
+        np.testing.assert_allclose(r.partial_film(), want, rtol=2e-5, atol=1e-5)
+
+    clock = [0.0]
+
+    def fake_clock():  # a quarter second per reading: partial images every few slices
+        clock[0] += 0.25
+        return clock[0]
+
+    monkeypatch.setattr(I.time, "perf_counter", fake_clock)
+    a = I.make_integrator(sd.path, num_chains=4096)
+    film = a.Render()
+    monkeypatch.undo()
+    b = I.Integrator(sd, num_chains=4096)
+    sd.options.reportIntervalSeconds = 0
+    ref = b.Render()
+    assert a.renderer.stats() == b.renderer.stats()
+    np.testing.assert_allclose(film, ref, rtol=1e-4, atol=1e-6)
+    part = os.path.join(d, "drmlt_partial")
+    times = open(os.path.join(part, "drmlt_time.csv")).read().split()
+    assert len(times) >= 2
+    for k in range(1, len(times) + 1):
+        img = exr.read_exr(os.path.join(part, "drmlt_%d.exr" % k))
+        assert img.shape == (sd.height, sd.width, 3) and np.isfinite(img).all() and img.mean() > 0
+    assert [float(t.rstrip(",")) for t in times] == sorted(float(t.rstrip(",")) for t in times)
+    out = a.write_image()
+    assert out == os.path.join(os.path.abspath(d), "image.exr")
+    np.testing.assert_array_equal(exr.read_exr(out), film.astype(np.float16).astype(np.float32))
+    a.renderer.close()
+    b.renderer.close()
