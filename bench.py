@@ -140,6 +140,13 @@ NCU_TRAFFIC = {
     "config4": {"stage1": 2 * 145.7e6},
 }
 
+# Floating-point operations (FP32, FP64) of the derivative and Gaussian
+# kernels per chain-loop iteration (both chain groups): ncu's executed-op
+# counters (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on.sum and
+# the d-variants, an FMA counted as 2) summed over the bench's own launches of
+# these kernels after the autotuner; None where not captured.
+NCU_FLOPS = {}
+
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
 # HBM). A Slot is 328 B, the per-chain scratch 128 B (both asserted in
 # csrc/chain.cuh), a stored FP64 Gaussian 5008 B.
@@ -182,6 +189,8 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     stats = r.stats()
     rays = ray_roofline(r, _peaks()[0]) if rank == 0 else None
+    fma = {"fp32_tflops": r.fma_benchmark(False)["tflops"], "fp64_tflops": r.fma_benchmark(True)["tflops"]} \
+        if rank == 0 else None
     r.close()
     if world > 1:
         t = torch.tensor([dev_ms], device="cuda")
@@ -235,6 +244,22 @@ def run_ours(args, world, rank, local):
             "frac": achieved / hbm, "traffic": NCU_TRAFFIC.get(args.workload, {}).get(dom), "peak_kind": peak_kind,
             "stage_ms_per_iteration": {k: v / iters for k, v in prof.items()}}
 
+    # ---- compute rooflines: derivative kernel on the FP32 FMA roof, Gaussian
+    # kernel on the FP64 roof, both against this device's measured FMA peaks
+    compute = None
+    if fma is not None:
+        compute = {"peaks_measured": fma}
+        for st in ("derivs_x", "derivs_z", "gauss_x", "gauss_z"):
+            ms = prof[st] / iters
+            ent = {"ms_per_iteration": ms}
+            counts = NCU_FLOPS.get(args.workload, {}).get(st)
+            if counts is not None:
+                for kind, n, peak in (("fp32", counts[0], fma["fp32_tflops"]), ("fp64", counts[1], fma["fp64_tflops"])):
+                    a = n / (ms * 1e-3) / 1e12
+                    ent[kind] = {"flops_per_iteration": n, "achieved": a, "peak": peak, "unit": "TFLOP/s",
+                                 "frac": a / peak}
+            compute[st] = ent
+
     out = None
     if rank == 0:
         relmse = relmse_plain = None
@@ -261,6 +286,7 @@ def run_ours(args, world, rank, local):
                        "l2": "chain state (3 slots + 3 FP64 Gaussians per chain, %.2f GB) exceeds L2" % gb},
             "e2e": e2e,
             "roofline": roof,
+            "compute_roofline": compute,
             "cpu_baseline": cpu,
             "rays": rays,
             "time_to_relmse": relmse,

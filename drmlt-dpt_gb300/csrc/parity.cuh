@@ -390,4 +390,37 @@ int drmlt_ray_benchmark(void *handle, int kind, int n_rays, int repeats, float *
     return DRMLT_OK;
 }
 
+int drmlt_fma_benchmark(void *handle, int fp64, int iterations, float *ms, double *flops) {
+    if (!handle || !ms || !flops) return fail(DRMLT_E_ARG, "null argument");
+    if (iterations <= 0) return fail(DRMLT_E_ARG, "iterations must be positive");
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = 4 * sms, threads = 256;
+    DevBuf<double> sink;
+    int rc;
+    if ((rc = sink.alloc(blocks))) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    for (int pass = 0; pass < 2; pass++) {  // pass 0: warm-up at a tenth of the length
+        const int it = pass == 0 ? iterations / 10 + 1 : iterations;
+        if (pass == 1) CK(cudaEventRecord(e0));
+        if (fp64)
+            k_fma_peak<double><<<blocks, threads>>>(it, 0.999999, 1e-6, sink.p);
+        else
+            k_fma_peak<float><<<blocks, threads>>>(it, 0.9999f, 1e-6f, reinterpret_cast<float *>(sink.p));
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t;
+    *flops = 2.0 * 8.0 * double(blocks) * threads * double(iterations);
+    return DRMLT_OK;
+}
+
 }  // extern "C"

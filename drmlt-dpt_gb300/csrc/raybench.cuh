@@ -5,6 +5,8 @@
 //   kind 1  diffuse bounce rays from the camera rays' first hits, cosine-
 //           distributed about the shading normal (closest hit)
 //   kind 2  shadow rays of length 2 from the same hits (any hit)
+// Also the arithmetic-peak benchmark (k_fma_peak) that the compute rooflines
+// of the derivative (FP32) and Gaussian (FP64) kernels are quoted against.
 #pragma once
 #include "bsdf_light.cuh"
 
@@ -73,6 +75,28 @@ __global__ void __launch_bounds__(128) k_rays_trace(SceneView s, int anyHit, int
             atomicAdd(counters + 2, (unsigned long long)tests);
         }
     }
+}
+
+// FMA throughput: 8 independent fused multiply-add chains per thread (enough
+// in flight to cover the FMA latency on every SM sub-partition), iterated
+// `iters` times; 2 flops per FMA. The chains converge to b / (1 - a) > 0, so
+// the sink store never happens; it keeps the chains live.
+__device__ __forceinline__ float fma_t(float x, float a, float b) { return fmaf(x, a, b); }
+__device__ __forceinline__ double fma_t(double x, double a, double b) { return fma(x, a, b); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, T *sink) {
+    T x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = T(threadIdx.x + k) * T(1e-3);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = fma_t(x[k], a, b);
+    }
+    T sum = T(0);
+#pragma unroll
+    for (int k = 0; k < 8; k++) sum += x[k];
+    if (sum == T(-1)) sink[blockIdx.x] = sum;
 }
 
 }  // namespace drmlt

@@ -110,6 +110,7 @@ _SIGS = {
     "drmlt_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "drmlt_kernel_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "drmlt_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "drmlt_fma_benchmark": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "drmlt_ray_benchmark": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_void_p]),
     "drmlt_profile": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int64)]),
     "drmlt_total_iterations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

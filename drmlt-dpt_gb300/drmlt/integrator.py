@@ -131,6 +131,13 @@ class Renderer:
                                                   C.byref(ms), counts.ctypes.data))
         return {"ms": ms.value, "rays": counts[0], "nodes": counts[1], "tris": counts[2]}
 
+    def fma_benchmark(self, fp64: bool = False, iterations: int | None = None) -> dict:
+        """drmlt_fma_benchmark: the device's FP32 or FP64 FMA throughput."""
+        ms, flops = C.c_float(), C.c_double()
+        it = iterations or (4000 if fp64 else 200000)
+        capi.check(capi.lib().drmlt_fma_benchmark(self.handle, int(fp64), int(it), C.byref(ms), C.byref(flops)))
+        return {"ms": ms.value, "flops": flops.value, "tflops": flops.value / (ms.value * 1e-3) / 1e12}
+
     STAGES = ("stage1", "derivs_x", "gauss_x", "stage2", "derivs_z", "gauss_z", "finish")
 
     def profile(self, iterations: int):

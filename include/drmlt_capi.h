@@ -270,6 +270,14 @@ int drmlt_trace_rays(void *handle, const float *org, const float *dir, float tmi
  * (48 B each) in one pass. */
 int drmlt_ray_benchmark(void *handle, int kind, int n_rays, int repeats, float *ms_per_pass, double *counts);
 
+/* Arithmetic peak of the current device: a full-occupancy kernel of
+ * independent FMA chains (fp64 = 0: FP32 fmaf, 1: FP64 fma), `iterations`
+ * steps per chain, event-timed after a short warm-up launch. Returns the
+ * kernel time in *ms and its floating-point operations in *flops (2 per FMA).
+ * The compute rooflines of the derivative (FP32) and Gaussian (FP64) kernels
+ * are quoted against it. */
+int drmlt_fma_benchmark(void *handle, int fp64, int iterations, float *ms, double *flops);
+
 /* ComputeGaussian (drsmallstep.cpp:219-266) in FP64: returns mean (MAX_DIM),
  * invCov and cov (MAX_DIM^2 each, row-major) and logDet per input. */
 int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, const float *grad,

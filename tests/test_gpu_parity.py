@@ -254,6 +254,22 @@ def test_ray_benchmark_counts(renderers, kind):
     assert b["nodes"] >= b["rays"] and b["tris"] > 0
 
 
+@pytest.mark.parametrize("fp64", [False, True])
+def test_fma_benchmark(renderers, fp64):
+    """drmlt_fma_benchmark counts 2 flops per FMA over its full-occupancy grid
+    (4 blocks of 256 threads per SM, 8 chains per thread) and runs at a
+    plausible rate; FP32 outruns FP64 on this part."""
+    import torch
+    r = renderers("cfg1")
+    it = 1000 if fp64 else 20000
+    b = r.fma_benchmark(fp64, it)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert b["flops"] == 2 * 8 * 4 * sms * 256 * it
+    assert b["ms"] > 0 and 0.05 < b["tflops"] < 500
+    if not fp64:
+        assert b["tflops"] > r.fma_benchmark(True, 1000)["tflops"]
+
+
 def test_autograd_wrapper_matches_the_derivative_pair(renderers):
     """drmlt.autograd: torch's first and second derivatives of log f through the
     C-ABI pair equal drmlt_path_grad_hess's gradient and Hessian."""
