@@ -30,9 +30,11 @@ def make_options(sd: SceneData, *, seed: int = 0x1234ABCD, device: int = 0,
     if d.integrator not in _INTEGRATORS:
         raise ValueError("Unknown integrator %r" % d.integrator)
     o.integrator = _INTEGRATORS[d.integrator]
-    if d.integrator in ("h2mc", "mcmc") and d.lensPerturbProb > 0:
-        warnings.warn("the lens mutation of integrator=%s (h2mc.cpp:466-532) is not implemented; "
-                      "lensperturbprob=%g is treated as 0" % (d.integrator, d.lensPerturbProb))
+    # mcmc's SmallStep never proposes a lens mutation (mutation.cpp:126-166); only
+    # H2MCSmallStep does (h2mc.cpp:466-532)
+    if d.integrator == "h2mc" and d.lensPerturbProb > 0:
+        warnings.warn("the lens mutation of integrator=h2mc (h2mc.cpp:466-532) is not implemented; "
+                      "lensperturbprob=%g is treated as 0" % d.lensPerturbProb)
     o.dr_type = capi.DR_MIRA if d.type == "mira" else capi.DR_GREEN
     o.aniso_perturb_prob = d.anisoPerturbProb
     o.aniso_perturb_stddev = d.anisoperturbstddev
