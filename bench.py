@@ -145,7 +145,10 @@ NCU_TRAFFIC = {
 # counters (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on.sum and
 # the d-variants, an FMA counted as 2) summed over the bench's own launches of
 # these kernels after the autotuner; None where not captured.
-NCU_FLOPS = {}
+NCU_FLOPS = {
+    "config2": {"derivs_x": (7.256e8, 0.0), "derivs_z": (7.500e8, 0.0),
+                "gauss_x": (9.821e7, 2.690e7), "gauss_z": (1.059e8, 4.613e7)},
+}
 
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
 # HBM). A Slot is 328 B, the per-chain scratch 128 B (both asserted in
