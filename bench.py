@@ -267,9 +267,9 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         relmse = relmse_plain = None
         if not args.no_relmse:
-            ref_spp = 256
+            ref_spp = args.ref_spp
             ref = render_reference(sd, local, ref_spp)
-            spp = 64 if args.workload == "config2" else 128
+            spp = args.relmse_spp or (64 if args.workload == "config2" else 128)
             relmse = time_to_relmse(sd, local, ref, ref_spp, spp=spp)
             relmse_plain = time_to_relmse(sd, local, ref, ref_spp, spp=spp, plain=True)
         if xml is None:
@@ -348,9 +348,11 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False)
     long render (`ref`, ref_spp samples per pixel, other random streams) of the
     same scene: the direct-lighting pass, the prepass (and the autotuner's
     iterations) plus the chain-loop device time up to the first checkpoint
-    (iteration counts growing by 1.25x) that meets the target. Partial images
-    scale the indirect film by total / done iterations. plain=True runs the
-    plain per-stage-launch configuration (PLAIN) without autotuning."""
+    that meets the target (iteration counts growing by 1.25x, by 1/32 once the
+    relMSE is within 1.5x of the target, so the crossing is resolved to ~3%).
+    Partial images scale the indirect film by total / done iterations.
+    plain=True runs the plain per-stage-launch configuration (PLAIN) without
+    autotuning."""
     from drmlt.integrator import Renderer
 
     kw = dict(PLAIN) if plain else {}
@@ -379,7 +381,7 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False)
         if e <= target:
             hit = setup_s + run_s
             break
-        step = max(8, done // 4)
+        step = max(8, done // 4) if e > 1.5 * target else max(8, done // 32)
     r.close()
     return {"value": hit, "unit": "s", "target_relmse": target, "reference": "%d spp GPU render" % ref_spp,
             "setup_s": setup_s, "iterations": done, "spp_equivalent": done * sd.options.numChains /
@@ -433,6 +435,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE measurement")
     ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"])
+    ap.add_argument("--ref-spp", type=int, default=256, help="samples per pixel of the relMSE reference render")
+    ap.add_argument("--relmse-spp", type=int, default=0, help="spp budget of the time-to-relMSE renders")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":
