@@ -50,6 +50,20 @@ def _dist():
     return world, rank, local
 
 
+def replica_totals(dev_ms: float, done: int, world: int, device: str = "cpu"):
+    """Independent replicas (one per rank, no data exchange): the slowest rank's
+    timed-region device time and the mutations of all ranks."""
+    if world <= 1:
+        return dev_ms, done
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([dev_ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(done)], device=device, dtype=torch.float64)
+    dist.all_reduce(n)
+    return float(t.item()), int(n.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
 
@@ -195,15 +209,7 @@ def run_ours(args, world, rank, local):
     fma = {"fp32_tflops": r.fma_benchmark(False)["tflops"], "fp64_tflops": r.fma_benchmark(True)["tflops"]} \
         if rank == 0 else None
     r.close()
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
-        n = torch.tensor([done], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(n)
-        done_all = int(n.item())
-    else:
-        done_all = done
+    dev_ms, done_all = replica_totals(dev_ms, done, world, "cuda")
     value = done_all / (dev_ms * 1e-3)
 
     # ---- end to end through the C ABI: host scene -> film on the host (scene
