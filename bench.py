@@ -341,8 +341,12 @@ PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, deriv_warps=1)
 
 
 def render_reference(sd, device, spp):
+    """The relMSE reference: a long render of the same scene with other random
+    streams, its direct-lighting pass also 64x longer than the scene's
+    (at the scene's directspp the direct pass alone keeps two renders of
+    config 4 ~0.005 apart in relMSE, whatever their chain budget)."""
     from drmlt.integrator import Renderer
-    r = Renderer(sd, device=device, seed=0xBADC0FFE, spp=spp)
+    r = Renderer(sd, device=device, seed=0xBADC0FFE, spp=spp, direct_spp=64 * max(1, sd.options.directSpp))
     r.render()
     img = r.film().astype(np.float64)
     r.close()
@@ -389,7 +393,7 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False)
             break
         step = max(8, done // 4) if e > 1.5 * target else max(8, done // 32)
     r.close()
-    return {"value": hit, "unit": "s", "target_relmse": target, "reference": "%d spp GPU render" % ref_spp,
+    return {"value": hit, "unit": "s", "target_relmse": target, "reference": "%d spp GPU render, direct pass at %d spp" % (ref_spp, 64 * max(1, sd.options.directSpp)),
             "setup_s": setup_s, "iterations": done, "spp_equivalent": done * sd.options.numChains /
             (sd.width * sd.height), "mutations_per_s": done * sd.options.numChains / max(run_s, 1e-9),
             "checkpoints": checkpoints}
