@@ -337,7 +337,7 @@ def rel_mse(img, ref):
 # The plain per-stage-launch GPU drop-in: the same kernels launched one stage
 # at a time on one stream without CUDA graphs, one chain per lane in the
 # per-chain kernels, one warp per chain's derivatives, no launch autotuning.
-PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, deriv_warps=1)
+PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, stage2_lanes=32, deriv_warps=1)
 
 
 def render_reference(sd, device, spp):

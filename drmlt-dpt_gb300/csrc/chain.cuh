@@ -94,6 +94,7 @@ struct RunParams {
     int maxDerv;
     int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch
     int lanes;           // chains per warp in the per-chain stage kernels (1..32)
+    int lanes2;          // chains per warp in the second-stage list kernels (1..32)
     const int *iterp;    // the group's current iteration (device memory)
     int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
     unsigned long long seed;

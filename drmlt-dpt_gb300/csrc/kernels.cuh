@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p) {
 __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
     const int iter = *p.iterp;
     bool on;
-    const int t = sparse_index(p.lanes, on);
+    const int t = sparse_index(p.lanes2, on);
     if (!on || t >= p.d.counters[2]) return;
     const int i = p.d.listS[t];
     Scratch &sc = p.d.scr[i];
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
 __global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p) {
     const int iter = *p.iterp;
     bool on;
-    const int t = sparse_index(p.lanes, on);
+    const int t = sparse_index(p.lanes2, on);
     if (!on || t >= p.d.counters[2]) return;
     const int i = p.d.listS[t];
     Scratch &sc = p.d.scr[i];

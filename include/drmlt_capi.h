@@ -126,6 +126,8 @@ typedef struct drmlt_options {
                                      -1 = the driver's choice per kernel */
     int32_t autotune;             /* drmlt_render picks stage_lanes / deriv_warps with drmlt_autotune
                                      (default 1; renders of fewer than 1024 iterations are not tuned) */
+    int32_t stage2_lanes;         /* chains per warp in the second-stage list kernels (stage 2 and
+                                     Green's y*), 1..32 (0 = min(stage_lanes, 4)) */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus

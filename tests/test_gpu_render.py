@@ -119,14 +119,14 @@ def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_
 
 
 def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
-    """Graph replay, chain groups, chains per warp and derivative-team size only
+    """Graph replay, chain groups, chains per warp (stage 1 and stage 2) and derivative-team size only
     change the scheduling: the chains take the same steps (integer counters identical,
     film equal up to the order of the floating-point splat additions)."""
     from drmlt import scene as dscene
     from drmlt.integrator import Renderer
     sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
     out = []
-    for kw in (dict(), dict(use_graph=0), dict(chain_groups=4, stage_lanes=4, deriv_warps=1),
+    for kw in (dict(), dict(use_graph=0), dict(chain_groups=4, stage_lanes=4, deriv_warps=1, stage2_lanes=32),
                dict(chain_groups=3, stage_lanes=32, deriv_warps=4, use_graph=0)):
         with Renderer(sd, num_chains=4096, **kw) as r:
             r.prepass()
