@@ -40,7 +40,12 @@ __device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, 
 
 // A team of p.derivWarps warps per listed chain shares its Hessian entries. The
 // grid is sized for the GPU: team t takes list entries t, t + teams, ...
-__global__ void __launch_bounds__(128) k_derivs(RunParams p, int which) {
+// Four resident blocks per SM (128 registers a thread, 16 warps) hide more of
+// the instruction-fetch and memory latency than the 254 registers the
+// compiler takes unbounded (8 warps), for 28 bytes of spills: config 2 0.843 ->
+// 0.815 ms per iteration (three blocks 0.822, five 0.825), config 4 6.09 ->
+// 5.73 ms.
+__global__ void __launch_bounds__(128, 4) k_derivs(RunParams p, int which) {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int teams = (gridDim.x * blockDim.x >> 5) / p.derivWarps;
     const int n = p.d.counters[which == 0 ? 0 : 1];
