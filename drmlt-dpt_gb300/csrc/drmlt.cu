@@ -147,6 +147,7 @@ struct Renderer {
     ~Renderer() {
         if (graph) cudaGraphExecDestroy(graph);
         if (forkEv) cudaEventDestroy(forkEv);
+        if (midEv) cudaEventDestroy(midEv);
         for (cudaStream_t s : gstreams) cudaStreamDestroy(s);
         for (cudaEvent_t e : gevents) cudaEventDestroy(e);
         for (void *p : owned) cudaFree(p);
@@ -694,6 +695,12 @@ struct Renderer {
     // carry its normalisation b.
     long long graphLaunches = 0;
     cudaEvent_t forkEv = nullptr;
+    cudaEvent_t midEv = nullptr;
+    // Iterations per graph launch (1 or 4, picked by the autotuner). The chain
+    // groups run free within a graph and join at its end: on config 4 joining
+    // them every iteration costs 3% (5.67 against 5.48 ms per iteration), on
+    // config 2 the join helps by 1% (0.815 against 0.823 ms).
+    int graphIters = 1;
     int build_graph() {
         if (!forkEv) CK(cudaEventCreateWithFlags(&forkEv, cudaEventDisableTiming));
         CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -701,7 +708,7 @@ struct Renderer {
         cudaError_t e = cudaEventRecord(forkEv, stream);
         for (int g = 0; g < G && e == cudaSuccess; g++) {
             e = cudaStreamWaitEvent(gstreams[g], forkEv, 0);
-            if (e == cudaSuccess) n += launch_iteration(g, gstreams[g]);
+            for (int k = 0; k < graphIters && e == cudaSuccess; k++) n += launch_iteration(g, gstreams[g]);
             if (e == cudaSuccess) e = cudaEventRecord(gevents[g], gstreams[g]);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, gevents[g], 0);
         }
@@ -733,15 +740,19 @@ struct Renderer {
         }
         k_set_iters<<<1, 32, 0, stream>>>(dIters, G, int(iterDone));
         CK(cudaEventRecord(ev0, stream));
+        long long it = iterDone;
         if (graph) {
-            for (long long it = iterDone; it < end; it++) {
+            for (; it + graphIters <= end; it += graphIters) {
                 CK(cudaGraphLaunch(graph, stream));
                 launches += graphLaunches;
-                mutations += (it < samplesPerChain) ? N : extraChains;
+                for (int k = 0; k < graphIters; k++) mutations += (it + k < samplesPerChain) ? N : extraChains;
             }
-        } else {
-            for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(gstreams[g], ev0, 0));
-            for (long long it = iterDone; it < end; it++) {
+        }
+        if (it < end) {  // without graphs, or the last iterations short of a graph's
+            if (!midEv) CK(cudaEventCreateWithFlags(&midEv, cudaEventDisableTiming));
+            CK(cudaEventRecord(midEv, stream));
+            for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(gstreams[g], midEv, 0));
+            for (; it < end; it++) {
                 for (int g = 0; g < G; g++) launches += launch_iteration(g, gstreams[g]);
                 mutations += (it < samplesPerChain) ? N : extraChains;
             }
@@ -764,7 +775,8 @@ struct Renderer {
     // number of chains per warp in the per-chain stage kernels, in two passes
     // of opposite order so that a drift of the iteration cost over the render
     // cancels, keeps the fastest, then does the same for the number of warps
-    // sharing one chain's derivatives. The iterations are part of the render:
+    // sharing one chain's derivatives, then (graphs on, `per` a multiple of 4)
+    // the number of iterations per graph launch. The iterations are part of the render:
     // the launch shape never changes which steps the chains take. Stops early
     // when the render runs out of iterations.
     int autotune(int per, int *lanesOut, int *warpsOut) {
@@ -816,6 +828,18 @@ struct Renderer {
             for (int i = 1; i < 3; i++)
                 if (tw[i] < tw[bi]) bi = i;
             bestW = kWarps[bi];
+        }
+        // iterations per graph launch
+        if (opt.use_graph && per % 4 == 0) {
+            static const int kIters[] = {1, 4};
+            float tg[2] = {0, 0};
+            for (int pass = 0; pass < 2 && !out; pass++)
+                for (int k = 0; k < 2 && !out; k++) {
+                    const int i = pass == 0 ? k : 1 - k;
+                    graphIters = kIters[i];
+                    if (int rc = trial(bestL, bestW, tg[i])) return rc;
+                }
+            graphIters = (!out && tg[1] < tg[0]) ? 4 : 1;
         }
         opt.stage_lanes = bestL;
         opt.deriv_warps = bestW;

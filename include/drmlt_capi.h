@@ -117,7 +117,8 @@ typedef struct drmlt_options {
     int32_t max_derivative_depth; /* --max-derivatives-depth (default 9) */
     uint64_t seed;                /* GPU random-stream key */
     int32_t device;               /* CUDA device ordinal */
-    int32_t use_graph;            /* replay each iteration as one CUDA graph (default 1) */
+    int32_t use_graph;            /* replay iterations as CUDA graphs of 1 (or, autotuned, 4)
+                                     iterations (default 1) */
     int32_t chain_groups;         /* chains are split into this many groups, each stepped on its own
                                      CUDA stream so the groups' kernels overlap (0 = default, 2) */
     int32_t stage_lanes;          /* chains per warp in the per-chain stage kernels, 1..32 (0 = 16) */
@@ -214,7 +215,9 @@ int drmlt_kernel_launches(void *handle, int64_t *n);
  * render under each candidate chains-per-warp count of the per-chain stage
  * kernels (2, 4, 8, 16, 32), in two passes of opposite order, then each
  * derivative team size (1, 2, 4 warps) the same way (CUDA events), and keeps
- * the fastest pair (written to the outputs, which may be NULL): 17 runs in all.
+ * the fastest pair (written to the outputs, which may be NULL): 17 runs. With
+ * CUDA graphs on and iterations_per_candidate a multiple of 4 it then times
+ * graphs of 1 and of 4 iterations (4 more runs) and keeps the faster.
  * The iterations count toward the render; the launch shape does not change the
  * chains' steps. */
 int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes, int *deriv_warps);
