@@ -142,7 +142,7 @@ def load_workload(name: str, tmp: str):
         return dscene.load_scene(xml), xml, WORKLOAD
     label, fn = LARGE[name]
     # enough samples per pixel that the autotuner, warm-up and timed steps fit in one render
-    return getattr(procedural, fn)(spp=64 if name == "config4" else 32), None, label
+    return getattr(procedural, fn)(spp=128 if name == "config4" else 32), None, label
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each chain-loop
@@ -286,7 +286,8 @@ def run_ours(args, world, rank, local):
         gb = (3 * SLOT_B + 3 * GAUSS_B + SCRATCH_B) * N / 1e9
         out = {
             "metric": METRIC, "value": value, "unit": "mutations/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "steps_done": round(done / N),  # fewer than steps when the render ran out of iterations
+            "warmup": args.warmup, "ms_per_step": dev_ms / max(1, round(done / N)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": label, "chains": N, "width": sd.width, "height": sd.height,
                        "max_depth": sd.options.maxDepth, "triangles": int(len(sd.positions)),
