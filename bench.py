@@ -191,6 +191,7 @@ def run_ours(args, world, rank, local):
     r.direct()
     r.prepass()
     lanes, dwarps = r.autotune(8)  # launch shape for this scene (drmlt_autotune)
+    shape = r.launch_shape()
     r.run(args.warmup)
     prof, prof_mut = r.profile(max(1, min(8, args.steps)))  # per-stage CUDA-event times (serialised)
     torch.cuda.synchronize()
@@ -292,7 +293,7 @@ def run_ours(args, world, rank, local):
             "config": {"workload": label, "chains": N, "width": sd.width, "height": sd.height,
                        "max_depth": sd.options.maxDepth, "triangles": int(len(sd.positions)),
                        "dr_type": sd.options.type, "mutations_per_step": N * world,
-                       "launch_shape": {"chains_per_warp": lanes, "derivative_warps": dwarps, "autotuned": True},
+                       "launch_shape": dict(shape, autotuned=True),
                        "l2": "chain state (3 slots + 3 FP64 Gaussians per chain, %.2f GB) exceeds L2" % gb},
             "e2e": e2e,
             "roofline": roof,

@@ -975,6 +975,17 @@ int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes,
     return static_cast<Renderer *>(handle)->autotune(iterations_per_candidate, stage_lanes, deriv_warps);
 }
 
+int drmlt_get_launch_shape(void *handle, int *stage_lanes, int *stage2_lanes, int *deriv_warps, int *graph_iters) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    const Renderer *r = static_cast<const Renderer *>(handle);
+    const RunParams p = r->params();
+    if (stage_lanes) *stage_lanes = p.lanes;
+    if (stage2_lanes) *stage2_lanes = p.lanes2;
+    if (deriv_warps) *deriv_warps = p.derivWarps;
+    if (graph_iters) *graph_iters = r->opt.use_graph ? r->graphIters : 0;
+    return DRMLT_OK;
+}
+
 int drmlt_get_film(void *handle, float *rgb) {
     if (!handle || !rgb) return fail(DRMLT_E_ARG, "null argument");
     return static_cast<Renderer *>(handle)->film(rgb);

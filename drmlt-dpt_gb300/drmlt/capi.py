@@ -104,6 +104,8 @@ _SIGS = {
     "drmlt_run": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "drmlt_render": (C.c_int, [C.c_void_p]),
     "drmlt_get_film": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "drmlt_get_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int)]),
     "drmlt_get_partial_film": (C.c_int, [C.c_void_p, C.c_void_p]),
     "drmlt_write_exr": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_void_p]),
     "drmlt_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),

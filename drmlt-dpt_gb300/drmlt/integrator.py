@@ -133,6 +133,13 @@ class Renderer:
                                                   C.byref(ms), counts.ctypes.data))
         return {"ms": ms.value, "rays": counts[0], "nodes": counts[1], "tris": counts[2]}
 
+    def launch_shape(self) -> dict:
+        """drmlt_get_launch_shape: the shape the next run uses."""
+        v = [C.c_int() for _ in range(4)]
+        capi.check(capi.lib().drmlt_get_launch_shape(self.handle, *(C.byref(x) for x in v)))
+        return dict(zip(("chains_per_warp", "stage2_chains_per_warp", "derivative_warps", "graph_iterations"),
+                        (x.value for x in v)))
+
     def fma_benchmark(self, fp64: bool = False, iterations: int | None = None) -> dict:
         """drmlt_fma_benchmark: the device's FP32 or FP64 FMA throughput."""
         ms, flops = C.c_float(), C.c_double()

@@ -222,6 +222,12 @@ int drmlt_kernel_launches(void *handle, int64_t *n);
  * chains' steps. */
 int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes, int *deriv_warps);
 
+/* The launch shape the next drmlt_run uses (after drmlt_autotune: the tuned
+ * one): chains per warp of the stage kernels and of the second-stage list
+ * kernels, warps per derivative team, iterations per CUDA graph launch (0 when
+ * graphs are off). Any output may be NULL. */
+int drmlt_get_launch_shape(void *handle, int *stage_lanes, int *stage2_lanes, int *deriv_warps, int *graph_iters);
+
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
  * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,
  * derivs(z), gauss(z), finish milliseconds. */

@@ -148,6 +148,10 @@ def test_autotuner_keeps_the_chains(built_lib, scene_root):
         a.prepass()
         lanes, warps = a.autotune(2)
         assert lanes in (2, 4, 8, 16, 32) and warps in (1, 2, 4)
+        # drmlt_get_launch_shape reports the tuned shape; 2 iterations per
+        # candidate leave the graph length at 1
+        assert a.launch_shape() == {"chains_per_warp": lanes, "stage2_chains_per_warp": min(lanes, 4),
+                                    "derivative_warps": warps, "graph_iterations": 1}
         tuned = a.stats()["mutations"] // 4096
         assert tuned == 2 * 17
         a.run(40 - tuned)
