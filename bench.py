@@ -1,25 +1,38 @@
-"""DRMLT hot-path benchmark: mutations/s of the GPU chain loop on one GB300.
+"""DRMLT hot-path benchmark: mutations/s and time to relMSE 0.01 of the GPU
+chain loop on one GB300.
 
-Workload (default): the H2MC second-stage configuration -- the Phong Cornell
-box (34 + 2 triangles) at 1024x1024, max depth 8, 16384 chains, type=mira,
-stage-2 anisotropic probability 0.5, sigma 1/64 -- written by
-drmlt/scenegen.py:config2 from a fixed seed (synthetic scene; the reference
-publishes no benchmark scene). One step = one DR iteration of every chain
-(16384 mutations). `value` is device-timed mutations/s over K steps with the
-chain state resident in HBM; `e2e` is the same metric through the public C ABI
-from host buffers (scene upload, prepass, direct pass, K steps, film readback).
+Workload (default ``config4``): the batched persistent-DRMLT configuration --
+a displaced geodesic sphere of 1,997,120 triangles (rough dielectric) over a
+Phong ground grid of 1,002,528 triangles, a constant environment map and a
+point light, 1024x1024, max depth 12, 65536 chains, type=mira, built in memory
+by drmlt/procedural.py:config4 from a fixed seed (synthetic scene: the
+reference publishes no benchmark scene). One step = one DR iteration of every
+chain (65536 mutations).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload config2|config4|config5]
+                  [--workload config4|config2|config5]
 
---workload config4 / config5 run the large procedural scenes of
-drmlt/procedural.py instead (3.0 M / 8.0 M triangles, max depth 12, 65536 /
-262144 chains; scene built in memory). Their CPU legs are not run: the
-oracle's brute-force intersector costs O(triangles) per ray.
+Keys of the JSON line (ours):
+  value            device-timed mutations/s over K graph-launched steps, chain
+                   state resident in HBM (1.06 GB, larger than L2)
+  e2e              the same metric through the C ABI as a user calls it: K
+                   steps of drmlt_run(1) each followed by a host read of the
+                   statistics, then the film read back; the one-time set-up
+                   (scene upload from host buffers, BVH build, prepass) is
+                   timed separately (setup_s) and given with it as
+                   value_with_setup
+  time_to_relmse   seconds (direct pass, prepass, autotuning, chain loop) until
+  (_plain)         relMSE <= 0.01 against a long render, for the batched form
+                   and for the plain per-stage-launch drop-in
+  roofline         the slowest chain-loop stage against the HBM peak
+  cpu_baseline     the oracle's CPU chain loop (all host cores, the oracle's
+                   own BVH) on a bounded sample of the same scene
 
-Under torchrun (N > 1) every rank renders its own shard of chains (different
-random streams) and the films are summed; chains are independent, so there is
-no collective in the timed region.
+--impl reference times that CPU chain loop alone on the same workload (the
+reference's own dpt does not build on this Arm host: Embree 2.17 and its SSE
+intrinsics are x86-only). Under torchrun (N > 1) every rank renders its own
+replica of the chains (different random streams); there is no collective in
+the timed region, and --gpus must equal the torchrun world size.
 """
 from __future__ import annotations
 
@@ -39,8 +52,9 @@ sys.path.insert(0, os.path.join(REPO, "drmlt-dpt_gb300"))
 import numpy as np  # noqa: E402
 
 PEAKS_PATH = os.path.join(REPO, "MEASURED_PEAKS.json")
-WORKLOAD = "drmlt-h2mc-phong-cornell-1024x1024-depth8-16384chains-mira"
+COUNTERS_PATH = os.path.join(REPO, "profiles", "ncu_counters.json")
 METRIC = "mutations_per_second"
+L2_BYTES = 129e6
 
 
 def _dist():
@@ -121,48 +135,64 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def write_workload(tmp: str, spp: int = 64) -> str:
-    from drmlt import scenegen
-    return scenegen.write_cornell(os.path.join(tmp, "cfg2"), seed=2, width=1024, height=1024, phong=True,
-                                  options=scenegen.SceneOptions(maxdepth=8, numchains=16384, spp=spp, type="mira"))
-
-
-LARGE = {
-    "config4": ("drmlt-h2mc-displaced-sphere-3.0Mtris-env-point-1024x1024-depth12-65536chains-mira", "config4"),
-    "config5": ("drmlt-h2mc-caustic-heightfield-8.0Mtris-2048x2048-depth12-262144chains-mira", "config5"),
+# workload -> (label, relMSE reference spp, time-to-relMSE spp budget)
+WORKLOADS = {
+    "config4": ("drmlt-h2mc-displaced-sphere-3.0Mtris-env-point-1024x1024-depth12-65536chains-mira", 512, 128),
+    "config2": ("drmlt-h2mc-phong-cornell-1024x1024-depth8-16384chains-mira", 256, 64),
+    "config5": ("drmlt-h2mc-caustic-heightfield-8.0Mtris-2048x2048-depth12-262144chains-mira", 128, 32),
 }
+DEFAULT_WORKLOAD = "config4"
 
 
 def load_workload(name: str, tmp: str):
-    """(scene data, XML path or None, workload label) of a bench workload."""
+    """(scene data, workload label) of a bench workload."""
     from drmlt import procedural
     from drmlt import scene as dscene
+    from drmlt import scenegen
+    label, _, spp = WORKLOADS[name]
     if name == "config2":
-        xml = write_workload(tmp)
-        return dscene.load_scene(xml), xml, WORKLOAD
-    label, fn = LARGE[name]
+        xml = scenegen.write_cornell(os.path.join(tmp, "cfg2"), seed=2, width=1024, height=1024, phong=True,
+                                     options=scenegen.SceneOptions(maxdepth=8, numchains=16384, spp=spp, type="mira"))
+        return dscene.load_scene(xml), label
     # enough samples per pixel that the autotuner, warm-up and timed steps fit in one render
-    return getattr(procedural, fn)(spp=128 if name == "config4" else 32), None, label
+    return getattr(procedural, name)(spp=spp), label
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each chain-loop
-# kernel per iteration (both chain groups), from `ncu --set full` captures of
-# the same kernels on these workloads; None where not captured.
-NCU_TRAFFIC = {
-    "config2": {"stage1": 2 * 3.47e6, "derivs_x": 2 * 0.63e6, "gauss_x": 2 * 0.82e6, "stage2": 2 * 2.00e6,
-                "derivs_z": 2 * 0.67e6, "gauss_z": 2 * 2.29e6, "finish": 2 * 5.34e6},
-    "config4": {"stage1": 2 * 145.7e6},
-}
+def workload_config(sd, label: str) -> dict:
+    """The `config` object both arms print for one workload."""
+    return {"workload": label, "chains": int(sd.options.numChains), "width": int(sd.width), "height": int(sd.height),
+            "max_depth": int(sd.options.maxDepth), "triangles": int(len(sd.positions)), "dr_type": sd.options.type}
 
-# Floating-point operations (FP32, FP64) of the derivative and Gaussian
-# kernels per chain-loop iteration (both chain groups): ncu's executed-op
-# counters (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on.sum and
-# the d-variants, an FMA counted as 2) summed over the bench's own launches of
-# these kernels after the autotuner; None where not captured.
-NCU_FLOPS = {
-    "config2": {"derivs_x": (7.256e8, 0.0), "derivs_z": (7.500e8, 0.0),
-                "gauss_x": (9.821e7, 2.690e7), "gauss_z": (1.059e8, 4.613e7)},
-}
+
+def source_hash() -> str:
+    """Hash of the CUDA/C++ sources and the ABI header: profiler counters are
+    valid only for the build they were captured on."""
+    import hashlib
+    h = hashlib.sha256()
+    csrc = os.path.join(REPO, "drmlt-dpt_gb300", "csrc")
+    for f in sorted(os.listdir(csrc)) + ["../../include/drmlt_capi.h"]:
+        with open(os.path.join(csrc, f), "rb") as fh:
+            h.update(f.encode() + b"\0" + fh.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_counters(workload: str):
+    """DRAM bytes and FP32/FP64 flops per iteration of the chain-loop kernels
+    from ncu captures (profiles/ncu_counters.json), when they were captured on
+    this build's sources; else (None, reason)."""
+    try:
+        with open(COUNTERS_PATH) as f:
+            c = json.load(f)
+    except Exception as e:  # noqa: BLE001
+        return None, "no counters file (%s)" % type(e).__name__
+    mine = source_hash()
+    if c.get("source_hash") != mine:
+        return None, "captured on sources %s, this build is %s" % (c.get("source_hash"), mine)
+    w = c.get("workloads", {}).get(workload)
+    if w is None:
+        return None, "no capture for %s" % workload
+    return w, c.get("command")
+
 
 # Algorithmic bytes each stage moves per chain (read + write of chain state in
 # HBM). A Slot is 328 B, the per-chain scratch 128 B (both asserted in
@@ -174,7 +204,6 @@ GAUSS_B = 8 * (24 * 24 + 2 * 24 + 2)
 
 def run_ours(args, world, rank, local):
     import torch
-    from drmlt import scene as dscene
     from drmlt.integrator import Renderer
 
     torch.cuda.set_device(local)
@@ -182,7 +211,7 @@ def run_ours(args, world, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     tmp = tempfile.mkdtemp()
-    sd, xml, label = load_workload(args.workload, tmp)
+    sd, label = load_workload(args.workload, tmp)
     N = sd.options.numChains
     seed = 0x1234ABCD + 7919 * rank
 
@@ -190,7 +219,7 @@ def run_ours(args, world, rank, local):
     r = Renderer(sd, device=local, seed=seed)
     r.direct()
     r.prepass()
-    lanes, dwarps = r.autotune(8)  # launch shape for this scene (drmlt_autotune)
+    r.autotune(8)  # launch shape for this scene (drmlt_autotune)
     shape = r.launch_shape()
     r.run(args.warmup)
     prof, prof_mut = r.profile(max(1, min(8, args.steps)))  # per-stage CUDA-event times (serialised)
@@ -206,33 +235,45 @@ def run_ours(args, world, rank, local):
     dev_ms = r.last_run_ms()
     torch.cuda.synchronize()
     stats = r.stats()
-    rays = ray_roofline(r, _peaks()[0]) if rank == 0 else None
+    rays = ray_roofline(r, _peaks()[0], len(sd.positions)) if rank == 0 else None
     fma = {"fp32_tflops": r.fma_benchmark(False)["tflops"], "fp64_tflops": r.fma_benchmark(True)["tflops"]} \
         if rank == 0 else None
     r.close()
     dev_ms, done_all = replica_totals(dev_ms, done, world, "cuda")
     value = done_all / (dev_ms * 1e-3)
 
-    # ---- end to end through the C ABI: host scene -> film on the host (scene
-    # upload, bootstrap prepass, K steps, film readback; the direct-lighting pass
-    # is not part of the mutation metric and is left out on both arms)
+    # ---- end to end through the C ABI with host buffers, at the tuned launch
+    # shape (no autotuning here): set-up = drmlt_create from the host scene
+    # (upload + BVH build) and drmlt_prepass; then K x (drmlt_run(1) + a host
+    # read of the statistics) and the film read back at the end
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    r2 = Renderer(sd, device=local, seed=seed + 1)
+    r2 = Renderer(sd, device=local, seed=seed + 1, autotune=0, stage_lanes=shape["chains_per_warp"],
+                  stage2_lanes=shape["stage2_chains_per_warp"], deriv_warps=shape["derivative_warps"],
+                  use_graph=1 if shape["graph_iterations"] else 0, graph_iters=max(1, shape["graph_iterations"]))
     r2.prepass()
-    r2.autotune(8)
-    r2.run(args.steps)
+    t1 = time.perf_counter()
+    e_done = 0
+    for _ in range(args.steps):
+        e_done += r2.run(1)
+        r2.stats()
     film = r2.film()
-    e2e_s = time.perf_counter() - t0
-    e_done = r2.stats()["mutations"]  # the autotuner's iterations included
+    t2 = time.perf_counter()
     r2.close()
-    scene_bytes = sd.positions.nbytes + sd.normals.nbytes + 64 * 4
-    e2e = {"value": e_done / e2e_s * world, "unit": "mutations/s", "h2d_bytes_per_step": scene_bytes // args.steps,
-           "d2h_bytes_per_step": film.nbytes // args.steps}
+    stats_bytes = 11 * 8
+    scene_bytes = sd.positions.nbytes + sd.normals.nbytes
+    e2e = {"value": e_done / (t2 - t1) * world, "unit": "mutations/s", "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": stats_bytes + film.nbytes // max(1, args.steps),
+           "steps": args.steps, "mutations": e_done, "steps_s": t2 - t1, "setup_s": t1 - t0,
+           "setup_h2d_bytes": scene_bytes,
+           "value_with_setup": e_done / (t2 - t0) * world,
+           "timed": "drmlt_run(1) + drmlt_get_stats per step, drmlt_get_film at the end; set-up (drmlt_create "
+                    "from host buffers incl. BVH build, drmlt_prepass) in setup_s"}
 
     # ---- roofline of the dominant stage kernel
     hbm, peak_kind = _peaks()
+    counters, counters_src = ncu_counters(args.workload)
     stage_bytes = {
         "stage1": N * (2 * SLOT_B + SCRATCH_B),
         "stage2": N * (2 * SLOT_B + SCRATCH_B),
@@ -250,21 +291,23 @@ def run_ours(args, world, rank, local):
         listed = max(1, stats["stage2_h2mc"] // max(1, stats["mutations"] // N)) if stats["mutations"] else 1
         stage_bytes[dom] = listed * (4 * (24 + 576) + GAUSS_B)
     achieved = stage_bytes[dom] / (per_launch_ms * 1e-3) / 1e9
+    traffic = counters.get("traffic", {}).get(dom) if counters else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": NCU_TRAFFIC.get(args.workload, {}).get(dom), "peak_kind": peak_kind,
+            "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+            "traffic_source": counters_src, "algorithmic_bytes_per_iteration": stage_bytes[dom],
             "stage_ms_per_iteration": {k: v / iters for k, v in prof.items()}}
 
     # ---- compute rooflines: derivative kernel on the FP32 FMA roof, Gaussian
     # kernel on the FP64 roof, both against this device's measured FMA peaks
     compute = None
     if fma is not None:
-        compute = {"peaks_measured": fma}
+        compute = {"peaks_measured": fma, "flops_source": counters_src}
         for st in ("derivs_x", "derivs_z", "gauss_x", "gauss_z"):
             ms = prof[st] / iters
             ent = {"ms_per_iteration": ms}
-            counts = NCU_FLOPS.get(args.workload, {}).get(st)
-            if counts is not None:
-                for kind, n, peak in (("fp32", counts[0], fma["fp32_tflops"]), ("fp64", counts[1], fma["fp64_tflops"])):
+            fl = counters.get("flops", {}).get(st) if counters else None
+            if fl is not None:
+                for kind, n, peak in (("fp32", fl[0], fma["fp32_tflops"]), ("fp64", fl[1], fma["fp64_tflops"])):
                     a = n / (ms * 1e-3) / 1e12
                     ent[kind] = {"flops_per_iteration": n, "achieved": a, "peak": peak, "unit": "TFLOP/s",
                                  "frac": a / peak}
@@ -274,27 +317,25 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         relmse = relmse_plain = None
         if not args.no_relmse:
-            ref_spp = args.ref_spp
+            _, ref_spp, budget = WORKLOADS[args.workload]
+            ref_spp = args.ref_spp or ref_spp
             ref = render_reference(sd, local, ref_spp)
-            spp = args.relmse_spp or (64 if args.workload == "config2" else 128)
+            spp = args.relmse_spp or budget
             relmse = time_to_relmse(sd, local, ref, ref_spp, spp=spp)
             relmse_plain = time_to_relmse(sd, local, ref, ref_spp, spp=spp, plain=True)
-        if xml is None:
-            cpu = {"value": None, "unit": "mutations/s", "cores": 0, "kind": "port",
-                   "sample": "not run: the oracle's brute-force intersector costs O(triangles) per ray"}
-        else:
-            cpu = cpu_baseline_sample(xml) if not args.no_cpu else None
+        cpu = None if args.no_cpu else cpu_baseline_sample(sd, seconds=15.0)
         gb = (3 * SLOT_B + 3 * GAUSS_B + SCRATCH_B) * N / 1e9
         out = {
             "metric": METRIC, "value": value, "unit": "mutations/s", "n_gpus": world, "steps": args.steps,
             "steps_done": round(done / N),  # fewer than steps when the render ran out of iterations
             "warmup": args.warmup, "ms_per_step": dev_ms / max(1, round(done / N)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": label, "chains": N, "width": sd.width, "height": sd.height,
-                       "max_depth": sd.options.maxDepth, "triangles": int(len(sd.positions)),
-                       "dr_type": sd.options.type, "mutations_per_step": N * world,
-                       "launch_shape": dict(shape, autotuned=True),
-                       "l2": "chain state (3 slots + 3 FP64 Gaussians per chain, %.2f GB) exceeds L2" % gb},
+            "config": workload_config(sd, label),
+            "mutations_per_step": N * world,
+            "launch_shape": dict(shape, autotuned=True),
+            "l2": "inputs larger than L2: chain state (3 slots + 3 FP64 Gaussians per chain, %.2f GB)%s" % (
+                gb, ", BVH + triangles (%.0f MB)" % (len(sd.positions) * 124 / 1e6)
+                if len(sd.positions) * 124 > L2_BYTES else ""),
             "e2e": e2e,
             "roofline": roof,
             "compute_roofline": compute,
@@ -314,20 +355,25 @@ def run_ours(args, world, rank, local):
     return out
 
 
-def ray_roofline(r, hbm_gbs, n_rays=1 << 21, repeats=10):
+def ray_roofline(r, hbm_gbs, n_tris, n_rays=1 << 21, repeats=10):
     """Rays/s of the BVH traversal kernel alone on the workload's scene
-    (drmlt_ray_benchmark) and the bytes it visits: nodes fetched x 64 B +
-    triangles tested x 48 B per pass over the kernel's event-timed duration,
-    against the HBM peak (the upper levels of the tree sit in L2, so the
-    fraction can exceed what DRAM alone delivers)."""
+    (drmlt_ray_benchmark) and the bytes it visits (nodes fetched x 64 B +
+    triangles tested x 48 B per pass over the kernel's event-timed duration).
+    The bytes are quoted against the HBM peak only when the scene's BVH and
+    triangles exceed L2; a smaller scene is cache-resident and its figure is
+    given without an HBM fraction."""
     out = {}
+    scene_bytes = n_tris * (48 + 36 + 36 + 4) + 32 * n_tris  # triangle records + ~n/2 64-byte nodes
+    hbm_bound = scene_bytes > L2_BYTES
     for kind in r.RAY_KINDS:
         b = r.ray_benchmark(kind, n_rays, repeats)
         sec = b["ms"] * 1e-3
         gbs = (64.0 * b["nodes"] + 48.0 * b["tris"]) / sec / 1e9
         out[kind] = {"rays_per_s": b["rays"] / sec, "ms_per_pass": b["ms"], "rays": int(b["rays"]),
                      "nodes_per_ray": b["nodes"] / max(b["rays"], 1), "tris_per_ray": b["tris"] / max(b["rays"], 1),
-                     "visited_gbs": gbs, "frac_of_hbm": gbs / hbm_gbs}
+                     "visited_gbs": gbs, "frac_of_hbm": gbs / hbm_gbs if hbm_bound else None}
+    out["scene_bytes"] = scene_bytes
+    out["residency"] = "HBM (scene larger than L2)" if hbm_bound else "L1/L2 (scene smaller than L2: no HBM fraction)"
     return out
 
 
@@ -401,56 +447,66 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False)
             "checkpoints": checkpoints}
 
 
-def cpu_baseline_sample(xml: str, seconds: float = 15.0):
-    """The oracle's CPU restatement of the chain loop on this host's cores, on a
-    bounded sample of the same workload."""
+def cpu_baseline_sample(sd, seconds: float = 15.0):
+    """The oracle's CPU restatement of the chain loop (its own BVH) on this
+    host's cores, on a bounded sample of the same workload."""
     try:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle_dr  # noqa: WPS433
     except Exception as e:  # oracle not built on this machine
         return {"value": None, "unit": "mutations/s", "cores": 0, "kind": "port", "sample": "unavailable: %s" % e}
-    return oracle_dr.cpu_throughput(xml, seconds=seconds)
+    return oracle_dr.cpu_throughput_scene(sd, seconds=seconds)
 
 
 def run_reference(args, world, rank):
-    """Reference arm: the reference's CPU algorithm (oracle restatement, all host
-    cores) on the same workload, metric and unit."""
+    """Reference arm: the reference's CPU algorithm (the oracle's restatement of
+    the chain loop, all host cores, the oracle's own BVH) on the same workload,
+    metric and unit. Each step is a bounded sample of the chain loop; the scene
+    set-up and bootstrap prepass are outside the samples."""
     if rank != 0:
         return None
     tmp = tempfile.mkdtemp()
-    xml = write_workload(tmp)
+    sd, label = load_workload(args.workload, tmp)
     try:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle_dr
     except Exception as e:
         return {"impl": "reference", "unavailable": "oracle CPU port not built: %s" % e}
-    per = min(15.0, max(0.25, 90.0 / max(1, args.steps + args.warmup)))
+    loop = oracle_dr.CpuChainLoop(sd)
+    per = min(15.0, max(0.5, 60.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
-        oracle_dr.cpu_throughput(xml, seconds=per)
-    vals = [oracle_dr.cpu_throughput(xml, seconds=per) for _ in range(args.steps)]
+        loop.sample(per)
+    vals = [loop.sample(per) for _ in range(args.steps)]
+    loop.close()
     v = statistics.median([x["value"] for x in vals])
     cpu = dict(vals[0])
     cpu["value"] = v
+    cpu["sample"] = "median of %d samples of %.1f s: %s" % (len(vals), per, vals[0]["sample"])
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "mutations/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD}, "cpu_baseline": cpu,
+            "config": workload_config(sd, label), "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": "mutations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE measurement")
-    ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"])
-    ap.add_argument("--ref-spp", type=int, default=256, help="samples per pixel of the relMSE reference render")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--ref-spp", type=int, default=0, help="samples per pixel of the relMSE reference render")
     ap.add_argument("--relmse-spp", type=int, default=0, help="spp budget of the time-to-relMSE renders")
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.gpus != world:
+        sys.exit("bench.py: --gpus %d but the torchrun world size is %d (launch N > 1 under torchrun)"
+                 % (args.gpus, world))
+    if args.warmup < 3:
+        sys.exit("bench.py: at least 3 warm-up steps")
     if args.impl == "reference":
         out = run_reference(args, world, rank)
     else:

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -453,6 +454,7 @@ struct Renderer {
         if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listS, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listA, size_t(N)))) return rc;
+        graphIters = opt.graph_iters > 0 ? std::min(opt.graph_iters, 8) : 1;
         G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 2;
         G = std::min(G, N);
         chunk = (N + G - 1) / G;
@@ -696,7 +698,8 @@ struct Renderer {
     long long graphLaunches = 0;
     cudaEvent_t forkEv = nullptr;
     cudaEvent_t midEv = nullptr;
-    // Iterations per graph launch (1 or 4, picked by the autotuner). The chain
+    // Iterations per graph launch (drmlt_options.graph_iters, or 1 or 4 picked
+    // by the autotuner). The chain
     // groups run free within a graph and join at its end: on config 4 joining
     // them every iteration costs 3% (5.67 against 5.48 ms per iteration), on
     // config 2 the join helps by 1% (0.815 against 0.823 ms).
@@ -916,6 +919,8 @@ void drmlt_default_options(drmlt_options *o) {
     o->deriv_warps = 0;
     o->autotune = 1;
     o->smem_carveout = -1;
+    o->stage2_lanes = 0;
+    o->graph_iters = 0;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }
@@ -1065,8 +1070,11 @@ __device__ __align__(256) double g_noallocGaussStore[size_t(kNoAllocMaxGaussians
 
 // Device address of g_noallocGaussStore, looked up once per device. In host
 // code the symbol name is only a host-side stand-in, never a device address.
+// The lookup is guarded by a mutex, so host threads whose first calls on a
+// device overlap do not race on it.
 constexpr int kNoAllocMaxDevices = 64;
 double *g_noallocStorePtr[kNoAllocMaxDevices] = {nullptr};
+std::mutex g_noallocSetupMutex;
 }  // namespace
 
 extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const float *ss, const float *grad,
@@ -1084,13 +1092,18 @@ extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const 
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(DRMLT_E_ARG, "device ordinal out of range");
-    if (g_noallocStorePtr[dev] == nullptr) {
-        // set-up on this device's first call (the device is current here)
-        int rc = gauss_kernels_setup();
-        if (rc) return rc;
-        double *p = nullptr;
-        CK(cudaGetSymbolAddress((void **)&p, g_noallocGaussStore));
-        g_noallocStorePtr[dev] = p;
+    double *store = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noallocSetupMutex);
+        if (g_noallocStorePtr[dev] == nullptr) {
+            // set-up on this device's first call (the device is current here)
+            int rc = gauss_kernels_setup();
+            if (rc) return rc;
+            double *p = nullptr;
+            CK(cudaGetSymbolAddress((void **)&p, g_noallocGaussStore));
+            g_noallocStorePtr[dev] = p;
+        }
+        store = g_noallocStorePtr[dev];
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // entries past each Gaussian's dimension are zero, as in drmlt_compute_gaussian
@@ -1100,7 +1113,7 @@ extern "C" int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const 
     // dims are device data here: scratch is sized for kMaxDim, and an odd or
     // out-of-range dimension yields zero outputs and a NaN log-determinant
     k_gauss_batch<<<n, 32 * kGaussTeamWarps, gauss_smem_bytes(kMaxDim), st>>>(
-        dims, ss, grad, hess, n, sigma, kMaxDim, g_noallocStorePtr[dev], mean, inv_cov, cov, log_det);
+        dims, ss, grad, hess, n, sigma, kMaxDim, store, mean, inv_cov, cov, log_det);
     CK(cudaGetLastError());
     return DRMLT_OK;
 }

@@ -61,7 +61,8 @@ class Options(C.Structure):
                 ("use_light_coordinate_sampling", C.c_int32), ("max_derivative_depth", C.c_int32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("use_graph", C.c_int32),
                 ("chain_groups", C.c_int32), ("stage_lanes", C.c_int32), ("deriv_warps", C.c_int32),
-                ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32)]
+                ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32),
+                ("graph_iters", C.c_int32)]
 
 
 class Stats(C.Structure):

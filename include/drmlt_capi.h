@@ -99,7 +99,10 @@ typedef struct drmlt_options {
     int32_t integrator;          /* DRMLT_INTEGRATOR_* */
     int32_t dr_type;             /* DRMLT_DR_GREEN | DRMLT_DR_MIRA */
     float aniso_perturb_prob;    /* anisoperturbprob */
-    float aniso_perturb_stddev;  /* second-stage isotropic sigma (reference keeps 0.0025, see DESIGN) */
+    float aniso_perturb_stddev;  /* second-stage isotropic sigma. The reference parses the XML
+                                     anisoperturbstddev into lensPerturbStdDev instead
+                                     (src/parsescene.cpp:553-554), so its sigma stays at the
+                                     0.0025 default; this value is honoured as given. */
     int32_t acceptance_map;
     float perturb_stddev;
     float large_step_prob;
@@ -129,6 +132,9 @@ typedef struct drmlt_options {
                                      (default 1; renders of fewer than 1024 iterations are not tuned) */
     int32_t stage2_lanes;         /* chains per warp in the second-stage list kernels (stage 2 and
                                      Green's y*), 1..32 (0 = min(stage_lanes, 4)) */
+    int32_t graph_iters;          /* iterations per CUDA graph launch, 1..8 (0 = 1; drmlt_autotune may
+                                     switch between 1 and 4). Iterations short of a whole graph at
+                                     the end of a run are launched without the graph. */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
@@ -309,8 +315,11 @@ int drmlt_compute_gaussian(void *handle, const int32_t *dims, const float *ss, c
  * Scratch lives in a fixed library-owned device array sized for 256 Gaussians
  * (about 1.3 MB, held on every device that loads the library until the process
  * exits); n > 256 is rejected with DRMLT_E_ARG. The first call on each device
- * looks the array's device address up (cudaGetSymbolAddress), so make that
- * first call before any stream capture. Every call shares the one array:
+ * looks the array's device address up (cudaGetSymbolAddress, once per device
+ * under a lock, so first calls from several host threads are safe), so make
+ * that first call before any stream capture. An odd, non-positive or too
+ * large dims[i] gives zero mean / inv_cov / cov rows and a NaN log_det[i].
+ * Every call shares the one array:
  * calls that overlap on the GPU (on different streams, or from different host
  * threads) race on it and must be serialised by the caller. */
 int drmlt_compute_gaussian_noalloc(int n, const int32_t *dims, const float *ss, const float *grad,

@@ -78,8 +78,18 @@ struct Light {
     float w, invArea;
     std::vector<float> triCdf;
 };
+// Bounding-volume hierarchy of the oracle's casts (built in ora_create, see cast_bvh).
+struct BvhNodeO {
+    float lo[3], hi[3];
+    int first, count;  // count > 0: leaf over idx[first, first + count); else children first, first + 1
+};
+struct BvhO {
+    std::vector<BvhNodeO> nodes;
+    std::vector<int> idx;
+};
 struct Scene {
     int ntri;
+    BvhO bvh;  // empty below kBvhMinTris triangles
     std::vector<V3> p0, e1, e2, n0, n1, n2;
     std::vector<int> triShape;
     std::vector<int> shapeBsdf, shapeLight, shapeFirst;
@@ -112,22 +122,30 @@ static int sample_discrete(const std::vector<float> &cdf, float u) {
 }
 
 // ---------------------------------------------------------------- ray casting
-// Closest hit over all triangles (float Moller-Trumbore, edges inclusive).
-static int cast(const Scene &s, V3 o, V3 d, float tmin, float tmax, bool anyHit) {
+// Float Moller-Trumbore (edges inclusive) of ray (o, d) against triangle t:
+// the hit distance, or NaN for a miss.
+static inline float tri_hit(const Scene &s, int t, V3 o, V3 d) {
+    const V3 pv = cross(d, s.e2[t]);
+    const float det = dot(s.e1[t], pv);
+    if (det == 0.0f) return NAN;
+    const float inv = 1.0f / det;
+    const V3 sv = sub(o, s.p0[t]);
+    const float u = dot(sv, pv) * inv;
+    if (!(u >= 0.0f && u <= 1.0f)) return NAN;
+    const V3 q = cross(sv, s.e1[t]);
+    const float v = dot(d, q) * inv;
+    if (!(v >= 0.0f && u + v <= 1.0f)) return NAN;
+    return dot(s.e2[t], q) * inv;
+}
+
+// Closest hit over all triangles in index order: the nearest t in (tmin, tmax]
+// and, among equal distances, the highest index (a later triangle at the same t
+// replaces the earlier one). anyHit: the lowest-index triangle in range.
+static int cast_brute(const Scene &s, V3 o, V3 d, float tmin, float tmax, bool anyHit) {
     int best = -1;
     float tb = tmax;
     for (int t = 0; t < s.ntri; t++) {
-        const V3 pv = cross(d, s.e2[t]);
-        const float det = dot(s.e1[t], pv);
-        if (det == 0.0f) continue;
-        const float inv = 1.0f / det;
-        const V3 sv = sub(o, s.p0[t]);
-        const float u = dot(sv, pv) * inv;
-        if (!(u >= 0.0f && u <= 1.0f)) continue;
-        const V3 q = cross(sv, s.e1[t]);
-        const float v = dot(d, q) * inv;
-        if (!(v >= 0.0f && u + v <= 1.0f)) continue;
-        const float th = dot(s.e2[t], q) * inv;
+        const float th = tri_hit(s, t, o, d);
         if (th > tmin && th <= tb && std::isfinite(th)) {
             best = t;
             tb = th;
@@ -135,6 +153,152 @@ static int cast(const Scene &s, V3 o, V3 d, float tmin, float tmax, bool anyHit)
         }
     }
     return best;
+}
+
+// Bounding-volume hierarchy for the multi-million-triangle scenes, so that the
+// oracle's casts stay O(log n). It is built independently of the GPU library's
+// binned-SAH tree: object-median splits along the longest centroid axis, leaves
+// of up to 4 triangles. Culling is conservative (boxes padded outward, the
+// distance window widened), and the hit rule is cast_brute's (nearest t, the
+// highest index on a tie), so a closest-hit cast returns the same triangle as
+// the brute-force loop over every triangle; an any-hit cast returns some hit in
+// range (the same occlusion answer, not necessarily the same triangle).
+static const int kBvhMinTris = 1024;  // below this the brute-force loop is used
+
+static void bvh_build(const Scene &s, BvhO &b) {
+    const int n = s.ntri;
+    b.idx.resize(n);
+    std::vector<float> cen(3 * size_t(n)), lo(3 * size_t(n)), hi(3 * size_t(n));
+    for (int t = 0; t < n; t++) {
+        b.idx[t] = t;
+        const V3 p[3] = {s.p0[t], add(s.p0[t], s.e1[t]), add(s.p0[t], s.e2[t])};
+        for (int a = 0; a < 3; a++) {
+            const float v0 = a == 0 ? p[0].x : a == 1 ? p[0].y : p[0].z;
+            const float v1 = a == 0 ? p[1].x : a == 1 ? p[1].y : p[1].z;
+            const float v2 = a == 0 ? p[2].x : a == 1 ? p[2].y : p[2].z;
+            const float l = std::min(v0, std::min(v1, v2)), h = std::max(v0, std::max(v1, v2));
+            // outward padding: relative to the coordinates' magnitude, so that a
+            // hit point computed in float from (p0, e1, e2) stays inside
+            const float pad = 1e-4f * std::max(std::fabs(l), std::fabs(h)) + 1e-6f;
+            lo[3 * size_t(t) + a] = l - pad;
+            hi[3 * size_t(t) + a] = h + pad;
+            cen[3 * size_t(t) + a] = 0.5f * (l + h);
+        }
+    }
+    b.nodes.clear();
+    b.nodes.reserve(2 * size_t(n / 2 + 1));
+    struct Job { int node, begin, end; };
+    std::vector<Job> stack;
+    b.nodes.push_back(BvhNodeO());
+    stack.push_back({0, 0, n});
+    while (!stack.empty()) {
+        const Job j = stack.back();
+        stack.pop_back();
+        float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int i = j.begin; i < j.end; i++) {
+            const size_t t = size_t(b.idx[i]);
+            for (int a = 0; a < 3; a++) {
+                blo[a] = std::min(blo[a], lo[3 * t + a]);
+                bhi[a] = std::max(bhi[a], hi[3 * t + a]);
+                clo[a] = std::min(clo[a], cen[3 * t + a]);
+                chi[a] = std::max(chi[a], cen[3 * t + a]);
+            }
+        }
+        BvhNodeO &nd = b.nodes[j.node];
+        for (int a = 0; a < 3; a++) {
+            nd.lo[a] = blo[a];
+            nd.hi[a] = bhi[a];
+        }
+        const int cnt = j.end - j.begin;
+        int axis = 0;
+        for (int a = 1; a < 3; a++)
+            if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+        if (cnt <= 4 || !(chi[axis] > clo[axis])) {
+            nd.first = j.begin;
+            nd.count = cnt;
+            continue;
+        }
+        const int mid = j.begin + cnt / 2;
+        std::nth_element(b.idx.begin() + j.begin, b.idx.begin() + mid, b.idx.begin() + j.end, [&](int x, int y) {
+            const float cx = cen[3 * size_t(x) + axis], cy = cen[3 * size_t(y) + axis];
+            return cx < cy || (cx == cy && x < y);
+        });
+        const int left = int(b.nodes.size());
+        b.nodes[j.node].first = left;
+        b.nodes[j.node].count = 0;
+        b.nodes.push_back(BvhNodeO());
+        b.nodes.push_back(BvhNodeO());
+        stack.push_back({left, j.begin, mid});
+        stack.push_back({left + 1, mid, j.end});
+    }
+}
+
+// Ray-box overlap on [t0, t1]; NaN slab values (a zero direction component on
+// a box face) leave the window unchanged, which only keeps more boxes.
+static inline bool box_overlap(const BvhNodeO &n, const float o[3], const float inv[3], float t0, float t1,
+                               float &tenter) {
+    for (int a = 0; a < 3; a++) {
+        float tn = (n.lo[a] - o[a]) * inv[a], tf = (n.hi[a] - o[a]) * inv[a];
+        if (tn > tf) std::swap(tn, tf);
+        t0 = std::max(t0, tn);
+        t1 = std::min(t1, tf);
+    }
+    tenter = t0;
+    return t0 <= t1;
+}
+
+static int cast_bvh(const Scene &s, V3 o, V3 d, float tmin, float tmax, bool anyHit) {
+    const BvhO &b = s.bvh;
+    const float of[3] = {o.x, o.y, o.z};
+    const float inv[3] = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    int best = -1;
+    float tb = tmax;
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    const float lowT = tmin - 1e-3f - 1e-4f * std::fabs(tmin);
+    while (sp > 0) {
+        const BvhNodeO &n = b.nodes[stack[--sp]];
+        // a triangle at exactly tb can still replace the best hit (tie rule)
+        const float highT = std::isfinite(tb) ? tb + 1e-4f * std::fabs(tb) + 1e-5f : tb;
+        float te;
+        if (!box_overlap(n, of, inv, lowT, highT, te)) continue;
+        if (n.count > 0) {
+            for (int i = n.first; i < n.first + n.count; i++) {
+                const int t = b.idx[i];
+                const float th = tri_hit(s, t, o, d);
+                if (th > tmin && std::isfinite(th) && (th < tb || (th == tb && t > best))) {
+                    best = t;
+                    tb = th;
+                    if (anyHit) return t;
+                }
+            }
+            continue;
+        }
+        float e0, e1;
+        const bool h0 = box_overlap(b.nodes[n.first], of, inv, lowT, highT, e0);
+        const bool h1 = box_overlap(b.nodes[n.first + 1], of, inv, lowT, highT, e1);
+        if (h0 && h1) {
+            // nearer child on top of the stack
+            if (e0 <= e1) {
+                stack[sp++] = n.first + 1;
+                stack[sp++] = n.first;
+            } else {
+                stack[sp++] = n.first;
+                stack[sp++] = n.first + 1;
+            }
+        } else if (h0) {
+            stack[sp++] = n.first;
+        } else if (h1) {
+            stack[sp++] = n.first + 1;
+        }
+    }
+    return best;
+}
+
+static int cast(const Scene &s, V3 o, V3 d, float tmin, float tmax, bool anyHit) {
+    return s.ntri >= kBvhMinTris ? cast_bvh(s, o, d, tmin, tmax, anyHit) : cast_brute(s, o, d, tmin, tmax, anyHit);
 }
 struct Isect {
     V3 p, ns, ng;

@@ -40,6 +40,7 @@ def lib():
         l.ora_tape_derivs.argtypes = [V, V, V, C.c_int, V, V]
         l.ora_compute_gaussian.argtypes = [V, V, V, V, C.c_int, C.c_float, V, V, V, V]
         l.ora_trace_rays.argtypes = [V, V, V, C.c_float, C.c_float, C.c_int, C.c_int, V, V]
+        l.ora_trace_rays_ex.argtypes = [V, V, V, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, V, V]
         l.ora_dr_run.restype = C.c_longlong
         l.ora_dr_run.argtypes = [V, C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_int, C.c_uint64, V, V, V, V]
         _lib = l
@@ -164,13 +165,16 @@ class Oracle:
                                    _p(ic), _p(cv), _p(ld))
         return mean, ic, cv, ld
 
-    def trace_rays(self, org, dirs, tmin=1e-3, tmax=float("inf"), any_hit=False):
+    def trace_rays(self, org, dirs, tmin=1e-3, tmax=float("inf"), any_hit=False, mode="auto"):
+        """Closest-hit (or any-hit) casts; mode "auto" (brute force below 1024
+        triangles, the oracle's BVH above), "brute" or "bvh"."""
         org = np.ascontiguousarray(org, np.float32).reshape(-1, 3)
         dirs = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
         n = len(org)
         tri = np.zeros(n, np.int32)
         t = np.zeros(n, np.float32)
-        lib().ora_trace_rays(self.h, _p(org), _p(dirs), tmin, tmax, n, int(any_hit), _p(tri), _p(t))
+        m = {"auto": 0, "brute": 1, "bvh": 2}[mode]
+        lib().ora_trace_rays_ex(self.h, _p(org), _p(dirs), tmin, tmax, n, int(any_hit), m, _p(tri), _p(t))
         return tri, t
 
     def dr_run(self, num_chains, iterations, seconds=0.0, threads=None, num_init=None, seed=0x1234):
@@ -186,15 +190,40 @@ class Oracle:
         return {"mutations": int(n), "seconds": el.value, "film": film, "stats": stats, "b": b.value}
 
 
-def cpu_throughput(xml: str, seconds: float = 15.0, threads: int | None = None, chains: int | None = None):
+class CpuChainLoop:
+    """The oracle's DR chain loop on this host's threads over one scene, kept
+    open so that several bounded samples share one scene set-up (and, on large
+    scenes, one BVH build)."""
+
+    def __init__(self, sd, threads: int | None = None, chains: int | None = None, num_init: int = 20000):
+        self.threads = threads or os.cpu_count() or 1
+        self.chains = chains or min(sd.options.numChains, 64 * self.threads)
+        self.num_init = num_init
+        self.oracle = Oracle(sd)
+        self.seed = 0x1234
+
+    def sample(self, seconds: float):
+        self.seed += 1
+        r = self.oracle.dr_run(self.chains, iterations=1 << 40, seconds=seconds, threads=self.threads,
+                               num_init=self.num_init, seed=self.seed)
+        return {"value": r["mutations"] / r["seconds"], "unit": "mutations/s", "cores": self.threads, "kind": "port",
+                "sample": "%d chains, %.1f s of the chain loop (prepass of %d bootstrap paths excluded), %d mutations"
+                          % (self.chains, r["seconds"], self.num_init, r["mutations"])}
+
+    def close(self):
+        self.oracle.close()
+
+
+def cpu_throughput_scene(sd, seconds: float = 15.0, threads: int | None = None, chains: int | None = None):
     """Mutations/s of the oracle's DR chain loop on this host: a bounded sample of
     the workload (its scene, options and derivative path), prepass excluded."""
-    sd = dscene.load_scene(xml)
-    threads = threads or os.cpu_count() or 1
-    o = Oracle(sd)
-    chains = chains or min(sd.options.numChains, 64 * threads)
-    r = o.dr_run(chains, iterations=1 << 40, seconds=seconds, threads=threads, num_init=20000)
-    o.close()
-    return {"value": r["mutations"] / r["seconds"], "unit": "mutations/s", "cores": threads, "kind": "port",
-            "sample": "%d chains, %.1f s of the chain loop (prepass of 20000 bootstrap paths excluded), %d mutations"
-                      % (chains, r["seconds"], r["mutations"])}
+    loop = CpuChainLoop(sd, threads, chains)
+    try:
+        return loop.sample(seconds)
+    finally:
+        loop.close()
+
+
+def cpu_throughput(xml: str, seconds: float = 15.0, threads: int | None = None, chains: int | None = None):
+    """cpu_throughput_scene on a scene XML file."""
+    return cpu_throughput_scene(dscene.load_scene(xml), seconds, threads, chains)

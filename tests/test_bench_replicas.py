@@ -52,3 +52,14 @@ def test_single_rank_passthrough():
     sys.path.insert(0, REPO)
     import bench
     assert bench.replica_totals(3.5, 7, 1) == (3.5, 7)
+
+
+def test_gpus_flag_must_match_world_size():
+    """--gpus N without a torchrun world of N ranks is refused, not silently run on one rank."""
+    import subprocess
+    env = dict(os.environ)
+    env.pop("WORLD_SIZE", None)
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--gpus", "2", "--steps", "1"],
+                       capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0
+    assert "world size is 1" in r.stderr

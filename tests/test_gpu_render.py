@@ -137,6 +137,32 @@ def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
         np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
 
 
+def test_multi_iteration_graphs_keep_the_chains(built_lib, scene_root):
+    """Graphs of 4 iterations (graph_iters=4: the chain groups run free inside a
+    graph and join only at its end) step the chains exactly as stage-by-stage
+    launches do, including the iterations short of a whole graph that run()
+    launches without it. 5041 chains on the 256x256 box at 1 spp get 13 samples
+    each, and 13 of them a 14th (the reference's chainsNeedExtraSamples rule),
+    so run(14) is three graph launches plus two leftover iterations, the last
+    of them the extra-sample iteration."""
+    from drmlt import scenegen
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    sd = dscene.load_scene(scenegen.config1(os.path.join(scene_root, "graph4"), spp=1))
+    out = []
+    for kw in (dict(use_graph=1, graph_iters=4), dict(use_graph=0)):
+        with Renderer(sd, num_chains=5041, **kw) as r:
+            assert r.total_iterations() == 14
+            if kw["use_graph"]:
+                assert r.launch_shape()["graph_iterations"] == 4
+            r.prepass()
+            assert r.run(14) == 13 * 5041 + 13
+            out.append((r.stats(), r.film().astype(np.float64)))
+    assert out[0][0] == out[1][0]
+    assert out[0][0]["mutations"] == 13 * 5041 + 13
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-4, atol=1e-6)
+
+
 def test_autotuner_keeps_the_chains(built_lib, scene_root):
     """drmlt_autotune runs real iterations under each candidate launch shape and
     settles on one of them; the render is the one an untuned render gives

@@ -189,3 +189,37 @@ def test_oracle_dr_loop_runs(oracles):
     assert st[0] + st[2] == st[8]            # every iteration is a large step or a stage-1 small step
     assert st[4] + st[6] <= st[2] - st[3]    # second stages only after rejected small steps
     assert np.isfinite(r["film"]).all() and r["film"].sum() > 0
+
+
+def test_oracle_bvh_matches_brute_force():
+    """The oracle's own BVH (object-median splits, used above 1024 triangles,
+    e.g. for the 3.0 M-triangle config-4 scene) returns the brute-force
+    answer: the same closest triangle and distance for every ray, the same
+    occlusion answer for every shadow ray (src/scene.cpp:80-111 semantics)."""
+    import oracle_dr
+    from drmlt import procedural
+    sd = procedural.config4(freq=24, grid=48, chains=256)  # 16,128 triangles, same construction as config 4
+    o = oracle_dr.Oracle(sd)
+    rng = np.random.default_rng(3)
+    n = 20000
+    org = (rng.random((n, 3)) * 4 - 2).astype(np.float32)
+    d = rng.standard_normal((n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    # rays from surface points along the normal-ish direction, the bounce-ray case
+    tb, thb = o.trace_rays(org, d, mode="brute")
+    tv, thv = o.trace_rays(org, d, mode="bvh")
+    assert (tb >= 0).mean() > 0.3
+    assert np.array_equal(tb, tv)
+    assert np.array_equal(thb, thv)
+    hit = tb >= 0
+    p = org[hit] + thb[hit, None] * d[hit]
+    d2 = rng.standard_normal(p.shape)
+    d2 = (d2 / np.linalg.norm(d2, axis=1, keepdims=True)).astype(np.float32)
+    p = p.astype(np.float32)
+    tb2, _ = o.trace_rays(p, d2, mode="brute")
+    tv2, _ = o.trace_rays(p, d2, mode="bvh")
+    assert np.array_equal(tb2, tv2)
+    ab, _ = o.trace_rays(org, d, tmax=1.0, any_hit=True, mode="brute")
+    av, _ = o.trace_rays(org, d, tmax=1.0, any_hit=True, mode="bvh")
+    assert np.array_equal(ab >= 0, av >= 0)
+    o.close()
