@@ -251,7 +251,8 @@ def run_ours(args, world, rank, local):
     t0 = time.perf_counter()
     r2 = Renderer(sd, device=local, seed=seed + 1, autotune=0, stage_lanes=shape["chains_per_warp"],
                   stage2_lanes=shape["stage2_chains_per_warp"], deriv_warps=shape["derivative_warps"],
-                  use_graph=1 if shape["graph_iterations"] else 0, graph_iters=max(1, shape["graph_iterations"]))
+                  use_graph=1 if shape["graph_iterations"] else 0, graph_iters=max(1, shape["graph_iterations"]),
+                  wavefront=shape["wavefront"])
     r2.prepass()
     t1 = time.perf_counter()
     e_done = 0
@@ -382,10 +383,11 @@ def rel_mse(img, ref):
     return float(np.mean((img - ref) ** 2 / (ref * ref + 1e-2)))
 
 
-# The plain per-stage-launch GPU drop-in: the same kernels launched one stage
-# at a time on one stream without CUDA graphs, one chain per lane in the
-# per-chain kernels, one warp per chain's derivatives, no launch autotuning.
-PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, stage2_lanes=32, deriv_warps=1)
+# The plain per-stage-launch GPU drop-in: the chain loop's stages launched one
+# at a time on one stream without CUDA graphs, one chain per lane tracing its
+# whole path (no wavefront rounds), one warp per chain's derivatives, no
+# launch autotuning.
+PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, stage2_lanes=32, deriv_warps=1, wavefront=0)
 
 
 def render_reference(sd, device, spp):

@@ -97,6 +97,8 @@ struct RunParams {
     int lanes2;          // chains per warp in the second-stage list kernels (1..32)
     const int *iterp;    // the group's current iteration (device memory)
     int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
+    int wave;            // 1: path tracing in wavefront rounds (wave.cuh), 0: one chain per lane
+    int waveRounds;      // rounds of a wavefront stage pass (max_depth + 1)
     unsigned long long seed;
 };
 
@@ -189,8 +191,5 @@ DEV void flush_stats(const StatAcc &acc, unsigned long long *global) {
 
 DEV long long samples_of(const RunParams &p, int i) { return p.samplesPerChain + (i < p.extraChains ? 1 : 0); }
 
-DEV float length_pmf(const ChainView &d, int len) {
-    return d.lengthFunc[len] / (d.lengthFuncInt * float(d.lengthCount));
-}
 
 }  // namespace drmlt

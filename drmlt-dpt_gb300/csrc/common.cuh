@@ -236,6 +236,7 @@ struct SceneView {
 // 32-bit output (PCG XSH-RR). Each (chain, iteration, stage) gets its own stream.
 struct Rng {
     uint64_t state;
+    Rng() = default;
     DEV static uint64_t mix(uint64_t z) {
         z += 0x9E3779B97F4A7C15ull;
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;

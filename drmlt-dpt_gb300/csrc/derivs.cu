@@ -75,6 +75,21 @@ __global__ void __launch_bounds__(128) k_gradhess_paths(SceneView s, const PathR
     derivs_for_path(s, r, 1.0f, kMaxLen, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim);
 }
 
+// Gradient + Hessian at each path's own primary vector, gated as in the chain
+// loop: zero (the isotropic fallback of drsmallstep.cpp:133-163) for a path
+// longer than maxDerv segments or with ss <= 1e-15.
+__global__ void __launch_bounds__(128) k_gradhess_gated(SceneView s, const PathRec *paths, const float *ss, int n,
+                                                        int maxDerv, float *grad, float *hess) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= n) return;
+    derivs_for_path(s, paths[w], ss[w], maxDerv, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim);
+}
+
+void launch_gradhess_gated(const SceneView &s, const PathRec *paths, const float *ss, int n, int maxDerv, float *grad,
+                           float *hess, cudaStream_t st) {
+    k_gradhess_gated<<<(n * 32 + 127) / 128, 128, 0, st>>>(s, paths, ss, n, maxDerv, grad, hess);
+}
+
 void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s) {
     k_derivs<<<blocks, 128, 0, s>>>(p, which);
 }

@@ -15,6 +15,9 @@ void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s);
 // The same for caller-supplied paths and primary samples (u: n x kMaxDim).
 void launch_gradhess_paths(const SceneView &s, const PathRec *paths, const float *u, int n, float *grad,
                            float *hess, cudaStream_t st);
+// The same at each path's own primary vector, gated by path length and ss as the chain loop gates it.
+void launch_gradhess_gated(const SceneView &s, const PathRec *paths, const float *ss, int n, int maxDerv, float *grad,
+                           float *hess, cudaStream_t st);
 cudaError_t set_derivs_carveout(int percent);
 // Resident blocks of the derivative kernel per SM (its grid-stride grid).
 int derivs_blocks_per_sm();

@@ -1,7 +1,7 @@
 // Host side of libdrmlt.so: scene upload, prepass orchestration, the chain
 // iteration schedule and the C ABI declared in include/drmlt_capi.h.
 #include "drmlt_capi.h"
-#include "kernels.cuh"
+#include "wave.cuh"
 #include "bvh.h"
 #include "errors.h"
 
@@ -132,6 +132,14 @@ struct Renderer {
     std::vector<cudaStream_t> gstreams;
     std::vector<cudaEvent_t> gevents;
     unsigned long long bootSeed = 0;
+    // wavefront queues (wave.cuh): per chain its machine and y* record; per
+    // queue slot (sliced per chain group) the chain, its ray and the answer
+    WaveChain *waveChains = nullptr;
+    PathRec *waveYstar = nullptr;
+    int *waveQ[2] = {nullptr, nullptr};
+    float4 *waveRayO[2] = {nullptr, nullptr}, *waveRayD[2] = {nullptr, nullptr};
+    int *waveHit = nullptr;
+    int *waveCount = nullptr;  // per group: 3 stage passes x kWaveCountStride
 
     template <class T>
     int alloc(T **p, size_t n) {
@@ -183,8 +191,28 @@ struct Renderer {
         p.lanes2 = opt.stage2_lanes > 0 ? std::min(opt.stage2_lanes, 32) : std::min(p.lanes, 4);
         p.iterp = dIters;
         p.derivWarps = opt.deriv_warps > 0 ? std::min(opt.deriv_warps, 4) : 2;
+        p.wave = opt.wavefront != 0 ? 1 : 0;
+        p.waveRounds = std::min(std::min(opt.max_depth, kMaxLen) + 1, kWaveMaxRounds);
         p.seed = opt.seed;
         return p;
+    }
+
+    // Chain group g's queues for stage pass `stage` (1: stage 1, 2: stage 2, 3: y*).
+    WaveView wave_view(int g, int stage) const {
+        const RunParams p = params(g);
+        WaveView w;
+        w.chains = waveChains;
+        w.ystar = waveYstar;
+        for (int b = 0; b < 2; b++) {
+            w.q[b] = waveQ[b] + p.c0;
+            w.rayO[b] = waveRayO[b] + p.c0;
+            w.rayD[b] = waveRayD[b] + p.c0;
+        }
+        w.hit = waveHit + p.c0;
+        w.count = waveCount + size_t(kWaveCountStride) * (3 * g + stage - 1);
+        w.cap = p.N;
+        w.rounds = p.waveRounds;
+        return w;
     }
 
     // chain group g: its chain range and its slices of the lists, counters and derivative rows
@@ -467,6 +495,16 @@ struct Renderer {
             CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             gevents.push_back(e);
         }
+        if ((rc = alloc(&waveChains, size_t(N)))) return rc;
+        if ((rc = alloc(&waveYstar, size_t(N)))) return rc;
+        for (int b = 0; b < 2; b++) {
+            if ((rc = alloc(&waveQ[b], size_t(N)))) return rc;
+            if ((rc = alloc(&waveRayO[b], size_t(N)))) return rc;
+            if ((rc = alloc(&waveRayD[b], size_t(N)))) return rc;
+        }
+        if ((rc = alloc(&waveHit, size_t(N)))) return rc;
+        if ((rc = alloc(&waveCount, size_t(3) * kWaveCountStride * G))) return rc;
+        CK(cudaMemset(waveCount, 0, size_t(3) * kWaveCountStride * G * sizeof(int)));
         if ((rc = alloc(&cv.counters, 4 * size_t(G)))) return rc;
         if ((rc = alloc(&cv.hist, size_t(kPlanBins) * G))) return rc;
         if ((rc = alloc(&dIters, size_t(G)))) return rc;
@@ -627,11 +665,15 @@ struct Renderer {
         const int nbWarp = std::min((p.N * 32 * p.derivWarps + 127) / 128, derivsGrid);
         const int nbG = std::min(p.N, gaussGrid);
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
+        const bool ystar = p.drType == 0 && p.integrator == 0;
         switch (k) {
             case 0:
-                k_reset_counters<<<1, 128, 0, s>>>(p.d.counters, p.d.hist);
+                k_reset_counters<<<1, 128, 0, s>>>(p.d.counters, p.d.hist,
+                                                  waveCount + size_t(3) * kWaveCountStride * g,
+                                                  p.wave ? 3 * kWaveCountStride : 0);
                 k_plan<<<nb, kStageBlock, 0, s>>>(p);
                 k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
+                if (p.wave) return 3 + launch_wave<1>(p, g, s);
                 k_stage1<<<nbS, kStageBlock, 0, s>>>(p);
                 return 4;
             case 1: launch_derivs(p, 0, nbWarp, s); return 1;
@@ -639,15 +681,37 @@ struct Renderer {
                 k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0);
                 k_h2mc_offset<<<(p.N * 32 + 127) / 128, 128, 0, s>>>(p);
                 return 2;
-            case 3: k_stage2<<<nbS2, kStageBlock, 0, s>>>(p); return 1;
+            case 3:
+                if (p.wave) return launch_wave<2>(p, g, s);
+                k_stage2<<<nbS2, kStageBlock, 0, s>>>(p);
+                return 1;
             case 4: launch_derivs(p, 2, nbWarp, s); return 1;
             case 5: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 2); return 1;
-            default:
-                if (p.drType == 0 && p.integrator == 0) k_ystar<<<nbS2, kStageBlock, 0, s>>>(p);
+            default: {
+                int n = 2;
+                if (ystar && p.wave) n += launch_wave<3>(p, g, s);
+                if (ystar && !p.wave) {
+                    k_ystar<<<nbS2, kStageBlock, 0, s>>>(p);
+                    n += 1;
+                }
                 k_finish<<<nbS, kStageBlock, 0, s>>>(p);
                 k_advance_iter<<<1, 1, 0, s>>>(dIters + g);
-                return p.drType == 0 && p.integrator == 0 ? 3 : 2;
+                return n;
+            }
         }
+    }
+    // One wavefront stage pass of chain group g: the prologue kernel, then
+    // waveRounds rounds of (traversal, machine steps). Returns the launches.
+    template <int kStage>
+    int launch_wave(const RunParams &p, int g, cudaStream_t s) const {
+        const WaveView w = wave_view(g, kStage);
+        const int nb = (p.N + kWaveBlock - 1) / kWaveBlock;
+        k_wave_begin<kStage><<<nb, kWaveBlock, 0, s>>>(p, w);
+        for (int r = 0; r < w.rounds; r++) {
+            k_wave_trace<<<nb, kWaveBlock, 0, s>>>(p.s, w, r);
+            k_wave_advance<kStage><<<nb, kWaveBlock, 0, s>>>(p, w, r);
+        }
+        return 1 + 2 * w.rounds;
     }
     // returns the number of kernels launched
     int launch_iteration(int g, cudaStream_t s) const {
@@ -775,11 +839,12 @@ struct Renderer {
 
     // Launch-shape autotuner: after `per` untimed iterations (past the first
     // iterations' transient), times `per` real iterations under each candidate
-    // number of chains per warp in the per-chain stage kernels, in two passes
-    // of opposite order so that a drift of the iteration cost over the render
-    // cancels, keeps the fastest, then does the same for the number of warps
-    // sharing one chain's derivatives, then (graphs on, `per` a multiple of 4)
-    // the number of iterations per graph launch. The iterations are part of the render:
+    // in two passes of opposite order (so that a drift of the iteration cost
+    // over the render cancels) and keeps the fastest: first wavefront against
+    // per-lane path tracing, then the number of chains per warp in the
+    // per-chain stage kernels, then the number of warps sharing one chain's
+    // derivatives, then (graphs on, `per` a multiple of 4) the number of
+    // iterations per graph launch. The iterations are part of the render:
     // the launch shape never changes which steps the chains take. Stops early
     // when the render runs out of iterations.
     int autotune(int per, int *lanesOut, int *warpsOut) {
@@ -806,6 +871,17 @@ struct Renderer {
         };
         float warm = 0.0f;
         if (int rc = trial(bestL, bestW, warm)) return rc;
+        // path tracing: wavefront rounds or one chain per lane
+        {
+            float tv[2] = {0, 0};
+            for (int pass = 0; pass < 2 && !out; pass++)
+                for (int k = 0; k < 2 && !out; k++) {
+                    const int i = pass == 0 ? k : 1 - k;
+                    opt.wavefront = i;
+                    if (int rc = trial(bestL, bestW, tv[i])) return rc;
+                }
+            if (!out) opt.wavefront = tv[1] <= tv[0] ? 1 : 0;
+        }
         // chains per warp
         float tl[5] = {0, 0, 0, 0, 0};
         for (int pass = 0; pass < 2 && !out; pass++)
@@ -921,6 +997,7 @@ void drmlt_default_options(drmlt_options *o) {
     o->smem_carveout = -1;
     o->stage2_lanes = 0;
     o->graph_iters = 0;
+    o->wavefront = -1;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }
@@ -988,6 +1065,12 @@ int drmlt_get_launch_shape(void *handle, int *stage_lanes, int *stage2_lanes, in
     if (stage2_lanes) *stage2_lanes = p.lanes2;
     if (deriv_warps) *deriv_warps = p.derivWarps;
     if (graph_iters) *graph_iters = r->opt.use_graph ? r->graphIters : 0;
+    return DRMLT_OK;
+}
+
+int drmlt_get_wavefront(void *handle, int *wavefront) {
+    if (!handle || !wavefront) return fail(DRMLT_E_ARG, "null argument");
+    *wavefront = static_cast<const Renderer *>(handle)->params().wave;
     return DRMLT_OK;
 }
 

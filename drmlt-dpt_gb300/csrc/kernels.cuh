@@ -78,6 +78,156 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(RunParams p) {
 static_assert(2 * kScatterBlock == kPlanBins, "k_scatter scans two bins per thread");
 
 // ------------------------------------------------------------- stage 1
+// The path-tracing stages (stage 1, stage 2, Green's y*) are written as a
+// prologue, the path machine (path.cuh) and an epilogue, shared by the
+// per-lane kernels below (one chain per lane traces its whole path) and the
+// wavefront kernels (wave.cuh), so that both schedules take identical steps.
+enum : int {
+    kTraceNone = 0,     // no path to trace: the prologue finished the stage
+    kTraceFail = 1,     // a large step whose sampled length is empty: finish as a failed proposal
+    kTracePerturb = 2,  // PerturbPathBidir machine
+    kTraceSubpath = 3   // GenerateSubpath machine
+};
+
+// The multiplexed large step's acceptance (src/mutation.cpp:86-98): technique
+// pmfs 1 / (length + 1) and the path-length distribution's pmf
+// (PiecewiseConstant1D::Pmf of func over count lengths), for the current
+// technique of length lc and score lsc and the proposal's (ly, lsy).
+DEV float large_step_ratio(const float *lengthFunc, float lengthFuncInt, int lengthCount, int lc, float lsc, int ly,
+                           float lsy) {
+    const float pmfY = lengthFunc[ly] / (lengthFuncInt * float(lengthCount));
+    const float pmfC = lengthFunc[lc] / (lengthFuncInt * float(lengthCount));
+    return clamp01((float(ly + 1) * lsy / pmfY) / (float(lc + 1) * lsc / pmfC));
+}
+
+// Stage-1 prologue of chain i (delayed.cpp:396-441 up to the proposal's path
+// sampling): the large-step coin and, for a large step, its length and light
+// subpath length (LargeStep::Mutate, src/mutation.cpp:7-120, multiplexed and
+// bidirectional); for a small step the sigma1 offsets (SmallStep::Mutate,
+// src/mutation.cpp:126-166). Chains that trace nothing (inactive, or
+// integrator=h2mc's H2MC step) are finished here.
+DEV int stage1_begin(const RunParams &p, int i, int iter, Rng &rng, float *off, PathM &m, int &flags, StatAcc &acc) {
+    Scratch &sc = p.d.scr[i];
+    flags = 0;
+    if (iter >= samples_of(p, i)) {
+        sc.flags = 0;
+        sc.a1 = 0.0f;
+        sc.a2 = 0.0f;
+        return kTraceNone;
+    }
+    flags = kActive;
+    acc.c[kStatMutations]++;
+    rng = Rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 0ull);
+    const Slot &cur = slot_of(p.d, i, 0);
+    Slot &F = slot_of(p.d, i, 1);
+    const bool isLarge = flip_coin(p.largeProb, rng.uniform());
+    if (isLarge) flags |= kLarge;
+    if (!cur.valid || isLarge) {
+        acc.c[kStatLarge]++;
+        const int length = sample_discrete(p.d.lengthCdf, p.d.lengthCount, rng.uniform());
+        int lgtLength = int(rng.uniform() * float(length + 1));
+        lgtLength = lgtLength < 0 ? 0 : (lgtLength > length ? length : lgtLength);
+        F.gaussInit = 0;
+        if (length < 1) return kTraceFail;
+        m.pc = kGStart;
+        m.camLength = length - lgtLength + 1;
+        m.lgtLength = lgtLength;
+        return kTraceSubpath;
+    }
+    if (p.integrator == 1 && !(rng.uniform() < p.uniformMix)) {
+        // H2MCIntegrator (src/integrators/h2mc.cpp:200-240): H2MCSmallStep::Mutate
+        // (h2mc.cpp:448-606) without its lens branch, as the single stage,
+        // run by the second-stage kernels
+        flags |= kSecond | kAniso | kSingle;
+        acc.c[kStatH2mc]++;
+        p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
+        if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+        p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+        sc.flags = flags;
+        sc.a1 = 0.0f;
+        sc.a2 = 0.0f;
+        return kTraceNone;
+    }
+    // SmallStep::Mutate with perturbStdDev; for integrator=h2mc the
+    // uniform-mixing step (h2mc.cpp:454-459)
+    acc.c[kStatStage1]++;
+    const int dim = path_dim(cur.rec.c, cur.rec.l);
+    for (int k = 0; k < dim; k++) off[k] = p.sigma1 * rng.normal();
+    F.gaussInit = 0;
+    m.pc = kPStart;
+    return kTracePerturb;
+}
+
+// Stage-1 epilogue: the first acceptance (mutation.cpp:86-98 for a large step,
+// :155 for a small one), the second-stage decision (delayed.cpp:443-451) and
+// the chain's entries in the second-stage lists. `st` is the sampler's result
+// (kStepDone with the proposal's contribution in e, or kStepFail).
+DEV void stage1_end(const RunParams &p, int i, int mode, int flags, Rng &rng, int st, const Emit &e, StatAcc &acc) {
+    Scratch &sc = p.d.scr[i];
+    const Slot &cur = slot_of(p.d, i, 0);
+    Slot &F = slot_of(p.d, i, 1);
+    const bool ok = st == kStepDone;
+    float a1 = 0.0f;
+    bool accept1 = false;
+    if (mode != kTracePerturb) {
+        if (ok) {
+            rng.uniform();  // contribution pick over a single candidate
+            set_contrib(F, e, p.b);
+            if (cur.valid)
+                a1 = large_step_ratio(p.d.lengthFunc, p.d.lengthFuncInt, p.d.lengthCount, cur.rec.c + cur.rec.l - 1,
+                                      cur.ls, e.c + e.l - 1, e.ls);
+        }
+        if (is_invalid(a1)) {
+            a1 = 0.0f;
+        } else {
+            accept1 = flip_coin(a1, rng.uniform());
+            if (accept1) acc.c[kStatLargeAcc]++;
+        }
+    } else {
+        if (ok) {
+            set_contrib(F, e, p.b);
+            a1 = clamp01(e.ss / cur.ss);
+        }
+        if (is_invalid(a1)) {
+            a1 = 0.0f;
+        } else {
+            accept1 = flip_coin(a1, rng.uniform());
+            if (accept1) acc.c[kStatStage1Acc]++;
+        }
+    }
+    if (accept1) flags |= kAccept1;
+    const bool doSecond = !accept1 && !(flags & kLarge) && cur.valid && p.integrator == 0;
+    if (doSecond) {
+        flags |= kSecond;
+        p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
+        if (flip_coin(p.anisoProb, rng.uniform())) {
+            flags |= kAniso;
+            acc.c[kStatH2mc]++;
+            if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+            p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+        } else {
+            acc.c[kStatIso]++;
+        }
+    }
+    sc.flags = flags;
+    sc.a1 = a1;
+    sc.a2 = 0.0f;
+}
+
+// The machines with every ray answered on the spot (per-lane kernels).
+template <class R>
+DEV int run_subpath(const SceneView &s, R &rng, PathRec &rec, PathM &m) {
+    int hit = -1, st;
+    while ((st = subpath_step(s, rng, rec, m, hit)) == kStepRay) hit = answer_ray(s, m);
+    return st;
+}
+template <class J>
+DEV int run_perturb(const SceneView &s, const PathRec &in, const float *off, J &jit, PathRec &out, PathM &m) {
+    int hit = -1, st;
+    while ((st = perturb_step(s, in, off, jit, out, m, hit)) == kStepRay) hit = answer_ray(s, m);
+    return st;
+}
+
 __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
     const int iter = *p.iterp;
     bool on;
@@ -85,92 +235,17 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
     StatAcc acc;
     if (on && t < p.N) {
         const int i = p.d.order[t];
-        Scratch &sc = p.d.scr[i];
-        int flags = 0;
-        float a1 = 0.0f;
-        if (iter < samples_of(p, i)) {
-            flags |= kActive;
-            acc.c[kStatMutations]++;
-            Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 0ull);
-            Slot &cur = slot_of(p.d, i, 0);
-            Slot &F = slot_of(p.d, i, 1);
-            const bool isLarge = flip_coin(p.largeProb, rng.uniform());
-            if (isLarge) flags |= kLarge;
-            bool accept1 = false;
-            if (!cur.valid || isLarge) {
-                // LargeStep::Mutate, multiplexed + bidirectional (src/mutation.cpp:7-120)
-                acc.c[kStatLarge]++;
-                const int length = sample_discrete(p.d.lengthCdf, p.d.lengthCount, rng.uniform());
-                int lgtLength = int(rng.uniform() * float(length + 1));
-                lgtLength = lgtLength < 0 ? 0 : (lgtLength > length ? length : lgtLength);
-                const int camLength = length - lgtLength + 1;
-                Emit e;
-                const bool ok = length >= 1 && generate_subpath(p.s, camLength, lgtLength, rng, F.rec, e);
-                F.gaussInit = 0;
-                if (ok) {
-                    rng.uniform();  // contribution pick over a single candidate
-                    set_contrib(F, e, p.b);
-                    if (cur.valid) {
-                        const int lc = cur.rec.c + cur.rec.l - 1;
-                        const int ly = e.c + e.l - 1;
-                        a1 = clamp01((float(ly + 1) * e.ls / length_pmf(p.d, ly)) /
-                                     (float(lc + 1) * cur.ls / length_pmf(p.d, lc)));
-                    }
-                }
-                if (is_invalid(a1)) {
-                    a1 = 0.0f;
-                } else {
-                    accept1 = flip_coin(a1, rng.uniform());
-                    if (accept1) acc.c[kStatLargeAcc]++;
-                }
-            } else if (p.integrator == 1 && !(rng.uniform() < p.uniformMix)) {
-                // H2MCIntegrator (src/integrators/h2mc.cpp:200-240): H2MCSmallStep::Mutate
-                // (h2mc.cpp:448-606) without its lens branch, as the single stage,
-                // run by the second-stage kernels
-                flags |= kSecond | kAniso | kSingle;
-                acc.c[kStatH2mc]++;
-                p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
-                if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
-                p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
-            } else {
-                // SmallStep::Mutate with perturbStdDev (src/mutation.cpp:126-166); for
-                // integrator=h2mc the uniform-mixing step (h2mc.cpp:454-459)
-                acc.c[kStatStage1]++;
-                const int dim = path_dim(cur.rec.c, cur.rec.l);
-                float off[kMaxDim];
-                for (int k = 0; k < dim; k++) off[k] = p.sigma1 * rng.normal();
-                Emit e;
-                const bool ok = perturb_path(p.s, cur.rec, off, rng, F.rec, e);
-                F.gaussInit = 0;
-                if (ok) {
-                    set_contrib(F, e, p.b);
-                    a1 = clamp01(e.ss / cur.ss);
-                }
-                if (is_invalid(a1)) {
-                    a1 = 0.0f;
-                } else {
-                    accept1 = flip_coin(a1, rng.uniform());
-                    if (accept1) acc.c[kStatStage1Acc]++;
-                }
-            }
-            if (accept1) flags |= kAccept1;
-            const bool doSecond = !accept1 && !isLarge && cur.valid && p.integrator == 0;
-            if (doSecond) {
-                flags |= kSecond;
-                p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
-                if (flip_coin(p.anisoProb, rng.uniform())) {
-                    flags |= kAniso;
-                    acc.c[kStatH2mc]++;
-                    if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
-                    p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
-                } else {
-                    acc.c[kStatIso]++;
-                }
-            }
+        Rng rng;
+        float off[kMaxDim];
+        PathM m;
+        int flags;
+        const int mode = stage1_begin(p, i, iter, rng, off, m, flags, acc);
+        if (mode != kTraceNone) {
+            int st = kStepFail;
+            if (mode == kTraceSubpath) st = run_subpath(p.s, rng, slot_of(p.d, i, 1).rec, m);
+            if (mode == kTracePerturb) st = run_perturb(p.s, slot_of(p.d, i, 0).rec, off, rng, slot_of(p.d, i, 1).rec, m);
+            stage1_end(p, i, mode, flags, rng, st, m.e, acc);
         }
-        sc.flags = flags;
-        sc.a1 = a1;
-        sc.a2 = 0.0f;
     }
     flush_stats(acc, p.d.stats);
 }
@@ -251,36 +326,38 @@ __global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p) {
 }
 
 // ------------------------------------------------------------- stage 2 proposal
-// Over the group's second-stage list only (compacted by k_stage1).
-__global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
-    const int iter = *p.iterp;
-    bool on;
-    const int t = sparse_index(p.lanes2, on);
-    if (!on || t >= p.d.counters[2]) return;
-    const int i = p.d.listS[t];
-    Scratch &sc = p.d.scr[i];
-    Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
-    Slot &cur = slot_of(p.d, i, 0);
+// Stage-2 prologue (chains of the second-stage list built by stage 1): the
+// second proposal's offsets -- for PH2MCSmallStep::Mutate (drsmallstep.cpp:113-212)
+// the ones k_h2mc_offset sampled from this stream's first dim normals (skipped
+// here), for SmallStep::Mutate with the second-stage sigma (mutation.cpp:167-208)
+// sigma2 normals -- and the perturbation machine.
+DEV void stage2_begin(const RunParams &p, int i, int iter, Rng &rng, float *off, PathM &m) {
+    const Scratch &sc = p.d.scr[i];
+    rng = Rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
+    const Slot &cur = slot_of(p.d, i, 0);
     Slot &S = slot_of(p.d, i, 2);
     const int dim = path_dim(cur.rec.c, cur.rec.l);
-    float off[kMaxDim];
-    const bool aniso = sc.flags & kAniso;
-    if (aniso) {
-        // PH2MCSmallStep::Mutate (drsmallstep.cpp:113-212): the offset was
-        // sampled by k_h2mc_offset from this stream's first dim normals
+    if (sc.flags & kAniso) {
         for (int k = 0; k < dim; k++) {
             rng.normal();
             off[k] = sc.offset[k];
         }
     } else {
-        // SmallStep::Mutate with the second-stage sigma (mutation.cpp:167-208)
         for (int k = 0; k < dim; k++) off[k] = p.sigma2 * rng.normal();
     }
-    Emit e;
-    const bool ok = perturb_path(p.s, cur.rec, off, rng, S.rec, e);
     S.gaussInit = 0;
+    m.pc = kPStart;
+}
+
+// Stage-2 epilogue: the proposal's state, its isotropic acceptance, or its
+// entry in the list of Gaussians at z (H2MC).
+DEV void stage2_end(const RunParams &p, int i, int st, const Emit &e) {
+    Scratch &sc = p.d.scr[i];
+    const Slot &cur = slot_of(p.d, i, 0);
+    Slot &S = slot_of(p.d, i, 2);
+    const bool aniso = sc.flags & kAniso;
     float a2 = 0.0f;
-    if (ok) {
+    if (st == kStepDone) {
         sc.flags |= kZValid;
         S.screen[0] = e.screen[0];
         S.screen[1] = e.screen[1];
@@ -299,29 +376,57 @@ __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
     sc.a2 = a2;
 }
 
+// Over the group's second-stage list only (compacted by stage 1).
+__global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
+    const int iter = *p.iterp;
+    bool on;
+    const int t = sparse_index(p.lanes2, on);
+    if (!on || t >= p.d.counters[2]) return;
+    const int i = p.d.listS[t];
+    Rng rng;
+    float off[kMaxDim];
+    PathM m;
+    stage2_begin(p, i, iter, rng, off, m);
+    const int st = run_perturb(p.s, slot_of(p.d, i, 0).rec, off, rng, slot_of(p.d, i, 2).rec, m);
+    stage2_end(p, i, st, m.e);
+}
+
 // Green's reverse path y* = z + (x - y) and its first-stage acceptance from z
 // (SmallStep::Trace, mutation.cpp:210-238), over the second-stage list only.
+// Prologue: false (aStar = 0 written) when z holds no valid state.
+DEV bool ystar_begin(const RunParams &p, int i, int iter, Rng &rng, float *off, PathM &m) {
+    Scratch &sc = p.d.scr[i];
+    const Slot &cur = slot_of(p.d, i, 0);
+    const Slot &F = slot_of(p.d, i, 1);
+    const Slot &S = slot_of(p.d, i, 2);
+    if (!S.valid) {
+        sc.aStar = 0.0f;
+        return false;
+    }
+    const int dim = path_dim(cur.rec.c, cur.rec.l);
+    for (int k = 0; k < dim; k++) off[k] = cur.rec.u[k] - F.rec.u[k];
+    rng = Rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 3ull);
+    m.pc = kPStart;
+    return true;
+}
+DEV void ystar_end(const RunParams &p, int i, int st, const Emit &e) {
+    const Slot &S = slot_of(p.d, i, 2);
+    p.d.scr[i].aStar = st == kStepDone ? clamp01(e.ss / S.ss) : 0.0f;
+}
+
 __global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes2, on);
     if (!on || t >= p.d.counters[2]) return;
     const int i = p.d.listS[t];
-    Scratch &sc = p.d.scr[i];
-    const Slot &cur = slot_of(p.d, i, 0);
-    const Slot &F = slot_of(p.d, i, 1);
-    const Slot &S = slot_of(p.d, i, 2);
-    float aStar = 0.0f;
-    if (S.valid) {
-        const int dim = path_dim(cur.rec.c, cur.rec.l);
-        float off[kMaxDim];
-        for (int k = 0; k < dim; k++) off[k] = cur.rec.u[k] - F.rec.u[k];
-        Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 3ull);
-        PathRec ystar;
-        Emit e;
-        if (perturb_path(p.s, S.rec, off, rng, ystar, e)) aStar = clamp01(e.ss / S.ss);
-    }
-    sc.aStar = aStar;
+    Rng rng;
+    float off[kMaxDim];
+    PathM m;
+    if (!ystar_begin(p, i, iter, rng, off, m)) return;
+    PathRec ystar;
+    const int st = run_perturb(p.s, slot_of(p.d, i, 2).rec, off, rng, ystar, m);
+    ystar_end(p, i, st, m.e);
 }
 
 // log N(d | 0, sigma^2 I) differences for Mira's Q1 ratio (delayed.cpp:512-523), FP64.
@@ -332,6 +437,44 @@ DEV double iso_quad(int dim, const float *a, const float *b) {
         q += d * d;
     }
     return q;
+}
+
+// log of Mira's transition-kernel ratio Q1(z, y) / Q1(x, y) with the isotropic
+// first-stage kernel of sigma1 (delayed.cpp:512-523: GaussianLogPdf(z - y) -
+// GaussianLogPdf(x - y), whose normalisation terms cancel), in FP64.
+DEV double mira_log_q(int dim, const float *x, const float *y, const float *z, float sigma1) {
+    const double inv2s2 = 0.5 / (double(sigma1) * double(sigma1));
+    return -inv2s2 * (iso_quad(dim, z, y) - iso_quad(dim, x, y));
+}
+
+// The second-stage acceptance probability of delayed rejection for a valid
+// (non-negative, finite) second-stage ratio a2 and the first stage's a1:
+//   Green & Mira (2001) (delayed.cpp:473-500): min(1, a2 (1 - a*) / (1 - a1))
+//     with a* the acceptance of Green's reverse path y* (aStarGreen; an invalid
+//     value counts as 0), 0 when a* = 1;
+//   Tierney & Mira (1999) (delayed.cpp:502-541): a* = min(1, ss(y) / ss(z)) (an
+//     invalid value counts as 1), 0 when a* = 1, else min(1, a2 Q (1 - a*) /
+//     (1 - a1)) with Q = Q1(z, y) / Q1(x, y), 0 when Q is invalid.
+// `draw` is set when a uniform decides the acceptance (not when the proposal is
+// rejected outright); x, y, z are the primary vectors of the current state and
+// the two proposals.
+DEV float dr_second_acceptance(int drType, float a1, float a2, float aStarGreen, float ssY, float ssZ, int dim,
+                               const float *x, const float *y, const float *z, float sigma1, bool &draw) {
+    draw = false;
+    if (drType == 0) {
+        float aStar = aStarGreen;
+        if (is_invalid(aStar)) aStar = 0.0f;
+        if (aStar == 1.0f) return 0.0f;
+        draw = true;
+        return metropolis_clamp(a2 * (1.0f - aStar) / (1.0f - a1));
+    }
+    float aStar = metropolis_clamp(ssY / ssZ);
+    if (is_invalid(aStar)) aStar = 1.0f;
+    if (aStar == 1.0f) return 0.0f;
+    const float transRatio = float(::exp(mira_log_q(dim, x, y, z, sigma1)));
+    if (is_invalid(transRatio)) return 0.0f;
+    draw = true;
+    return metropolis_clamp(a2 * transRatio * (1.0f - aStar) / (1.0f - a1));
 }
 
 // ------------------------------------------------------------- finish
@@ -367,33 +510,11 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
                 // the usual MH acceptance, Clamp(a, 0, 1) (h2mc.cpp:580-584, 220)
                 a2 = clamp01(a2);
                 accept2 = flip_coin(a2, rng.uniform());
-            } else if (p.drType == 0) {
-                // Green & Mira (2001) (delayed.cpp:473-500); y* traced by k_ystar
-                float aStar = sc.aStar;
-                if (is_invalid(aStar)) aStar = 0.0f;
-                if (aStar == 1.0f) {
-                    a2 = 0.0f;
-                } else {
-                    a2 = metropolis_clamp(a2 * (1.0f - aStar) / (1.0f - a1));
-                    accept2 = flip_coin(a2, rng.uniform());
-                }
             } else {
-                // Tierney & Mira (1999) (delayed.cpp:502-541)
-                float aStar = metropolis_clamp(F.ss / S.ss);
-                if (is_invalid(aStar)) aStar = 1.0f;
-                if (aStar == 1.0f) {
-                    a2 = 0.0f;
-                } else {
-                    const double inv2s2 = 0.5 / (double(p.sigma1) * double(p.sigma1));
-                    const double lr = -inv2s2 * (iso_quad(dim, S.rec.u, F.rec.u) - iso_quad(dim, cur.rec.u, F.rec.u));
-                    const float transRatio = float(::exp(lr));
-                    if (is_invalid(transRatio)) {
-                        a2 = 0.0f;
-                    } else {
-                        a2 = metropolis_clamp(a2 * transRatio * (1.0f - aStar) / (1.0f - a1));
-                        accept2 = flip_coin(a2, rng.uniform());
-                    }
-                }
+                bool draw;
+                a2 = dr_second_acceptance(p.drType, a1, a2, sc.aStar, F.ss, S.ss, dim, cur.rec.u, F.rec.u, S.rec.u,
+                                          p.sigma1, draw);
+                if (draw) accept2 = flip_coin(a2, rng.uniform());
             }
             if (accept2) acc.c[aniso ? kStatH2mcAcc : kStatIsoAcc]++;
         }
@@ -444,9 +565,12 @@ __global__ void k_set_iters(int *iters, int n, int value) {
     for (int g = threadIdx.x; g < n; g += blockDim.x) iters[g] = value;
 }
 
-__global__ void k_reset_counters(int *counters, int *hist) {
+// A chain group's list counters, work-class histogram and (nWave > 0) the
+// queue counters of its wavefront stage passes, at the start of an iteration.
+__global__ void k_reset_counters(int *counters, int *hist, int *waveCount, int nWave) {
     if (threadIdx.x < 4) counters[threadIdx.x] = 0;
     for (int k = threadIdx.x; k < kPlanBins; k += blockDim.x) hist[k] = 0;
+    for (int k = threadIdx.x; k < nWave; k += blockDim.x) waveCount[k] = 0;
 }
 
 // ------------------------------------------------------------- prepass

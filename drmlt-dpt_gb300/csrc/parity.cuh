@@ -424,3 +424,225 @@ int drmlt_fma_benchmark(void *handle, int fp64, int iterations, float *ms, doubl
 }
 
 }  // extern "C"
+
+// ============================================================================ per-stage acceptances
+namespace {
+
+// y = x + o1, z = x + o2 and Green's y* = z + (x - y), with the first-stage and
+// isotropic second-stage acceptances (the chain loop's prologue / epilogue
+// arithmetic on given offsets; discrete jitter off).
+__global__ void k_dr_eval_trace(SceneView s, const PathRec *x, const drmlt_contrib *xc, const float *o1,
+                                const float *o2, int n, PathRec *y, PathRec *z, float *ssz, drmlt_dr_result *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    NoJitter nj;
+    SceneView sv = s;
+    sv.opt.discreteStdDev = 0.0f;
+    drmlt_dr_result ev;
+    memset(&ev, 0, sizeof(ev));
+    PathM m;
+    m.pc = kPStart;
+    int st = run_perturb(sv, x[i], o1 + size_t(i) * kMaxDim, nj, y[i], m);
+    float a1 = 0.0f;
+    if (st == kStepDone) {
+        ev.valid_y = 1;
+        ev.ss_y = m.e.ss;
+        a1 = clamp01(m.e.ss / xc[i].ss);
+    }
+    ev.a1 = is_invalid(a1) ? 0.0f : a1;
+    m.pc = kPStart;
+    st = run_perturb(sv, x[i], o2 + size_t(i) * kMaxDim, nj, z[i], m);
+    if (st == kStepDone) {
+        ev.valid_z = 1;
+        ev.ss_z = m.e.ss;
+        const int dim = path_dim(x[i].c, x[i].l);
+        float off[kMaxDim];
+        for (int k = 0; k < dim; k++) off[k] = x[i].u[k] - y[i].u[k];
+        PathRec ys;
+        m.pc = kPStart;
+        if (run_perturb(sv, z[i], off, nj, ys, m) == kStepDone) ev.a_star_green = clamp01(m.e.ss / ev.ss_z);
+    }
+    ssz[i] = ev.ss_z;
+    out[i] = ev;
+}
+
+// The H2MC kernel ratio of PH2MCSmallStep::Mutate (drsmallstep.cpp:169-196) as
+// the chain loop's Gaussian kernel computes it: the Gaussians at x and z from
+// their derivatives (grad/hess rows i and n + i), then log N_z(-o) - log N_x(o)
+// in FP64. One team per H2MC case with a contributing z.
+__global__ void __launch_bounds__(32 * kGaussTeamWarps) k_dr_eval_ratio(const PathRec *x, const drmlt_contrib *xc,
+                                                                       const float *ssz, const float *o2,
+                                                                       const int *aniso, int n, float sigma,
+                                                                       int maxDim, const float *grad,
+                                                                       const float *hess, double *store,
+                                                                       drmlt_dr_result *out) {
+    extern __shared__ double gsm[];
+    const int i = blockIdx.x;
+    if (i >= n || !aniso[i] || !out[i].valid_z) return;
+    const int dim = path_dim(x[i].c, x[i].l);
+    if (dim > maxDim) return;
+    GaussSmem sm(gsm, maxDim);
+    const Team tm(gauss_reduction(gsm, maxDim));
+    double *gx = store + size_t(2 * i) * kGaussStride, *gz = store + size_t(2 * i + 1) * kGaussStride;
+    compute_gaussian_team(dim, H2mcParam(sigma), xc[i].ss, grad + size_t(i) * kMaxDim,
+                          hess + size_t(i) * kMaxDim * kMaxDim, sm, GaussView(gx), tm);
+    __syncthreads();
+    compute_gaussian_team(dim, H2mcParam(sigma), ssz[i], grad + size_t(n + i) * kMaxDim,
+                          hess + size_t(n + i) * kMaxDim * kMaxDim, sm, GaussView(gz), tm);
+    __syncthreads();
+    const float *o = o2 + size_t(i) * kMaxDim;
+    const double px = gauss_logpdf_team(dim, o, -1.0, GaussView(gz), tm);
+    const double py = gauss_logpdf_team(dim, o, 1.0, GaussView(gx), tm);
+    if (threadIdx.x == 0) out[i].log_ratio = px - py;
+}
+
+// The second-stage ratio and the Green / Mira acceptances (k_finish's arithmetic).
+__global__ void k_dr_eval_finish(const PathRec *x, const drmlt_contrib *xc, const PathRec *y, const PathRec *z,
+                                 const int *aniso, int n, float sigma1, drmlt_dr_result *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    drmlt_dr_result ev = out[i];
+    const int dim = path_dim(x[i].c, x[i].l);
+    float a2 = 0.0f;
+    if (ev.valid_z) a2 = aniso[i] ? float(::exp(ev.log_ratio)) * ev.ss_z / xc[i].ss : clamp01(ev.ss_z / xc[i].ss);
+    ev.log_q_mira = mira_log_q(dim, x[i].u, y[i].u, z[i].u, sigma1);
+    if (is_invalid(a2)) {
+        ev.a2 = 0.0f;
+    } else {
+        ev.a2 = a2;
+        bool draw;
+        ev.alpha2_green = dr_second_acceptance(0, ev.a1, a2, ev.a_star_green, ev.ss_y, ev.ss_z, dim, x[i].u, y[i].u,
+                                               z[i].u, sigma1, draw);
+        ev.alpha2_mira = dr_second_acceptance(1, ev.a1, a2, ev.a_star_green, ev.ss_y, ev.ss_z, dim, x[i].u, y[i].u,
+                                              z[i].u, sigma1, draw);
+    }
+    out[i] = ev;
+}
+
+__global__ void k_large_step_eval(SceneView s, const float *tapes, const int *tapeLen, int stride, int n,
+                                  const PathRec *x, const drmlt_contrib *xc, const float *lengthCdf,
+                                  const float *lengthFunc, float lengthFuncInt, int lengthCount, float *a1,
+                                  int *tech, drmlt_contrib *ct, int *consumed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    TapeRng rng{tapes + size_t(i) * stride, tapeLen[i], 0};
+    const int length = sample_discrete(lengthCdf, lengthCount, rng.uniform());
+    int lgtLength = int(rng.uniform() * float(length + 1));
+    lgtLength = lgtLength < 0 ? 0 : (lgtLength > length ? length : lgtLength);
+    float a = 0.0f;
+    drmlt_contrib c;
+    memset(&c, 0, sizeof(c));
+    tech[2 * i] = tech[2 * i + 1] = 0;
+    if (length >= 1) {
+        PathRec rec;
+        Emit e;
+        if (generate_subpath(s, length - lgtLength + 1, lgtLength, rng, rec, e)) {
+            rng.uniform();  // contribution pick over a single candidate
+            a = large_step_ratio(lengthFunc, lengthFuncInt, lengthCount, x[i].c + x[i].l - 1, xc[i].ls, e.c + e.l - 1,
+                                 e.ls);
+            tech[2 * i] = e.c;
+            tech[2 * i + 1] = e.l;
+            c.screen[0] = e.screen[0];
+            c.screen[1] = e.screen[1];
+            c.rgb[0] = e.rgb.x;
+            c.rgb[1] = e.rgb.y;
+            c.rgb[2] = e.rgb.z;
+            c.ls = e.ls;
+            c.ss = e.ss;
+            c.valid = 1;
+        }
+    }
+    a1[i] = a;
+    ct[i] = c;
+    consumed[i] = rng.pos;
+}
+
+}  // namespace
+
+extern "C" {
+
+int drmlt_dr_eval(void *handle, int n, const drmlt_path *x, const drmlt_contrib *x_contrib, const float *offset1,
+                  const float *offset2, const int32_t *aniso, drmlt_dr_result *out, drmlt_path *y_out,
+                  drmlt_path *z_out) {
+    if (!handle || n < 0 || (n && (!x || !x_contrib || !offset1 || !offset2 || !aniso || !out)))
+        return fail(DRMLT_E_ARG, "bad argument");
+    if (n == 0) return DRMLT_OK;
+    int rc = check_paths(x, n);
+    if (rc) return rc;
+    Renderer *r = static_cast<Renderer *>(handle);
+    const int maxDim = kMaxDim;
+    DevBuf<PathRec> dx, dyz;
+    DevBuf<drmlt_contrib> dxc;
+    DevBuf<float> do1, do2, dss, dg, dh;
+    DevBuf<int> dan;
+    DevBuf<drmlt_dr_result> dout;
+    DevBuf<double> dstore;
+    if ((rc = dx.put(reinterpret_cast<const PathRec *>(x), n)) || (rc = dxc.put(x_contrib, n)) ||
+        (rc = do1.put(offset1, size_t(n) * kMaxDim)) || (rc = do2.put(offset2, size_t(n) * kMaxDim)) ||
+        (rc = dan.put(aniso, n)) || (rc = dyz.alloc(2 * size_t(n))) || (rc = dss.alloc(2 * size_t(n))) ||
+        (rc = dout.alloc(n)) || (rc = dg.alloc(2 * size_t(n) * kMaxDim)) ||
+        (rc = dh.alloc(2 * size_t(n) * kMaxDim * kMaxDim)) || (rc = dstore.alloc(2 * size_t(n) * kGaussStride)))
+        return rc;
+    PathRec *dy = dyz.p, *dz = dyz.p + n;
+    k_dr_eval_trace<<<(n + 127) / 128, 128>>>(r->sv, dx.p, dxc.p, do1.p, do2.p, n, dy, dz, dss.p + n, dout.p);
+    CK(cudaGetLastError());
+    // derivatives at x (rows 0..n-1, score ss(x)) and z (rows n..2n-1, score ss(z))
+    std::vector<float> ssx(n);
+    for (int i = 0; i < n; i++) ssx[i] = x_contrib[i].ss;
+    CK(cudaMemcpy(dss.p, ssx.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    DevBuf<PathRec> dxz;
+    if ((rc = dxz.alloc(2 * size_t(n)))) return rc;
+    CK(cudaMemcpy(dxz.p, dx.p, n * sizeof(PathRec), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(dxz.p + n, dz, n * sizeof(PathRec), cudaMemcpyDeviceToDevice));
+    launch_gradhess_gated(r->sv, dxz.p, dss.p, 2 * n, r->opt.max_derivative_depth, dg.p, dh.p, 0);
+    CK(cudaGetLastError());
+    k_dr_eval_ratio<<<n, 32 * kGaussTeamWarps, gauss_smem_bytes(maxDim)>>>(
+        dx.p, dxc.p, dss.p + n, do2.p, dan.p, n, r->opt.perturb_stddev, maxDim, dg.p, dh.p, dstore.p, dout.p);
+    CK(cudaGetLastError());
+    k_dr_eval_finish<<<(n + 127) / 128, 128>>>(dx.p, dxc.p, dy, dz, dan.p, n, r->opt.perturb_stddev, dout.p);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if ((rc = dout.get(out, n))) return rc;
+    if (y_out) CK(cudaMemcpy(y_out, dy, n * sizeof(PathRec), cudaMemcpyDeviceToHost));
+    if (z_out) CK(cudaMemcpy(z_out, dz, n * sizeof(PathRec), cudaMemcpyDeviceToHost));
+    return DRMLT_OK;
+}
+
+int drmlt_large_step_eval(void *handle, int n, const float *tapes, const int32_t *tape_len, int stride,
+                          const drmlt_path *x, const drmlt_contrib *x_contrib, const float *length_func,
+                          int num_lengths, float *a1, int32_t *out_tech, drmlt_contrib *out_contrib,
+                          int32_t *out_consumed) {
+    if (!handle || n < 0 || stride < 1 || num_lengths < 1 ||
+        (n && (!tapes || !tape_len || !x || !x_contrib || !length_func || !a1 || !out_tech || !out_contrib ||
+               !out_consumed)))
+        return fail(DRMLT_E_ARG, "bad argument");
+    if (n == 0) return DRMLT_OK;
+    int rc = check_paths(x, n);
+    if (rc) return rc;
+    for (int i = 0; i < n; i++) {
+        if (tape_len[i] < 0 || tape_len[i] > stride) return fail(DRMLT_E_ARG, "tape length out of range");
+        if (x[i].c + x[i].l - 1 >= num_lengths) return fail(DRMLT_E_ARG, "current path longer than the length table");
+    }
+    Renderer *r = static_cast<Renderer *>(handle);
+    std::vector<float> func(length_func, length_func + num_lengths), cdf;
+    float funcInt;
+    piecewise_constant(func, cdf, funcInt);
+    DevBuf<float> dt, dcdf, dfunc, da;
+    DevBuf<int> dlen, dtech, dcons;
+    DevBuf<PathRec> dx;
+    DevBuf<drmlt_contrib> dxc, dct;
+    if ((rc = dt.put(tapes, size_t(n) * stride)) || (rc = dlen.put(tape_len, n)) ||
+        (rc = dx.put(reinterpret_cast<const PathRec *>(x), n)) || (rc = dxc.put(x_contrib, n)) ||
+        (rc = dcdf.put(cdf.data(), cdf.size())) || (rc = dfunc.put(func.data(), func.size())) ||
+        (rc = da.alloc(n)) || (rc = dtech.alloc(2 * size_t(n))) || (rc = dct.alloc(n)) || (rc = dcons.alloc(n)))
+        return rc;
+    k_large_step_eval<<<(n + 127) / 128, 128>>>(r->sv, dt.p, dlen.p, stride, n, dx.p, dxc.p, dcdf.p, dfunc.p, funcInt,
+                                                num_lengths, da.p, dtech.p, dct.p, dcons.p);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if ((rc = da.get(a1, n)) || (rc = dtech.get(out_tech, 2 * size_t(n))) || (rc = dct.get(out_contrib, n)))
+        return rc;
+    return dcons.get(out_consumed, n);
+}
+
+}  // extern "C"

@@ -128,8 +128,23 @@ DEV void convert_mis(const SceneView &s, int depth, int light, const V3 &rayOrg,
     ps.accMISWThis *= invCosTheta;
 }
 
+// The shadow ray of a connection: the connection contributes iff nothing lies
+// on (org, org + dist * dir) (Occluded, src/scene.cpp:95-105).
+struct Shadow {
+    V3 org, dir;
+    float dist;
+};
+
+// The connections below are split in two: *_pre does every test and the whole
+// evaluation except the visibility test and returns the shadow ray; the
+// connection contributes iff *_pre succeeds and the ray is not occluded. The
+// reference casts the shadow ray first, but the cast has no side effect and
+// every failing test returns false, so the order does not change any result.
+// This lets the wavefront sampler queue the shadow ray like any other ray.
+
 // ConnectToCamera (src/path.cpp:518-606).
-DEV bool connect_to_camera(const SceneView &s, int lgtDepth, const BState &ps, const SVert &v, Emit &e) {
+DEV bool connect_to_camera_pre(const SceneView &s, int lgtDepth, const BState &ps, const SVert &v, Emit &e,
+                               Shadow &sh) {
     V3 camOrg, camDir;
     float a, b;
     sample_primary(s.cam, 0.5f, 0.5f, camOrg, camDir, a, b);
@@ -140,7 +155,9 @@ DEV bool connect_to_camera(const SceneView &s, int lgtDepth, const BState &ps, c
     const float distSq = length_sq(dirToCamera);
     const float dist = sqrtf(distSq);
     dirToCamera = dirToCamera * (1.0f / dist);
-    if (occluded(s, ps.isect.position, dirToCamera, dist)) return false;
+    sh.org = ps.isect.position;
+    sh.dir = dirToCamera;
+    sh.dist = dist;
     const Bsdf &bsdf = bsdf_of_tri(s, v.tri);
     BsdfOut bo;
     bsdf_evaluate<true>(bsdf, ps.wi, ps.isect.shadingNormal, dirToCamera, bo);
@@ -171,6 +188,10 @@ DEV bool connect_to_camera(const SceneView &s, int lgtDepth, const BState &ps, c
     e.ls = score;
     e.ss = score * ps.ssJacobian;
     return true;
+}
+DEV bool connect_to_camera(const SceneView &s, int lgtDepth, const BState &ps, const SVert &v, Emit &e) {
+    Shadow sh;
+    return connect_to_camera_pre(s, lgtDepth, ps, v, e, sh) && !occluded(s, sh.org, sh.dir, sh.dist);
 }
 
 // BSDFSampling<adjoint, perturb> (src/path.cpp:608-724). `next` may alias `ps`;
@@ -221,14 +242,16 @@ DEV bool bsdf_sampling(const SceneView &s, const BState &ps, SVert &v, BState &n
 }
 
 // DirectLighting, bidirectional form (src/path.cpp:726-811).
-DEV bool direct_lighting(const SceneView &s, int camDepth, const BState &ps, float sx, float sy, float pickProb,
-                         const SVert &v, Emit &e) {
+DEV bool direct_lighting_pre(const SceneView &s, int camDepth, const BState &ps, float sx, float sy, float pickProb,
+                             const SVert &v, Emit &e, Shadow &sh) {
     V3 dirToLight, lightContrib;
     float dist, cosAtLight, directPdf, emissionPdf;
     if (!light_sample_direct(s, v.dlLight, v.dlPrim, ps.isect.position, v.dl[0], v.dl[1], dirToLight, dist,
                              lightContrib, cosAtLight, directPdf, emissionPdf))
         return false;
-    if (occluded(s, ps.isect.position, dirToLight, dist)) return false;
+    sh.org = ps.isect.position;
+    sh.dir = dirToLight;
+    sh.dist = dist;
     const Bsdf &bsdf = bsdf_of_tri(s, v.tri);
     BsdfOut bo;
     bsdf_evaluate(bsdf, ps.wi, ps.isect.shadingNormal, dirToLight, bo);
@@ -253,6 +276,11 @@ DEV bool direct_lighting(const SceneView &s, int camDepth, const BState &ps, flo
     e.ls = score;
     e.ss = score * ps.ssJacobian;
     return true;
+}
+DEV bool direct_lighting(const SceneView &s, int camDepth, const BState &ps, float sx, float sy, float pickProb,
+                         const SVert &v, Emit &e) {
+    Shadow sh;
+    return direct_lighting_pre(s, camDepth, ps, sx, sy, pickProb, v, e, sh) && !occluded(s, sh.org, sh.dir, sh.dist);
 }
 
 // HandleHitLight, bidirectional form (src/path.cpp:813-865).
@@ -283,13 +311,15 @@ DEV bool handle_hit_light(const SceneView &s, int camDepth, int light, const V3 
 }
 
 // ConnectVertex (src/path.cpp:867-976).
-DEV bool connect_vertex(const SceneView &s, int camDepth, int lgtDepth, const BState &lp, const SVert &lv,
-                        const BState &cp, const SVert &cv, float sx, float sy, Emit &e) {
+DEV bool connect_vertex_pre(const SceneView &s, int camDepth, int lgtDepth, const BState &lp, const SVert &lv,
+                            const BState &cp, const SVert &cv, float sx, float sy, Emit &e, Shadow &sh) {
     V3 dirToLight = lp.isect.position - cp.isect.position;
     const float distSq = length_sq(dirToLight);
     const float dist = sqrtf(distSq);
     dirToLight = dirToLight * (1.0f / dist);
-    if (occluded(s, cp.isect.position, dirToLight, dist)) return false;
+    sh.org = cp.isect.position;
+    sh.dir = dirToLight;
+    sh.dist = dist;
     BsdfOut cb;
     bsdf_evaluate(bsdf_of_tri(s, cv.tri), cp.wi, cp.isect.shadingNormal, dirToLight, cb);
     if (is_zero(cb.contrib)) return false;
@@ -324,17 +354,26 @@ DEV bool connect_vertex(const SceneView &s, int camDepth, int lgtDepth, const BS
     e.ss = score * ssJ;
     return true;
 }
+DEV bool connect_vertex(const SceneView &s, int camDepth, int lgtDepth, const BState &lp, const SVert &lv,
+                        const BState &cp, const SVert &cv, float sx, float sy, Emit &e) {
+    Shadow sh;
+    return connect_vertex_pre(s, camDepth, lgtDepth, lp, lv, cp, cv, sx, sy, e, sh) &&
+           !occluded(s, sh.org, sh.dir, sh.dist);
+}
 
-// LightCoordinateSampling, bidirectional form (src/path.cpp:1430-1478).
-DEV bool light_coordinate_sampling(const SceneView &s, const SVert &cur, int nextTri, BState &ps, V3 &dir,
-                                   V3 &bsdfContrib) {
+// LightCoordinateSampling, bidirectional form (src/path.cpp:1430-1478). The
+// path continues from ps along `dir` only if the shadow ray is clear.
+DEV bool light_coordinate_sampling_pre(const SceneView &s, const SVert &cur, int nextTri, BState &ps, V3 &dir,
+                                       V3 &bsdfContrib, Shadow &sh) {
     V3 nextPos, nextNormal;
     sample_triangle(s, nextTri, cur.rnd[0], cur.rnd[1], nextPos, nextNormal);
     dir = nextPos - ps.isect.position;
     const float distToLightSq = length_sq(dir);
     const float distToLight = sqrtf(distToLightSq);
     dir = dir * (1.0f / distToLight);
-    if (occluded(s, ps.isect.position, dir, distToLight)) return false;
+    sh.org = ps.isect.position;
+    sh.dir = dir;
+    sh.dist = distToLight;
     BsdfOut bo;
     bsdf_evaluate(bsdf_of_tri(s, cur.tri), ps.wi, ps.isect.shadingNormal, dir, bo);
     if (is_zero(bo.contrib)) return false;
@@ -359,8 +398,11 @@ DEV bool russian_roulette(int depth, const V3 &bsdfContrib, float &rrWeight, V3 
 
 // Light-coordinate re-parameterisation when a camera subpath hits an area light
 // (src/path.cpp:1056-1071 and 1208-1223).
-DEV void light_coordinate_convert(const SceneView &s, SVert &prev, int lightTri, const V3 &rayOrg, BState &ps) {
-    triangle_sample_param(s, lightTri, ps.isect.position, prev.rnd[0], prev.rnd[1]);
+// prevRnd0/1: the direction parameters of the previous camera vertex, rewritten
+// as the light triangle's sample parameters.
+DEV void light_coordinate_convert(const SceneView &s, float &prevRnd0, float &prevRnd1, int lightTri,
+                                  const V3 &rayOrg, BState &ps) {
+    triangle_sample_param(s, lightTri, ps.isect.position, prevRnd0, prevRnd1);
     V3 dirToPrev = ps.isect.position - rayOrg;
     const float distSq = length_sq(dirToPrev);
     const float invDistSq = 1.0f / distSq;
@@ -515,7 +557,7 @@ DEV void generate_path_bidir(const SceneView &s, int minDepth, int maxDepth, R &
             if (light >= 0) {
                 if (!hit) v.tri = -1;  // a path that ends on the environment light
                 if (s.opt.useLightCoordinateSampling && d > 1 && s.lights[light].type == kLightArea)
-                    light_coordinate_convert(s, f.cam[d - 1], tri, org, cp);
+                    light_coordinate_convert(s, f.cam[d - 1].rnd[0], f.cam[d - 1].rnd[1], tri, org, cp);
                 Emit e;
                 if (handle_hit_light(s, d, light, dir, f.screen[0], f.screen[1], cp, e)) sink(e);
                 return;
@@ -553,237 +595,443 @@ DEV void generate_path_bidir(const SceneView &s, int minDepth, int maxDepth, R &
     }
 }
 
-// ---------------------------------------------------------------- multiplexed large step
-// GenerateSubpath (src/path.cpp:1123-1269) with bidirMIS = true. Returns true
-// and fills `rec`/`e` when the technique (camLength, lgtLength) contributes.
-template <class R>
-DEV bool generate_subpath(const SceneView &s, int camLength, int lgtLength, R &rng, PathRec &rec, Emit &e) {
-    FullPath f;
-    f.time = rng.uniform();
-    BState lp;
-    zero_state(lp);
-    f.nLgt = 0;
-    f.lgtLight = -1;
-    f.lgtPrim = -1;
-    V3 org, dir;
-    if (lgtLength > 1) {
-        f.lgtPos[1] = rng.uniform();
-        f.lgtPos[0] = rng.uniform();
-        f.lgtDir[1] = rng.uniform();
-        f.lgtDir[0] = rng.uniform();
-        float pickProb;
-        f.lgtLight = pick_light(s, rng.uniform(), pickProb);
-        const Light &L = s.lights[f.lgtLight];
-        const float ud = rng.uniform();
-        f.lgtPrim = L.type == kLightArea ? sample_discrete(s.lightTriCdf + L.triCdfOffset, L.numTris, ud) : -1;
-        emit_from_light(s, pickProb, f.lgtLight, f.lgtPrim, f.lgtPos, f.lgtDir, org, dir, lp);
-        #pragma unroll 1
-        for (int d = 0; d < kMaxFull; d++) {
-            SVert &v = f.lgt[d];
-            clear_vert(v);
-            f.nLgt = d + 1;
-            int tri = -1;
-            const bool hit = intersect(s, org, dir, kIsectEps, INFINITY, tri, lp.isect);
-            v.tri = tri;
-            if (!hit) return false;
-            v.disc = rng.uniform();
-            lp.wi = -dir;
-            convert_mis(s, d, f.lgtLight, org, dir, lp);
-            if (d + 2 == lgtLength) {
-                if (camLength == 1) {
-                    if (!connect_to_camera(s, d, lp, v, e)) return false;
-                    make_rec(f, 1, lgtLength, rec);
-                    return true;
-                }
-                break;
-            }
-            v.rnd[1] = rng.uniform();
-            v.rnd[0] = rng.uniform();
-            V3 bc;
-            if (!bsdf_sampling<true, false>(s, lp, v, lp, false, dir, bc)) return false;
-            v.rr = 1.0f;
-            org = lp.isect.position;
-        }
-    }
-    f.screen[1] = rng.uniform();
-    f.screen[0] = rng.uniform();
-    BState cp;
-    zero_state(cp);
-    float minT, maxT;
-    emit_from_camera(s, f.screen[0], f.screen[1], org, dir, minT, maxT, cp);
-    #pragma unroll 1
-    for (int d = 0; d < kMaxFull; d++) {
-        SVert &v = f.cam[d];
-        clear_vert(v);
-        f.nCam = d + 1;
-        int tri = -1;
-        const bool hit = intersect(s, org, dir, minT, maxT, tri, cp.isect);
-        v.tri = tri;
-        cp.wi = -dir;
-        if (hit) convert_mis(s, d, -1, org, dir, cp);
-        if (d + 2 >= camLength && lgtLength == 0) {
-            const int light = hit ? area_light_of_tri(s, tri) : s.envLight;
-            if (light < 0) return false;
-            if (!hit) v.tri = -1;
-            if (d > 1 && s.lights[light].type == kLightArea)
-                light_coordinate_convert(s, f.cam[d - 1], tri, org, cp);
-            if (!handle_hit_light(s, d, light, dir, f.screen[0], f.screen[1], cp, e)) return false;
-            make_rec(f, camLength, 0, rec);
-            return true;
-        }
-        if (!hit) return false;
-        v.disc = rng.uniform();
-        if (d + 2 == camLength) {
-            bool ok;
-            if (lgtLength == 1) {
-                float dlPick;
-                v.dlLight = pick_light(s, rng.uniform(), dlPick);
-                v.dl[1] = rng.uniform();
-                v.dl[0] = rng.uniform();
-                const Light &L = s.lights[v.dlLight];
-                const float ud = rng.uniform();
-                v.dlPrim = L.type == kLightArea ? sample_discrete(s.lightTriCdf + L.triCdfOffset, L.numTris, ud) : 0;
-                ok = direct_lighting(s, d, cp, f.screen[0], f.screen[1], dlPick, v, e);
-            } else {
-                ok = connect_vertex(s, d, lgtLength - 2, lp, f.lgt[f.nLgt - 1], cp, v, f.screen[0], f.screen[1], e);
-            }
-            if (!ok) return false;
-            make_rec(f, camLength, lgtLength, rec);
-            return true;
-        }
-        v.rnd[1] = rng.uniform();
-        v.rnd[0] = rng.uniform();
-        V3 bc;
-        if (!bsdf_sampling<false, false>(s, cp, v, cp, false, dir, bc)) return false;
-        v.rr = 1.0f;
-        org = cp.isect.position;
-        minT = kIsectEps;
-        maxT = INFINITY;
-    }
-    return false;
+// ---------------------------------------------------------------- path machines
+// The two technique-path samplers of the chain loop -- the multiplexed large
+// step (GenerateSubpath) and the small-step perturbation (PerturbPathBidir) --
+// as resumable state machines. A step advances the path to its next ray cast,
+// leaves that ray in the machine and returns kStepRay; the next step takes the
+// cast's answer (closest hit: the BVH's triangle or -1; shadow ray: 1 if
+// occluded). kStepDone leaves the contribution in m.e; kStepFail means the
+// technique does not contribute. The sequential samplers below answer each ray
+// on the spot; the wavefront sampler (wave.cuh) queues the rays of all chains
+// and answers them with a separate traversal kernel. Both run these same
+// (out-of-line) step functions, so both take identical steps.
+enum : int { kStepRay = 0, kStepDone = 1, kStepFail = 2 };
+enum : int { kRayClosest = 0, kRayAny = 1 };
+
+struct PathM {
+    int pc;                    // resume point
+    int d;                     // vertex index within the subpath being traced
+    int k;                     // next primary coordinate (perturbation)
+    int lastLgtTri;            // triangle of the last light-subpath vertex (ConnectVertex)
+    int lightCoords;           // perturbation: light-coordinate sampling of the last camera segment
+    int camLength, lgtLength;  // large step: the technique
+    int kind;                  // kind of the ray below: kRayClosest | kRayAny
+    float sx, sy;              // screen position of the camera subpath
+    V3 org, dir;               // the ray: closest hit in (tmin, tmax], or a shadow ray over [tmin, tmax]
+    float tmin, tmax;
+    BState lp, cp;             // light / camera subpath states
+    Emit e;                    // the contribution (with kStepDone; before, one awaiting its shadow ray)
+};
+
+DEV int want_closest(PathM &m, int pc, float tmin, float tmax) {
+    m.pc = pc;
+    m.kind = kRayClosest;
+    m.tmin = tmin;
+    m.tmax = tmax;
+    return kStepRay;
+}
+// The shadow ray of Occluded(scene, time, ray, dist) (src/scene.cpp:95-105).
+DEV int want_shadow(PathM &m, int pc, const Shadow &sh) {
+    m.pc = pc;
+    m.kind = kRayAny;
+    m.org = sh.org;
+    m.dir = sh.dir;
+    m.tmin = kIsectEps;
+    m.tmax = isinf(sh.dist) ? INFINITY : (1.0f - kShadowEps) * sh.dist;
+    return kStepRay;
+}
+// The answer to a closest-hit ray: Intersect of src/path.cpp:94-103 after the
+// BVH returned `hit`; `tri` is updated whenever the BVH reports a hit, even if
+// the re-intersection fails.
+DEV bool take_hit(const SceneView &s, const PathM &m, int hit, int &tri, Isect &isect) {
+    if (hit < 0) return false;
+    tri = hit;
+    return reintersect(s, hit, m.org, m.dir, isect);
+}
+// Answers the machine's pending ray on the spot (the sequential samplers).
+DEV int answer_ray(const SceneView &s, const PathM &m) {
+    if (m.kind == kRayAny) return traverse<true>(s, m.org, m.dir, m.tmin, m.tmax) >= 0 ? 1 : 0;
+    return traverse<false>(s, m.org, m.dir, m.tmin, m.tmax);
 }
 
-// ---------------------------------------------------------------- small-step perturbation
-// PerturbPathBidir (src/path.cpp:1480-1628) applied to a technique path.
-// `out` receives the perturbed state (coordinates are perturbed in order and
-// the state keeps whatever was updated before an early exit, as the
-// reference's Path does). Discrete parameters get N(0, discreteStdDev) jitter
-// drawn from `jit`. Returns true with `e` filled if the path contributes.
+// Guarded writes into a path record: a degenerate large step (camLength =
+// lgtLength = 1, which never connects) keeps tracing camera vertices past the
+// record's capacity, as the reference's loop does, and always fails.
+DEV void rec_u(PathRec &r, int i, float v) {
+    if (i >= 0 && i < kMaxDim) r.u[i] = v;
+}
+DEV void rec_clear_vert(PathRec &r, int vi, int tri) {
+    if (vi >= kMaxVerts) return;
+    r.tri[vi] = tri;
+    r.disc[vi] = 0.0f;
+    r.rr[vi] = 0.0f;
+    r.useAbs &= ~(1u << vi);
+}
+
+// ---- multiplexed large step: GenerateSubpath (src/path.cpp:1123-1269) with
+// bidirMIS = true for the technique (m.camLength, m.lgtLength). The path record
+// is written as the path is built, in the layout Path::Initialize and
+// GetPathPos give it (src/path.h:109-120, src/path.cpp:2393-2439): light
+// vertices first, u = light position / direction, light-vertex directions,
+// screen position, camera-vertex directions, direct-light sample.
+enum : int { kGStart = 0, kGLgtHit, kGCamStart, kGCamHit, kGFinalShadow };
+
+template <class R>
+DEV_SHARED int subpath_step(const SceneView &s, R &rng, PathRec &rec, PathM &m, int hit) {
+    const int camLength = m.camLength, lgtLength = m.lgtLength;
+    const int nl = n_lgt(lgtLength);
+    const int camBase = lgtLength > 1 ? 2 * nl + 2 : 0;  // u index of the screen position
+    for (;;) {
+        switch (m.pc) {
+            case kGStart: {
+                rng.uniform();  // time
+                zero_state(m.lp);
+                rec.c = camLength;
+                rec.l = lgtLength;
+                rec.lgtLight = -1;
+                rec.lgtPrim = -1;
+                rec.dlLight = -1;
+                rec.dlPrim = -1;
+                rec.useAbs = 0u;
+                m.lastLgtTri = -1;
+                if (lgtLength > 1) {
+                    // EmitFromLightInit: position then direction, second components first
+                    rec.u[1] = rng.uniform();
+                    rec.u[0] = rng.uniform();
+                    rec.u[3] = rng.uniform();
+                    rec.u[2] = rng.uniform();
+                    float pickProb;
+                    rec.lgtLight = pick_light(s, rng.uniform(), pickProb);
+                    const Light &L = s.lights[rec.lgtLight];
+                    const float ud = rng.uniform();
+                    rec.lgtPrim = L.type == kLightArea ? sample_discrete(s.lightTriCdf + L.triCdfOffset, L.numTris, ud) : -1;
+                    const float pos[2] = {rec.u[0], rec.u[1]};
+                    const float dirp[2] = {rec.u[2], rec.u[3]};
+                    emit_from_light(s, pickProb, rec.lgtLight, rec.lgtPrim, pos, dirp, m.org, m.dir, m.lp);
+                    m.d = 0;
+                    return want_closest(m, kGLgtHit, kIsectEps, INFINITY);
+                }
+                m.pc = kGCamStart;
+                continue;
+            }
+            case kGLgtHit: {
+                const int d = m.d;
+                SVert v;
+                clear_vert(v);
+                int tri = -1;
+                const bool okH = take_hit(s, m, hit, tri, m.lp.isect);
+                v.tri = tri;
+                rec_clear_vert(rec, d, tri);
+                if (!okH) return kStepFail;
+                v.disc = rng.uniform();
+                rec.disc[d] = v.disc;
+                m.lp.wi = -m.dir;
+                convert_mis(s, d, rec.lgtLight, m.org, m.dir, m.lp);
+                if (d + 2 == lgtLength) {
+                    if (camLength == 1) {
+                        Shadow sh;
+                        if (!connect_to_camera_pre(s, d, m.lp, v, m.e, sh)) return kStepFail;
+                        return want_shadow(m, kGFinalShadow, sh);
+                    }
+                    m.lastLgtTri = v.tri;
+                    m.pc = kGCamStart;
+                    continue;
+                }
+                v.rnd[1] = rng.uniform();
+                v.rnd[0] = rng.uniform();
+                V3 bc;
+                const bool okS = bsdf_sampling<true, false>(s, m.lp, v, m.lp, false, m.dir, bc);
+                rec_u(rec, 4 + 2 * d, v.rnd[0]);  // as sampled, or re-parameterised (absolute parameters)
+                rec_u(rec, 5 + 2 * d, v.rnd[1]);
+                if (v.useAbs) rec.useAbs |= 1u << d;
+                if (!okS) return kStepFail;
+                rec.rr[d] = 1.0f;
+                m.org = m.lp.isect.position;
+                m.d = d + 1;
+                if (m.d >= kMaxFull) {  // the reference's vertex bound (unreachable for lgtLength <= 12)
+                    m.pc = kGCamStart;
+                    continue;
+                }
+                return want_closest(m, kGLgtHit, kIsectEps, INFINITY);
+            }
+            case kGCamStart: {
+                m.sy = rng.uniform();
+                m.sx = rng.uniform();
+                rec_u(rec, camBase, m.sx);
+                rec_u(rec, camBase + 1, m.sy);
+                zero_state(m.cp);
+                float minT, maxT;
+                emit_from_camera(s, m.sx, m.sy, m.org, m.dir, minT, maxT, m.cp);
+                m.d = 0;
+                return want_closest(m, kGCamHit, minT, maxT);
+            }
+            case kGCamHit: {
+                const int d = m.d, vi = nl + d;
+                SVert v;
+                clear_vert(v);
+                int tri = -1;
+                const bool okH = take_hit(s, m, hit, tri, m.cp.isect);
+                v.tri = tri;
+                rec_clear_vert(rec, vi, tri);
+                m.cp.wi = -m.dir;
+                if (okH) convert_mis(s, d, -1, m.org, m.dir, m.cp);
+                if (d + 2 >= camLength && lgtLength == 0) {
+                    const int light = okH ? area_light_of_tri(s, tri) : s.envLight;  // GetHitLight
+                    if (light < 0) return kStepFail;
+                    if (!okH) rec_clear_vert(rec, vi, -1);  // a path that ends on the environment light
+                    if (d > 1 && s.lights[light].type == kLightArea)
+                        light_coordinate_convert(s, rec.u[camBase + 2 * d], rec.u[camBase + 2 * d + 1], tri, m.org,
+                                                 m.cp);
+                    return handle_hit_light(s, d, light, m.dir, m.sx, m.sy, m.cp, m.e) ? kStepDone : kStepFail;
+                }
+                if (!okH) return kStepFail;
+                v.disc = rng.uniform();
+                if (vi < kMaxVerts) rec.disc[vi] = v.disc;
+                if (d + 2 == camLength) {
+                    Shadow sh;
+                    bool okC;
+                    if (lgtLength == 1) {
+                        float dlPick;
+                        v.dlLight = pick_light(s, rng.uniform(), dlPick);
+                        v.dl[1] = rng.uniform();
+                        v.dl[0] = rng.uniform();
+                        const Light &L = s.lights[v.dlLight];
+                        const float ud = rng.uniform();
+                        v.dlPrim = L.type == kLightArea ? sample_discrete(s.lightTriCdf + L.triCdfOffset, L.numTris, ud) : 0;
+                        rec.dlLight = v.dlLight;
+                        rec.dlPrim = v.dlPrim;
+                        rec_u(rec, camBase + 2 * d + 2, v.dl[0]);
+                        rec_u(rec, camBase + 2 * d + 3, v.dl[1]);
+                        okC = direct_lighting_pre(s, d, m.cp, m.sx, m.sy, dlPick, v, m.e, sh);
+                    } else {
+                        SVert lv;
+                        clear_vert(lv);
+                        lv.tri = m.lastLgtTri;
+                        okC = connect_vertex_pre(s, d, lgtLength - 2, m.lp, lv, m.cp, v, m.sx, m.sy, m.e, sh);
+                    }
+                    if (!okC) return kStepFail;
+                    return want_shadow(m, kGFinalShadow, sh);
+                }
+                v.rnd[1] = rng.uniform();
+                v.rnd[0] = rng.uniform();
+                V3 bc;
+                const bool okS = bsdf_sampling<false, false>(s, m.cp, v, m.cp, false, m.dir, bc);
+                rec_u(rec, camBase + 2 + 2 * d, v.rnd[0]);
+                rec_u(rec, camBase + 3 + 2 * d, v.rnd[1]);
+                if (v.useAbs && vi < kMaxVerts) rec.useAbs |= 1u << vi;
+                if (!okS) return kStepFail;
+                if (vi < kMaxVerts) rec.rr[vi] = 1.0f;
+                m.org = m.cp.isect.position;
+                m.d = d + 1;
+                if (m.d >= kMaxFull) return kStepFail;  // the reference's vertex bound
+                return want_closest(m, kGCamHit, kIsectEps, INFINITY);
+            }
+            case kGFinalShadow:
+                return hit ? kStepFail : kStepDone;
+            default:
+                return kStepFail;
+        }
+    }
+}
+
+// ---- small-step perturbation: PerturbPathBidir (src/path.cpp:1480-1628) of the
+// technique path `in` by `offset`, into `out`. Coordinates are perturbed in
+// order and `out` keeps whatever was updated before an early exit, as the
+// reference's Path does. Discrete parameters get N(0, discreteStdDev) jitter
+// drawn from `jit`.
+enum : int { kPStart = 0, kPLgtHit, kPCamStart, kPCamHit, kPLcsShadow, kPCamNext, kPFinalShadow };
+
 template <class J>
-DEV bool perturb_path(const SceneView &s, const PathRec &in, const float *offset, J &jit, PathRec &out, Emit &e) {
-    out = in;
+DEV_SHARED int perturb_step(const SceneView &s, const PathRec &in, const float *offset, J &jit, PathRec &out,
+                            PathM &m, int hit) {
     const int c = in.c, l = in.l;
     const int nl = n_lgt(l), nc = c - 1;
     const float sd = s.opt.discreteStdDev;
-    int k = 0;
-    BState lp;
-    zero_state(lp);
-    SVert lastLgt;
-    clear_vert(lastLgt);
-    if (l > 1) {
-        const float pickProb = pick_light_prob(s, in.lgtLight);
-        for (int i = 0; i < 4; i++, k++) out.u[k] = mod1(in.u[k] + offset[k]);
-        const float pos[2] = {out.u[0], out.u[1]};
-        const float dirp[2] = {out.u[2], out.u[3]};
-        V3 org, dir;
-        emit_from_light(s, pickProb, in.lgtLight, in.lgtPrim, pos, dirp, org, dir, lp);
-        #pragma unroll 1
-        for (int d = 0; d < nl; d++) {
-            SVert v;
-            clear_vert(v);
-            v.tri = out.tri[d];
-            int tri = v.tri;
-            const bool hit = intersect(s, org, dir, kIsectEps, INFINITY, tri, lp.isect);
-            out.tri[d] = tri;
-            v.tri = tri;
-            if (!hit) return false;
-            lp.wi = -dir;
-            out.disc[d] = mod1(out.disc[d] + (sd > 0.0f ? sd * jit.normal() : 0.0f));
-            v.disc = out.disc[d];
-            convert_mis(s, d, in.lgtLight, org, dir, lp);
-            if (d == nl - 1 && c == 1) return connect_to_camera(s, d, lp, v, e);
-            if (d == nl - 1) {
-                lastLgt = v;
-                break;
+    for (;;) {
+        switch (m.pc) {
+            case kPStart: {
+                out = in;
+                m.k = 0;
+                zero_state(m.lp);
+                m.lastLgtTri = -1;
+                if (l > 1) {
+                    const float pickProb = pick_light_prob(s, in.lgtLight);
+                    for (int i = 0; i < 4; i++) out.u[i] = mod1(in.u[i] + offset[i]);
+                    m.k = 4;
+                    const float pos[2] = {out.u[0], out.u[1]};
+                    const float dirp[2] = {out.u[2], out.u[3]};
+                    emit_from_light(s, pickProb, in.lgtLight, in.lgtPrim, pos, dirp, m.org, m.dir, m.lp);
+                    m.d = 0;
+                    return want_closest(m, kPLgtHit, kIsectEps, INFINITY);
+                }
+                m.pc = kPCamStart;
+                continue;
             }
-            out.u[k] = mod1(in.u[k] + offset[k]);
-            out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
-            v.rnd[0] = out.u[k];
-            v.rnd[1] = out.u[k + 1];
-            k += 2;
-            V3 bc;
-            const bool ok = bsdf_sampling<true, true>(s, lp, v, lp, false, dir, bc);
-            if (v.useAbs) out.useAbs |= 1u << d; else out.useAbs &= ~(1u << d);
-            if (!ok) return false;
-            lp.throughput = lp.throughput * out.rr[d];
-            org = lp.isect.position;
-        }
-    }
-    out.u[k] = mod1(in.u[k] + offset[k]);
-    out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
-    const float sx = out.u[k], sy = out.u[k + 1];
-    k += 2;
-    V3 org, dir;
-    float minT, maxT;
-    BState cp;
-    zero_state(cp);
-    emit_from_camera(s, sx, sy, org, dir, minT, maxT, cp);
-    bool lightCoords = false;
-    #pragma unroll 1
-    for (int d = 0; d < nc; d++) {
-        const int vi = nl + d;
-        SVert v;
-        clear_vert(v);
-        int tri = out.tri[vi];
-        const bool hit = intersect(s, org, dir, minT, maxT, tri, cp.isect);
-        out.tri[vi] = tri;
-        v.tri = tri;
-        cp.wi = -dir;
-        if (hit) convert_mis(s, d, -1, org, dir, cp);
-        if (d == nc - 1 && l == 0) {
-            const int light = hit ? area_light_of_tri(s, tri) : s.envLight;
-            if (light < 0) return false;
-            if (!hit) out.tri[vi] = -1;  // the path ends on the environment light
-            return handle_hit_light(s, d, light, dir, sx, sy, cp, e);
-        }
-        if (!hit) return false;
-        out.disc[vi] = mod1(out.disc[vi] + (sd > 0.0f ? sd * jit.normal() : 0.0f));
-        v.disc = out.disc[vi];
-        if (d == nc - 1) {
-            if (l == 1) {
+            case kPLgtHit: {
+                const int d = m.d;
+                SVert v;
+                clear_vert(v);
+                int tri = out.tri[d];
+                const bool okH = take_hit(s, m, hit, tri, m.lp.isect);
+                out.tri[d] = tri;
+                v.tri = tri;
+                if (!okH) return kStepFail;
+                m.lp.wi = -m.dir;
+                out.disc[d] = mod1(out.disc[d] + (sd > 0.0f ? sd * jit.normal() : 0.0f));
+                v.disc = out.disc[d];
+                convert_mis(s, d, in.lgtLight, m.org, m.dir, m.lp);
+                if (d == nl - 1 && c == 1) {
+                    Shadow sh;
+                    if (!connect_to_camera_pre(s, d, m.lp, v, m.e, sh)) return kStepFail;
+                    return want_shadow(m, kPFinalShadow, sh);
+                }
+                if (d == nl - 1) {
+                    m.lastLgtTri = v.tri;
+                    m.pc = kPCamStart;
+                    continue;
+                }
+                const int k = m.k;
                 out.u[k] = mod1(in.u[k] + offset[k]);
                 out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
-                v.dlLight = in.dlLight;
-                v.dlPrim = in.dlPrim;
-                v.dl[0] = out.u[k];
-                v.dl[1] = out.u[k + 1];
-                return direct_lighting(s, d, cp, sx, sy, pick_light_prob(s, in.dlLight), v, e);
+                v.rnd[0] = out.u[k];
+                v.rnd[1] = out.u[k + 1];
+                m.k = k + 2;
+                V3 bc;
+                const bool okS = bsdf_sampling<true, true>(s, m.lp, v, m.lp, false, m.dir, bc);
+                if (v.useAbs) out.useAbs |= 1u << d; else out.useAbs &= ~(1u << d);
+                if (!okS) return kStepFail;
+                m.lp.throughput = m.lp.throughput * out.rr[d];
+                m.org = m.lp.isect.position;
+                m.d = d + 1;
+                return want_closest(m, kPLgtHit, kIsectEps, INFINITY);
             }
-            return connect_vertex(s, d, nl - 1, lp, lastLgt, cp, v, sx, sy, e);
+            case kPCamStart: {
+                const int k = m.k;
+                out.u[k] = mod1(in.u[k] + offset[k]);
+                out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
+                m.sx = out.u[k];
+                m.sy = out.u[k + 1];
+                m.k = k + 2;
+                zero_state(m.cp);
+                float minT, maxT;
+                emit_from_camera(s, m.sx, m.sy, m.org, m.dir, minT, maxT, m.cp);
+                m.lightCoords = 0;
+                m.d = 0;
+                if (nc <= 0) return kStepFail;
+                return want_closest(m, kPCamHit, minT, maxT);
+            }
+            case kPCamHit: {
+                const int d = m.d, vi = nl + d;
+                SVert v;
+                clear_vert(v);
+                int tri = out.tri[vi];
+                const bool okH = take_hit(s, m, hit, tri, m.cp.isect);
+                out.tri[vi] = tri;
+                v.tri = tri;
+                m.cp.wi = -m.dir;
+                if (okH) convert_mis(s, d, -1, m.org, m.dir, m.cp);
+                if (d == nc - 1 && l == 0) {
+                    const int light = okH ? area_light_of_tri(s, tri) : s.envLight;
+                    if (light < 0) return kStepFail;
+                    if (!okH) out.tri[vi] = -1;  // the path ends on the environment light
+                    return handle_hit_light(s, d, light, m.dir, m.sx, m.sy, m.cp, m.e) ? kStepDone : kStepFail;
+                }
+                if (!okH) return kStepFail;
+                out.disc[vi] = mod1(out.disc[vi] + (sd > 0.0f ? sd * jit.normal() : 0.0f));
+                v.disc = out.disc[vi];
+                if (d == nc - 1) {
+                    Shadow sh;
+                    bool okC;
+                    if (l == 1) {
+                        const int k = m.k;
+                        out.u[k] = mod1(in.u[k] + offset[k]);
+                        out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
+                        v.dlLight = in.dlLight;
+                        v.dlPrim = in.dlPrim;
+                        v.dl[0] = out.u[k];
+                        v.dl[1] = out.u[k + 1];
+                        okC = direct_lighting_pre(s, d, m.cp, m.sx, m.sy, pick_light_prob(s, in.dlLight), v, m.e, sh);
+                    } else {
+                        SVert lv;
+                        clear_vert(lv);
+                        lv.tri = m.lastLgtTri;
+                        okC = connect_vertex_pre(s, d, nl - 1, m.lp, lv, m.cp, v, m.sx, m.sy, m.e, sh);
+                    }
+                    if (!okC) return kStepFail;
+                    return want_shadow(m, kPFinalShadow, sh);
+                }
+                const int k = m.k;
+                out.u[k] = mod1(in.u[k] + offset[k]);
+                out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
+                v.rnd[0] = out.u[k];
+                v.rnd[1] = out.u[k + 1];
+                m.k = k + 2;
+                if (s.opt.useLightCoordinateSampling && d == nc - 2 && l == 0) {
+                    const int lastTri = in.tri[nl + nc - 1];
+                    if (lastTri >= 0 && area_light_of_tri(s, lastTri) >= 0) m.lightCoords = 1;
+                }
+                V3 bc;
+                if (m.lightCoords) {
+                    // the next segment aims at the light triangle; its shadow ray
+                    // leaves from the vertex along the new direction (m.org, m.dir)
+                    Shadow sh;
+                    if (!light_coordinate_sampling_pre(s, v, in.tri[nl + nc - 1], m.cp, m.dir, bc, sh))
+                        return kStepFail;
+                    return want_shadow(m, kPLcsShadow, sh);
+                }
+                const bool okS = bsdf_sampling<false, true>(s, m.cp, v, m.cp, false, m.dir, bc);
+                if (v.useAbs) out.useAbs |= 1u << vi; else out.useAbs &= ~(1u << vi);
+                if (!okS) return kStepFail;
+                m.pc = kPCamNext;
+                continue;
+            }
+            case kPLcsShadow:
+                if (hit) return kStepFail;  // occluded
+                m.pc = kPCamNext;
+                continue;
+            case kPCamNext: {
+                // after sampling camera vertex d: the segment to vertex d + 1
+                m.cp.throughput = m.cp.throughput * out.rr[nl + m.d];
+                m.org = m.cp.isect.position;
+                m.d += 1;
+                if (m.d >= nc) return kStepFail;
+                return want_closest(m, kPCamHit, kIsectEps, INFINITY);
+            }
+            case kPFinalShadow:
+                return hit ? kStepFail : kStepDone;
+            default:
+                return kStepFail;
         }
-        out.u[k] = mod1(in.u[k] + offset[k]);
-        out.u[k + 1] = mod1(in.u[k + 1] + offset[k + 1]);
-        v.rnd[0] = out.u[k];
-        v.rnd[1] = out.u[k + 1];
-        k += 2;
-        if (s.opt.useLightCoordinateSampling && d == nc - 2 && l == 0) {
-            const int lastTri = in.tri[nl + nc - 1];
-            if (lastTri >= 0 && area_light_of_tri(s, lastTri) >= 0) lightCoords = true;
-        }
-        V3 bc;
-        if (lightCoords) {
-            if (!light_coordinate_sampling(s, v, in.tri[nl + nc - 1], cp, dir, bc)) return false;
-        } else {
-            const bool ok = bsdf_sampling<false, true>(s, cp, v, cp, false, dir, bc);
-            if (v.useAbs) out.useAbs |= 1u << vi; else out.useAbs &= ~(1u << vi);
-            if (!ok) return false;
-        }
-        cp.throughput = cp.throughput * out.rr[vi];
-        org = cp.isect.position;
-        minT = kIsectEps;
-        maxT = INFINITY;
     }
-    return false;
+}
+
+// Sequential samplers: the machines with every ray answered on the spot.
+// GenerateSubpath: true and `rec` / `e` filled when technique (camLength,
+// lgtLength) contributes (on failure `rec` holds a partial path).
+template <class R>
+DEV bool generate_subpath(const SceneView &s, int camLength, int lgtLength, R &rng, PathRec &rec, Emit &e) {
+    PathM m;
+    m.pc = kGStart;
+    m.camLength = camLength;
+    m.lgtLength = lgtLength;
+    int hit = -1, st;
+    while ((st = subpath_step(s, rng, rec, m, hit)) == kStepRay) hit = answer_ray(s, m);
+    if (st != kStepDone) return false;
+    e = m.e;
+    return true;
+}
+
+// PerturbPathBidir: true with `e` filled if the perturbed path contributes.
+template <class J>
+DEV bool perturb_path(const SceneView &s, const PathRec &in, const float *offset, J &jit, PathRec &out, Emit &e) {
+    PathM m;
+    m.pc = kPStart;
+    int hit = -1, st;
+    while ((st = perturb_step(s, in, offset, jit, out, m, hit)) == kStepRay) hit = answer_ray(s, m);
+    if (st != kStepDone) return false;
+    e = m.e;
+    return true;
 }
 
 // ---------------------------------------------------------------- direct-lighting pass

@@ -62,7 +62,7 @@ class Options(C.Structure):
                 ("seed", C.c_uint64), ("device", C.c_int32), ("use_graph", C.c_int32),
                 ("chain_groups", C.c_int32), ("stage_lanes", C.c_int32), ("deriv_warps", C.c_int32),
                 ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32),
-                ("graph_iters", C.c_int32)]
+                ("graph_iters", C.c_int32), ("wavefront", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -91,6 +91,10 @@ PATH_DTYPE = np.dtype([("c", "<i4"), ("l", "<i4"), ("lgt_light", "<i4"), ("lgt_p
                        ("disc", "<f4", (MAX_LEN,)), ("rr", "<f4", (MAX_LEN,))])
 CONTRIB_DTYPE = np.dtype([("screen", "<f4", (2,)), ("rgb", "<f4", (3,)), ("ls", "<f4"),
                           ("ss", "<f4"), ("valid", "<i4")])
+DR_RESULT_DTYPE = np.dtype([("a1", "<f4"), ("ss_y", "<f4"), ("ss_z", "<f4"), ("valid_y", "<i4"), ("valid_z", "<i4"),
+                            ("a2", "<f4"), ("log_ratio", "<f8"), ("a_star_green", "<f4"), ("alpha2_green", "<f4"),
+                            ("alpha2_mira", "<f4"), ("pad", "<i4"), ("log_q_mira", "<f8")])
+assert DR_RESULT_DTYPE.itemsize == 56
 assert PATH_DTYPE.itemsize == C.sizeof(Path)
 assert CONTRIB_DTYPE.itemsize == C.sizeof(Contrib)
 
@@ -108,6 +112,7 @@ _SIGS = {
     "drmlt_get_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                           C.POINTER(C.c_int)]),
     "drmlt_get_partial_film": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "drmlt_get_wavefront": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "drmlt_write_exr": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_void_p]),
     "drmlt_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "drmlt_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
@@ -122,6 +127,10 @@ _SIGS = {
     "drmlt_perturb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "drmlt_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "drmlt_dr_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_void_p]),
+    "drmlt_large_step_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "drmlt_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_int, C.c_int,
                                    C.c_void_p, C.c_void_p]),
     "drmlt_compute_gaussian": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,

@@ -137,8 +137,12 @@ class Renderer:
         """drmlt_get_launch_shape: the shape the next run uses."""
         v = [C.c_int() for _ in range(4)]
         capi.check(capi.lib().drmlt_get_launch_shape(self.handle, *(C.byref(x) for x in v)))
-        return dict(zip(("chains_per_warp", "stage2_chains_per_warp", "derivative_warps", "graph_iterations"),
-                        (x.value for x in v)))
+        shape = dict(zip(("chains_per_warp", "stage2_chains_per_warp", "derivative_warps", "graph_iterations"),
+                         (x.value for x in v)))
+        w = C.c_int()
+        capi.check(capi.lib().drmlt_get_wavefront(self.handle, C.byref(w)))
+        shape["wavefront"] = w.value
+        return shape
 
     def fma_benchmark(self, fp64: bool = False, iterations: int | None = None) -> dict:
         """drmlt_fma_benchmark: the device's FP32 or FP64 FMA throughput."""
@@ -225,6 +229,44 @@ class Renderer:
                                             capi.ptr(ll), mc, capi.ptr(cnt), capi.ptr(tech), capi.ptr(ct),
                                             capi.ptr(pth), capi.ptr(cons)))
         return cnt, tech, ct, pth, cons
+
+    def dr_eval(self, paths, contribs, offset1, offset2, aniso):
+        """drmlt_dr_eval: per-stage acceptances of one DR iteration from states
+        `paths` (with contributions) for given first / second-stage offsets.
+        Returns (results, y paths, z paths)."""
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        contribs = np.ascontiguousarray(contribs, capi.CONTRIB_DTYPE)
+        o1 = np.ascontiguousarray(offset1, np.float32).reshape(n, capi.MAX_DIM)
+        o2 = np.ascontiguousarray(offset2, np.float32).reshape(n, capi.MAX_DIM)
+        an = np.ascontiguousarray(aniso, np.int32)
+        out = np.zeros(n, capi.DR_RESULT_DTYPE)
+        y = np.zeros(n, capi.PATH_DTYPE)
+        z = np.zeros(n, capi.PATH_DTYPE)
+        capi.check(capi.lib().drmlt_dr_eval(self.handle, n, capi.ptr(paths), capi.ptr(contribs), capi.ptr(o1),
+                                            capi.ptr(o2), capi.ptr(an), capi.ptr(out), capi.ptr(y), capi.ptr(z)))
+        return out, y, z
+
+    def large_step_eval(self, tapes, paths, contribs, length_func):
+        """drmlt_large_step_eval: (a1, technique (n x 2), contributions, uniforms consumed)."""
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        stride = max(1, max(len(t) for t in tapes))
+        T = np.zeros((n, stride), np.float32)
+        lens = np.zeros(n, np.int32)
+        for i, t in enumerate(tapes):
+            T[i, :len(t)] = t
+            lens[i] = len(t)
+        contribs = np.ascontiguousarray(contribs, capi.CONTRIB_DTYPE)
+        lf = np.ascontiguousarray(length_func, np.float32)
+        a1 = np.zeros(n, np.float32)
+        tech = np.zeros((n, 2), np.int32)
+        ct = np.zeros(n, capi.CONTRIB_DTYPE)
+        cons = np.zeros(n, np.int32)
+        capi.check(capi.lib().drmlt_large_step_eval(self.handle, n, capi.ptr(T), capi.ptr(lens), stride,
+                                                    capi.ptr(paths), capi.ptr(contribs), capi.ptr(lf), len(lf),
+                                                    capi.ptr(a1), capi.ptr(tech), capi.ptr(ct), capi.ptr(cons)))
+        return a1, tech, ct, cons
 
     def trace_rays(self, org, dirs, tmin=1e-3, tmax=float("inf"), any_hit=False):
         org = np.ascontiguousarray(org, np.float32).reshape(-1, 3)

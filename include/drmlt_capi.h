@@ -135,6 +135,11 @@ typedef struct drmlt_options {
     int32_t graph_iters;          /* iterations per CUDA graph launch, 1..8 (0 = 1; drmlt_autotune may
                                      switch between 1 and 4). Iterations short of a whole graph at
                                      the end of a run are launched without the graph. */
+    int32_t wavefront;            /* path tracing of stage 1, stage 2 and Green's y*: 1 = wavefront
+                                     rounds (rays of all chains queued per bounce and traced by a
+                                     separate full-warp traversal kernel), 0 = one chain per lane
+                                     traces its whole path; -1 = default (1). Both take identical
+                                     steps; drmlt_autotune times both. */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
@@ -218,10 +223,12 @@ int drmlt_kernel_launches(void *handle, int64_t *n);
 
 /* Launch-shape autotuner (after drmlt_prepass): after one untimed run of
  * `iterations_per_candidate` iterations, times that many iterations of the
- * render under each candidate chains-per-warp count of the per-chain stage
- * kernels (2, 4, 8, 16, 32), in two passes of opposite order, then each
- * derivative team size (1, 2, 4 warps) the same way (CUDA events), and keeps
- * the fastest pair (written to the outputs, which may be NULL): 17 runs. With
+ * render under wavefront and per-lane path tracing, then under each candidate
+ * chains-per-warp count of the per-chain kernels (2, 4, 8, 16, 32), then each
+ * derivative team size (1, 2, 4 warps), every choice in two passes of opposite
+ * order (CUDA events), and keeps the fastest (chains per warp and team size
+ * written to the outputs, which may be NULL; the wavefront choice is reported
+ * by drmlt_get_launch_shape): 21 runs. With
  * CUDA graphs on and iterations_per_candidate a multiple of 4 it then times
  * graphs of 1 and of 4 iterations (4 more runs) and keeps the faster.
  * The iterations count toward the render; the launch shape does not change the
@@ -231,8 +238,10 @@ int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes,
 /* The launch shape the next drmlt_run uses (after drmlt_autotune: the tuned
  * one): chains per warp of the stage kernels and of the second-stage list
  * kernels, warps per derivative team, iterations per CUDA graph launch (0 when
- * graphs are off). Any output may be NULL. */
+ * graphs are off). Any output may be NULL. drmlt_get_wavefront gives the path
+ * tracing schedule (1 wavefront rounds, 0 one chain per lane). */
 int drmlt_get_launch_shape(void *handle, int *stage_lanes, int *stage2_lanes, int *deriv_warps, int *graph_iters);
+int drmlt_get_wavefront(void *handle, int *wavefront);
 
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
  * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,
@@ -271,6 +280,62 @@ int drmlt_perturb(void *handle, const drmlt_path *in, const float *offset, int n
 int drmlt_replay(void *handle, int mode, const float *tapes, const int32_t *tape_len, int stride, int n,
                  const int32_t *cam_len, const int32_t *lgt_len, int max_contribs, int32_t *out_count,
                  int32_t *out_tech, drmlt_contrib *out_contrib, drmlt_path *out_path, int32_t *out_consumed);
+
+/* The acceptance quantities of one delayed-rejection iteration from a current
+ * state x with the proposals' offsets given (for the parity tests; the chain
+ * loop computes the same quantities with the same device code):
+ *   a1          first-stage acceptance of y = PerturbPathBidir(x, offset1):
+ *               Clamp(ss(y) / ss(x), 0, 1), 0 when y does not contribute or the
+ *               value is invalid (SmallStep::Mutate, src/mutation.cpp:126-166;
+ *               delayed.cpp:430-437)
+ *   a2          second-stage ratio for z = PerturbPathBidir(x, offset2): with
+ *               aniso = 0 the isotropic Clamp(ss(z) / ss(x), 0, 1)
+ *               (mutation.cpp:167-208), with aniso = 1 the unclamped H2MC ratio
+ *               exp(log_ratio) ss(z) / ss(x) (PH2MCSmallStep::Mutate,
+ *               drsmallstep.cpp:169-196); 0 when z does not contribute
+ *   log_ratio   H2MC: log N_z(-offset2) - log N_x(offset2), the Gaussians at x
+ *               and z from the path derivatives (gated like the chain loop by
+ *               max_derivative_depth and ss), in FP64
+ *   a_star_green acceptance of Green's reverse path y* = PerturbPathBidir(z,
+ *               x - y) from z (SmallStep::Trace, mutation.cpp:210-238; 0 when z
+ *               does not contribute)
+ *   log_q_mira  log Q1(z, y) / Q1(x, y), Mira's isotropic kernel ratio with
+ *               sigma = perturb_stddev (delayed.cpp:512-523), in FP64
+ *   alpha2_green, alpha2_mira  the second-stage acceptance probabilities of
+ *               Green & Mira and of Tierney & Mira (delayed.cpp:466-541)
+ * y and z are evaluated with the discrete jitter off. */
+typedef struct drmlt_dr_result {
+    float a1;
+    float ss_y, ss_z;
+    int32_t valid_y, valid_z;
+    float a2;
+    double log_ratio;
+    float a_star_green;
+    float alpha2_green, alpha2_mira;
+    int32_t pad;
+    double log_q_mira;
+} drmlt_dr_result;
+
+/* Per-stage acceptances (above) for n current states x (paths and their
+ * contributions: ss and ls are used), offsets (DRMLT_MAX_DIM stride) and the
+ * second stage's kind per state (aniso[i]: 0 isotropic, 1 H2MC). The
+ * first-stage proposals y and second-stage proposals z are written to y_out /
+ * z_out (may be NULL). */
+int drmlt_dr_eval(void *handle, int n, const drmlt_path *x, const drmlt_contrib *x_contrib, const float *offset1,
+                  const float *offset2, const int32_t *aniso, drmlt_dr_result *out, drmlt_path *y_out,
+                  drmlt_path *z_out);
+
+/* LargeStep::Mutate (src/mutation.cpp:7-120, multiplexed, bidirectional) on n
+ * recorded uniform streams (stride floats each, tape_len[i] used): the path
+ * length from the distribution of per-length weights length_func[num_lengths]
+ * (PiecewiseConstant1D), the light subpath length, GenerateSubpath and the
+ * contribution pick, then the acceptance against the current state x[i] (its
+ * technique and ls). Writes a1, the proposal's technique (c, l; 0, 0 when it
+ * does not contribute), its contribution and the uniforms consumed. */
+int drmlt_large_step_eval(void *handle, int n, const float *tapes, const int32_t *tape_len, int stride,
+                          const drmlt_path *x, const drmlt_contrib *x_contrib, const float *length_func,
+                          int num_lengths, float *a1, int32_t *out_tech, drmlt_contrib *out_contrib,
+                          int32_t *out_consumed);
 
 /* Closest-hit (any_hit = 0) or occlusion (any_hit = 1) ray casts against the
  * scene BVH, the rtcIntersect / rtcOccluded calls of src/scene.cpp:80-111.

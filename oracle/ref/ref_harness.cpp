@@ -16,7 +16,7 @@
 // the continuous offsets move the path.
 //
 // usage: ref_harness <scene.xml> <libdir> <maxDervDepth> <out.jsonl> <mode> <seed0> <count> [extra]
-//   mode = camera | bidir | subpath | direct | tech | mesh
+//   mode = camera | bidir | subpath | direct | tech | accept | mesh
 //   (mesh: every shape's triangles as loaded by ParseObj / LoadSerialized,
 //    src/parseobj.cpp:148-264, src/loadserialized.cpp:236-317)
 #include "parsescene.h"
@@ -28,6 +28,8 @@
 #include "camera.h"
 #include "gaussian.h"
 #include "integrators/delayed/drsmallstep.h"
+#include "mutation.h"
+#include "distribution.h"
 #include "texturesystem.h"
 #include <cstdio>
 #include <unistd.h>
@@ -340,6 +342,190 @@ void ModeTech(uint64_t seed0, int count, int nPerturb, const PathFuncLib &lib, i
     }
 }
 
+// Per-stage acceptances of one delayed-rejection iteration, from the
+// reference's own mutation code on fixed current states with recorded draws.
+// For each technique path x (bootstrap samples, as in ModeTech):
+//   large   LargeStep::Mutate (src/mutation.cpp:7-120) on a recorded uniform
+//           stream with a fixed path-length distribution: its proposal and a1;
+//   small   SmallStep::Mutate (mutation.cpp:126-166): offsets o1 (recorded from
+//           the same stream) -> y and a1;
+//   iso     SmallStep::Mutate with the second-stage sigma (mutation.cpp:167-208):
+//           o2 -> z and a2;
+//   h2mc    PH2MCSmallStep::Mutate (drsmallstep.cpp:113-212): its offset
+//           (GenerateSample from the Gaussian at x, recorded by replaying the
+//           stream), z, the unclamped ratio a2 and log N_z(-o) - log N_x(o)
+//           (GaussianLogPdf, gaussian.cpp:18-34);
+//   y*      SmallStep::Trace (mutation.cpp:210-238) of z by x - y, per second stage;
+// and the second-stage acceptances of Green & Mira and of Tierney & Mira, the
+// blocks of delayed.cpp:466-541 restated below on those values (they are
+// inline in DRIntegrator::Render, so there is no function to call).
+void ModeAccept(uint64_t seed0, int count, const PathFuncLib &lib, int maxDervDepth) {
+    const Scene *scene = g_scene;
+    const int maxDepth = scene->options->maxDepth;
+    const int minDepth = std::max(scene->options->minDepth, 3);
+    const MLTState mltState{scene, GeneratePathBidir, PerturbPathBidir, PerturbLensBidir, lib.funcMap,
+                            lib.dervFuncMap, lib.staticFuncMap, lib.staticDervFuncMap, lib.lensFuncMap,
+                            lib.lensDervFuncMap};
+    // a fixed, uneven path-length distribution over lengths 0..maxDepth
+    std::vector<Float> lengthFunc(maxDepth + 1, Float(0.0));
+    for (int L = 2; L <= maxDepth; L++) lengthFunc[L] = Float(1.0) + Float(0.25) * Float(L % 3) + Float(L);
+    auto lengthDist = std::make_shared<PiecewiseConstant1D>(&lengthFunc[0], int(lengthFunc.size()));
+    LargeStep largeStep(lengthDist);
+    SmallStep smallStep;
+    PH2MCSmallStep h2mc(scene, maxDervDepth, scene->options->perturbStdDev);
+    const Float sigma1 = scene->options->perturbStdDev;
+    const Float sigma2 = scene->options->anisoperturbstddev;
+    const Float b = Float(1.0);
+    auto isInvalid = [](Float x) { return std::isnan(x) || std::isinf(x) || x < Float(0.0); };
+    auto metropolisClamp = [](Float x) { return std::min(Float(1.0), x); };
+    int written = 0;
+    for (int s = 0; written < count && s < 100 * count; s++) {
+        RNG brng(seed0 + s);
+        Path full;
+        std::vector<SubpathContrib> contribs;
+        GeneratePathBidir(scene, Vector2i(-1, -1), minDepth, maxDepth, full, contribs, brng);
+        for (const SubpathContrib &c : contribs) {
+            if (written >= count) break;
+            const uint64_t cs = 1000u * (seed0 + s) + uint64_t(written);
+            MarkovState cur;
+            cur.valid = true;
+            cur.spContrib = c;
+            cur.path = full;
+            cur.path.Initialize(c.camDepth, c.lightDepth);
+            const int dim = GetDimension(cur.path);
+            const Vector x = GetPathPos(cur.path);
+            fprintf(g_out, "{\"mode\":\"accept\",\"seed\":%llu,\"dim\":%d,\"path\":", (unsigned long long)(seed0 + s),
+                    dim);
+            DumpPath(cur.path);
+            fprintf(g_out, ",\"contrib\":");
+            DumpContribs({c});
+            fprintf(g_out, ",\"pos\":");
+            Arr(x, dim);
+            fprintf(g_out, ",\"sigma1\":");
+            F(sigma1);
+            fprintf(g_out, ",\"sigma2\":");
+            F(sigma2);
+            fprintf(g_out, ",\"lengthFunc\":");
+            Arr(lengthFunc, int(lengthFunc.size()));
+            // ---- large step
+            {
+                UniformTape tape(cs * 4u + 0u, 1024);
+                RNG rng = tape.start;
+                MarkovState prop;
+                const Float a = largeStep.Mutate(mltState, b, cur, prop, rng);
+                fprintf(g_out, ",\"large\":{");
+                tape.Dump(tape.Consumed(rng));
+                fprintf(g_out, ",\"a1\":");
+                F(a);
+                fprintf(g_out, ",\"contribs\":");
+                DumpContribs(largeStep.spContribs);
+                fputc('}', g_out);
+            }
+            // ---- first stage, isotropic small step
+            MarkovState Y;
+            Vector o1(dim);
+            Float a1;
+            {
+                RNG rng(cs * 4u + 1u);
+                RNG copy = rng;
+                std::normal_distribution<Float> nd(Float(0.0), sigma1);
+                for (int i = 0; i < dim; i++) o1[i] = nd(copy);
+                a1 = smallStep.Mutate(mltState, b, cur, Y, rng);
+                const bool valid = !smallStep.spContribs.empty();
+                fprintf(g_out, ",\"small\":{\"offset\":");
+                Arr(o1, dim);
+                fprintf(g_out, ",\"a1\":");
+                F(a1);
+                fprintf(g_out, ",\"valid\":%d,\"ss\":", int(valid));
+                F(valid ? Y.spContrib.ssScore : Float(0.0));
+                fprintf(g_out, ",\"ypos\":");
+                Arr(GetPathPos(Y.path), dim);
+                fputc('}', g_out);
+                if (isInvalid(a1)) a1 = Float(0.0);
+            }
+            const Vector y = GetPathPos(Y.path);
+            // ---- second stages
+            for (int kind = 0; kind < 2; kind++) {
+                MarkovState Z;
+                Vector o2(dim);
+                Float a2;
+                double logRatio = 0.0;
+                RNG rng(cs * 4u + 2u + kind);
+                if (kind == 0) {
+                    RNG copy = rng;
+                    std::normal_distribution<Float> nd(Float(0.0), sigma2);
+                    for (int i = 0; i < dim; i++) o2[i] = nd(copy);
+                    a2 = smallStep.Mutate(mltState, b, cur, Z, sigma2, rng);
+                } else {
+                    // the offset GenerateSample draws from the Gaussian at x: Mutate
+                    // computes that Gaussian first without drawing, so the same
+                    // Gaussian and a copy of the stream give the same offset
+                    cur.gaussianInitialized = false;
+                    a2 = h2mc.Mutate(mltState, b, cur, Z, rng);
+                    RNG copy(cs * 4u + 2u + kind);
+                    GenerateSample(cur.gaussian, o2, copy);
+                    if (!h2mc.spContribs.empty()) {
+                        const Float py = GaussianLogPdf(o2, cur.gaussian);
+                        const Float px = GaussianLogPdf(Vector(-o2), Z.gaussian);
+                        logRatio = double(px) - double(py);
+                    }
+                }
+                const bool validZ = kind == 0 ? !smallStep.spContribs.empty() : !h2mc.spContribs.empty();
+                const Float ssZ = validZ ? Z.spContrib.ssScore : Float(0.0);
+                // Green's reverse path from z (the proposal object counts as a
+                // valid state, as after the chain's first second-stage accept)
+                Float aStar = Float(0.0);
+                if (validZ) {
+                    Z.valid = true;
+                    MarkovState star;
+                    RNG trng(cs * 4u + 3u);
+                    Vector off = x - y;
+                    aStar = smallStep.Trace(mltState, off, Z, star, trng);
+                }
+                // delayed.cpp:466-541
+                Float alphaGreen = Float(0.0), alphaMira = Float(0.0), transRatio = Float(0.0);
+                Float a2v = a2;
+                if (!isInvalid(a2v)) {
+                    Float as = isInvalid(aStar) ? Float(0.0) : aStar;
+                    alphaGreen = as == Float(1.0) ? Float(0.0) : metropolisClamp(a2v * (Float(1.0) - as) / (Float(1.0) - a1));
+                    // Y.spContrib keeps its zero default when the first stage did not contribute
+                    Float am = metropolisClamp(Y.spContrib.ssScore / ssZ);
+                    am = isInvalid(am) ? Float(1.0) : am;
+                    if (am != Float(1.0)) {
+                        const Vector z = GetPathPos(Z.path);
+                        Gaussian gaussIso;
+                        IsotropicGaussian(int(y.size()), sigma1, gaussIso);
+                        transRatio = std::exp(GaussianLogPdf(Vector(z - y), gaussIso) - GaussianLogPdf(Vector(x - y), gaussIso));
+                        if (!isInvalid(transRatio))
+                            alphaMira = metropolisClamp(a2v * transRatio * (Float(1.0) - am) / (Float(1.0) - a1));
+                    }
+                }
+                fprintf(g_out, ",\"%s\":{\"offset\":", kind == 0 ? "iso" : "h2mc");
+                Arr(o2, dim);
+                fprintf(g_out, ",\"a2\":");
+                F(a2);
+                fprintf(g_out, ",\"logRatio\":");
+                F(logRatio);
+                fprintf(g_out, ",\"valid\":%d,\"ss\":", int(validZ));
+                F(ssZ);
+                fprintf(g_out, ",\"zpos\":");
+                Arr(GetPathPos(Z.path), dim);
+                fprintf(g_out, ",\"aStar\":");
+                F(aStar);
+                fprintf(g_out, ",\"transRatio\":");
+                F(transRatio);
+                fprintf(g_out, ",\"alphaGreen\":");
+                F(alphaGreen);
+                fprintf(g_out, ",\"alphaMira\":");
+                F(alphaMira);
+                fputc('}', g_out);
+            }
+            fprintf(g_out, "}\n");
+            written++;
+        }
+    }
+}
+
 // Per shape: the world-space corner positions and shading normals of every
 // triangle, in TriMeshData index order.
 void ModeMesh() {
@@ -424,6 +610,10 @@ int main(int argc, char **argv) {
         if (chdir(libdir.c_str()) != 0) return 3;
         std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);
         ModeTech(seed0, count, extra, *lib, maxDervDepth);
+    } else if (mode == "accept") {
+        if (chdir(libdir.c_str()) != 0) return 3;
+        std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);
+        ModeAccept(seed0, count, *lib, maxDervDepth);
     } else {
         return 2;
     }

@@ -10,6 +10,11 @@ synthetic Cornell-box scenes of drmlt/scenegen.py and writes gzipped JSON lines:
   <cfg>_direct.jsonl.gz   GeneratePath direct-lighting pass: stream + pixel -> contributions
   <cfg>_tech.jsonl.gz     technique paths with chad log f, gradient, Hessian,
                           ComputeGaussian output and PerturbPathBidir results
+  <cfg>_accept.jsonl.gz   per-stage acceptances of one DR iteration from the
+                          reference's own mutations on fixed states: LargeStep::Mutate
+                          on a recorded stream, SmallStep::Mutate (both sigmas),
+                          PH2MCSmallStep::Mutate, SmallStep::Trace (Green's y*), with
+                          their offsets, and Green / Mira second-stage acceptances
   <cfg>_render*.json.gz   a full `dpt -d` render of the scene (the reference's
                           DRIntegrator::Render): its printed acceptance counters
                           and the final image averaged over 16 x 16 blocks
@@ -19,6 +24,7 @@ synthetic Cornell-box scenes of drmlt/scenegen.py and writes gzipped JSON lines:
 usage (in a container that has the reference at /root/reference):
   python tests/golden/make_golden.py [--render] [cfg1] [cfg2]   (--render: only the renders)
   python tests/golden/make_golden.py --mesh                     (only cfgM_mesh)
+  python tests/golden/make_golden.py --accept [cfg1] ...        (only the acceptance fixtures)
 """
 from __future__ import annotations
 
@@ -136,6 +142,29 @@ def run(cfg: str):
         shutil.rmtree(tmp)
 
 
+ACCEPT_COUNT = 80
+
+
+def accept(cfg: str):
+    writer, depth, _ = CONFIGS[cfg]
+    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
+    libdir = os.path.join(REF_DIR, "lib_d%d" % depth)
+    os.makedirs(libdir, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    try:
+        xml = writer(os.path.join(tmp, "scene"))
+        out = os.path.join(tmp, "accept.jsonl")
+        subprocess.check_call([HARNESS, xml, libdir, str(depth), out, "accept", "11", str(ACCEPT_COUNT), "0"],
+                              stdout=subprocess.DEVNULL)
+        dst = os.path.join(HERE, "%s_accept.jsonl.gz" % cfg)
+        with open(out, "rb") as f, open(dst, "wb") as raw:
+            with gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as g:
+                shutil.copyfileobj(f, g)
+        print(dst, os.path.getsize(dst))
+    finally:
+        shutil.rmtree(tmp)
+
+
 def mesh():
     subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
     tmp = tempfile.mkdtemp()
@@ -156,6 +185,10 @@ if __name__ == "__main__":
     args = sys.argv[1:]
     if "--mesh" in args:
         mesh()
+        sys.exit(0)
+    if "--accept" in args:
+        for c in [a for a in args if not a.startswith("--")] or list(CONFIGS):
+            accept(c)
         sys.exit(0)
     only_render = "--render" in args
     for c in [a for a in args if not a.startswith("--")] or ["cfg1"]:

@@ -163,6 +163,36 @@ def test_multi_iteration_graphs_keep_the_chains(built_lib, scene_root):
     np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-4, atol=1e-6)
 
 
+@pytest.mark.parametrize("cfg,dr_type", [("cfg2", "mira"), ("cfg3", "green"), ("cfgL", "green"), ("cfgE", "green"),
+                                         ("cfg4s", "mira"), ("cfg4s", "green")])
+def test_wavefront_takes_the_per_lane_steps(built_lib, scene_root, cfg, dr_type):
+    """Path tracing in wavefront rounds (rays of all chains queued per bounce,
+    traced by a separate traversal kernel) and one chain per lane tracing its
+    whole path run the same path machines: the chains take the same steps
+    (integer counters identical, film equal up to the order of the splat
+    additions). The scenes cover camera connections, direct lighting, vertex
+    connections, light-coordinate sampling, the environment light, Green's y*
+    and depth-12 paths (cfg4s: the miniature config-4 scene)."""
+    from drmlt import scenegen
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    if cfg == "cfg4s":
+        xml = scenegen.config4_small(os.path.join(scene_root, "wave_cfg4s_" + dr_type), dr_type=dr_type)
+    else:
+        xml = _scene(cfg, dr_type, scene_root)
+    sd = dscene.load_scene(xml)
+    out = []
+    for wave in (1, 0):
+        with Renderer(sd, num_chains=4096, wavefront=wave) as r:
+            assert r.launch_shape()["wavefront"] == wave
+            r.prepass()
+            r.run(10)
+            out.append((r.stats(), r.film().astype(np.float64)))
+    assert out[0][0] == out[1][0]
+    assert out[0][0]["stage2_h2mc"] > 0 and out[0][0]["large_step_accepted"] > 0
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-4, atol=1e-6)
+
+
 def test_autotuner_keeps_the_chains(built_lib, scene_root):
     """drmlt_autotune runs real iterations under each candidate launch shape and
     settles on one of them; the render is the one an untuned render gives
@@ -176,13 +206,15 @@ def test_autotuner_keeps_the_chains(built_lib, scene_root):
         assert lanes in (2, 4, 8, 16, 32) and warps in (1, 2, 4)
         # drmlt_get_launch_shape reports the tuned shape; 2 iterations per
         # candidate leave the graph length at 1
-        assert a.launch_shape() == {"chains_per_warp": lanes, "stage2_chains_per_warp": min(lanes, 4),
-                                    "derivative_warps": warps, "graph_iterations": 1}
+        shape = a.launch_shape()
+        assert shape["wavefront"] in (0, 1)
+        assert shape == {"chains_per_warp": lanes, "stage2_chains_per_warp": min(lanes, 4),
+                         "derivative_warps": warps, "graph_iterations": 1, "wavefront": shape["wavefront"]}
         tuned = a.stats()["mutations"] // 4096
-        assert tuned == 2 * 17
-        a.run(40 - tuned)
+        assert tuned == 2 * 21
+        a.run(48 - tuned)
         b.prepass()
-        b.run(40)
+        b.run(48)
         assert a.stats() == b.stats()
         np.testing.assert_allclose(a.film(), b.film(), rtol=1e-4, atol=1e-6)
 
