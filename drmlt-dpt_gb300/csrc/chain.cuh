@@ -67,8 +67,8 @@ struct ChainView {
     float *grad;        // N x kMaxDim (indexed by list position)
     float *hess;        // N x kMaxDim^2
     unsigned long long *stats;
-    float *film;        // W x H x 3 (indirect)
-    float *direct;      // W x H x 3
+    float4 *film;       // W x H (indirect), RGB + unused
+    float4 *direct;     // W x H
     const float *lengthCdf;
     const float *lengthFunc;
     int lengthCount;
@@ -150,26 +150,64 @@ DEV void set_contrib(Slot &st, const Emit &e, float b) {
     st.hasSplat = 1;
 }
 
-// Splat (src/image.h:65-74): nearest pixel, finite values only.
-DEV void splat(float *film, int W, int H, float sx, float sy, float r, float g, float b) {
-    if (r == 0.0f && g == 0.0f && b == 0.0f) return;
-    if (!(isfinite(r) && isfinite(g) && isfinite(b))) return;
+// Films are W x H float4 pixels (RGB + an unused lane), so that one splat is one
+// 16-byte vector reduction (red.global.add.v4.f32) instead of three scalar ones.
+//
+// Splat (src/image.h:65-74): nearest pixel, finite values only. Returns the
+// pixel index, or -1 when the value is zero or not finite (nothing to add).
+DEV int splat_pixel(int W, int H, float sx, float sy, float r, float g, float b) {
+    if (r == 0.0f && g == 0.0f && b == 0.0f) return -1;
+    if (!(isfinite(r) && isfinite(g) && isfinite(b))) return -1;
     int ix = int(sx * float(W));
     int iy = int(sy * float(H));
     ix = ix < 0 ? 0 : (ix > W - 1 ? W - 1 : ix);
     iy = iy < 0 ? 0 : (iy > H - 1 ? H - 1 : iy);
-    float *px = film + 3 * (size_t(iy) * W + ix);
-    atomicAdd(px, r);
-    atomicAdd(px + 1, g);
-    atomicAdd(px + 2, b);
+    return iy * W + ix;
+}
+DEV void splat(float4 *film, int W, int H, float sx, float sy, float r, float g, float b) {
+    const int px = splat_pixel(W, H, sx, sy, r, g, b);
+    if (px >= 0) atomicAdd(film + px, make_float4(r, g, b, 0.0f));
 }
 
 // WeightedSplat (src/integrators/delayed/delayed.cpp:255-265): weight times the
-// stored splat, skipped when Eigen's isZero() holds for the product.
-DEV void weighted_splat(float *film, int W, int H, const float *sp, float w) {
+// stored splat, skipped when Eigen's isZero() holds for the product. Fills one
+// pending splat (pixel -1: none) for warp_splat.
+struct PendingSplat {
+    int px;
+    float r, g, b;
+};
+DEV PendingSplat weighted_splat_of(int W, int H, const float *sp, float w) {
     const V3 v(w * sp[2], w * sp[3], w * sp[4]);
-    if (is_zero(v)) return;
-    splat(film, W, H, sp[0], sp[1], v.x, v.y, v.z);
+    if (is_zero(v)) return PendingSplat{-1, 0.0f, 0.0f, 0.0f};
+    return PendingSplat{splat_pixel(W, H, sp[0], sp[1], v.x, v.y, v.z), v.x, v.y, v.z};
+}
+
+// Warp-aggregated splat: called by all 32 lanes of a warp together, each with
+// one pending splat (px = -1 for none). Lanes that hit the same pixel are
+// grouped with __match_any_sync; the lowest lane of each group adds the
+// group's sum with one vector reduction. The combining loop runs once per
+// lane that shares its pixel with a lower lane (rare at these chain counts:
+// most warps issue one reduction per distinct pixel and skip the loop).
+DEV void warp_splat(float4 *film, PendingSplat s) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(kFull, s.px);
+    const int leader = __ffs(peers) - 1;
+    unsigned pending = __ballot_sync(kFull, s.px >= 0 && lane != leader);
+    while (pending) {
+        const int j = __ffs(pending) - 1;
+        const float r = __shfl_sync(kFull, s.r, j);
+        const float g = __shfl_sync(kFull, s.g, j);
+        const float b = __shfl_sync(kFull, s.b, j);
+        const unsigned pj = __shfl_sync(kFull, peers, j);
+        if (lane == __ffs(pj) - 1) {
+            s.r += r;
+            s.g += g;
+            s.b += b;
+        }
+        pending &= pending - 1u;
+    }
+    if (s.px >= 0 && lane == leader) atomicAdd(film + s.px, make_float4(s.r, s.g, s.b, 0.0f));
 }
 
 // Block-aggregated statistics: one global atomic per counter per block.

@@ -512,11 +512,11 @@ struct Renderer {
         if ((rc = alloc(&cv.grad, size_t(N) * kMaxDim))) return rc;
         if ((rc = alloc(&cv.hess, size_t(N) * kMaxDim * kMaxDim))) return rc;
         if ((rc = alloc(&cv.stats, kNumStats))) return rc;
-        if ((rc = alloc(&cv.film, size_t(W) * H * 3))) return rc;
-        if ((rc = alloc(&cv.direct, size_t(W) * H * 3))) return rc;
+        if ((rc = alloc(&cv.film, size_t(W) * H))) return rc;
+        if ((rc = alloc(&cv.direct, size_t(W) * H))) return rc;
         CK(cudaMemset(cv.stats, 0, kNumStats * sizeof(unsigned long long)));
-        CK(cudaMemset(cv.film, 0, size_t(W) * H * 3 * sizeof(float)));
-        CK(cudaMemset(cv.direct, 0, size_t(W) * H * 3 * sizeof(float)));
+        CK(cudaMemset(cv.film, 0, size_t(W) * H * sizeof(float4)));
+        CK(cudaMemset(cv.direct, 0, size_t(W) * H * sizeof(float4)));
         CK(cudaMemset(cv.counters, 0, 4 * size_t(G) * sizeof(int)));
         // sample split of delayed.cpp:205-210, including its extra-sample rule
         const long long totalSamples = (long long)opt.spp * W * H;
@@ -931,32 +931,41 @@ struct Renderer {
         return DRMLT_OK;
     }
 
+    // The device films hold float4 pixels (RGB + an unused lane); the host film is RGB.
     int film(float *rgb) {
-        const size_t n = size_t(W) * H * 3;
-        std::vector<float> ind(n), dir(n);
-        CK(cudaMemcpy(ind.data(), cv.film, n * sizeof(float), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(dir.data(), cv.direct, n * sizeof(float), cudaMemcpyDeviceToHost));
+        const size_t n = size_t(W) * H;
+        std::vector<float4> ind(n), dir(n);
+        CK(cudaMemcpy(ind.data(), cv.film, n * sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(dir.data(), cv.direct, n * sizeof(float4), cudaMemcpyDeviceToHost));
         // MergeBuffer (src/image.h:76-93, delayed.cpp:681-685)
         const float dw = opt.direct_spp > 0 ? 1.0f / float(opt.direct_spp) : 0.0f;
         const float iw = opt.spp > 0 ? 1.0f / float(opt.spp) : 0.0f;
         for (size_t i = 0; i < n; i++) {
-            float v = 0.0f;
-            v += dw * dir[i];
-            v += iw * ind[i];
-            rgb[i] = v;
+            const float d[3] = {dir[i].x, dir[i].y, dir[i].z};
+            const float v[3] = {ind[i].x, ind[i].y, ind[i].z};
+            for (int k = 0; k < 3; k++) {
+                float o = 0.0f;
+                o += dw * d[k];
+                o += iw * v[k];
+                rgb[3 * i + k] = o;
+            }
         }
         return DRMLT_OK;
     }
 
     int partial_film(float *rgb) {
-        const size_t n = size_t(W) * H * 3;
-        std::vector<float> ind(n);
+        const size_t n = size_t(W) * H;
+        std::vector<float4> ind(n);
         unsigned long long h[kNumStats];
-        CK(cudaMemcpy(ind.data(), cv.film, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(ind.data(), cv.film, n * sizeof(float4), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(h, cv.stats, sizeof(h), cudaMemcpyDeviceToHost));
         const unsigned long long work = h[kStatMutations];
         const float factor = work > 0 ? float(double(W) * double(H) / double(work)) : 0.0f;
-        for (size_t i = 0; i < n; i++) rgb[i] = factor * ind[i];
+        for (size_t i = 0; i < n; i++) {
+            rgb[3 * i + 0] = factor * ind[i].x;
+            rgb[3 * i + 1] = factor * ind[i].y;
+            rgb[3 * i + 2] = factor * ind[i].z;
+        }
         return DRMLT_OK;
     }
 };

@@ -484,6 +484,9 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
     const int t = sparse_index(p.lanes, on);
     const int i = p.c0 + t;
     StatAcc acc;
+    const int W = p.s.cam.width, H = p.s.cam.height;
+    // up to three splats per chain, added warp-aggregated after the chain's work
+    PendingSplat sp[3] = {{-1, 0.0f, 0.0f, 0.0f}, {-1, 0.0f, 0.0f, 0.0f}, {-1, 0.0f, 0.0f, 0.0f}};
     if (on && t < p.N && (p.d.scr[i].flags & kActive)) {
         Scratch &sc = p.d.scr[i];
         const int flags = sc.flags;
@@ -522,14 +525,10 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
         const float w1 = a1;
         const float w2 = (1.0f - w1) * a2;
         const float wc = 1.0f - w1 - w2;
-        const int W = p.s.cam.width, H = p.s.cam.height;
         if (!p.accMap) {
-            if (cur.valid && wc > 0.0f && cur.hasSplat)
-                weighted_splat(p.d.film, W, H, cur.splat, wc);
-            if (w1 > 0.0f && F.hasSplat)
-                weighted_splat(p.d.film, W, H, F.splat, w1);
-            if (w2 > 0.0f && S.hasSplat)
-                weighted_splat(p.d.film, W, H, S.splat, w2);
+            if (cur.valid && wc > 0.0f && cur.hasSplat) sp[0] = weighted_splat_of(W, H, cur.splat, wc);
+            if (w1 > 0.0f && F.hasSplat) sp[1] = weighted_splat_of(W, H, F.splat, w1);
+            if (w2 > 0.0f && S.hasSplat) sp[2] = weighted_splat_of(W, H, S.splat, w2);
         }
         // accept / swap (delayed.cpp:563-606)
         int *perm = p.d.perm + 3 * i;
@@ -541,7 +540,8 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
             nc.gaussInit = 0;
             nc.valid = 1;
             const Slot &old = slot_of(p.d, i, 1);
-            if (p.accMap && !(flags & kLarge) && old.hasSplat) splat(p.d.film, W, H, old.splat[0], old.splat[1], 1.0f, 0.0f, 0.0f);
+            if (p.accMap && !(flags & kLarge) && old.hasSplat)
+                sp[0] = PendingSplat{splat_pixel(W, H, old.splat[0], old.splat[1], 1.0f, 0.0f, 0.0f), 1.0f, 0.0f, 0.0f};
         } else if (accept2) {
             const int t = perm[0];
             perm[0] = perm[2];
@@ -550,11 +550,13 @@ __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
             if (!aniso) nc.gaussInit = 0;
             nc.valid = 1;
             const Slot &old = slot_of(p.d, i, 2);
-            if (p.accMap && old.hasSplat) splat(p.d.film, W, H, old.splat[0], old.splat[1], 0.0f, 1.0f, 0.0f);
+            if (p.accMap && old.hasSplat)
+                sp[0] = PendingSplat{splat_pixel(W, H, old.splat[0], old.splat[1], 0.0f, 1.0f, 0.0f), 0.0f, 1.0f, 0.0f};
         }
         sc.flags = flags | (accept2 ? kAccept2 : 0);
         sc.a2 = a2;
     }
+    for (int k = 0; k < 3; k++) warp_splat(p.d.film, sp[k]);
     flush_stats(acc, p.d.stats);
 }
 
@@ -654,13 +656,13 @@ __global__ void __launch_bounds__(128) k_seed(RunParams p, unsigned long long bo
 
 // ------------------------------------------------------------- direct lighting pass
 struct SinkSplat {
-    float *film;
+    float4 *film;
     int W, H;
     DEV void operator()(const Emit &e) { splat(film, W, H, e.screen[0], e.screen[1], e.rgb.x, e.rgb.y, e.rgb.z); }
 };
 
 __global__ void __launch_bounds__(128) k_direct(SceneView s, unsigned long long seed, int spp, int minDepth,
-                                                int maxDepth, float *film) {
+                                                int maxDepth, float4 *film) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long npix = (long long)s.cam.width * s.cam.height;
     if (t >= npix * spp) return;
