@@ -1,6 +1,7 @@
 """Builds libdrmlt.so in-tree for sm_103a (nvcc: the chain-loop translation unit, the
-path-derivative translation unit, the host BVH builder and the host image writer,
-compiled in parallel).
+persistent-schedule translation unit, the path-derivative translation unit, the host
+BVH builder and the host image writer, compiled in parallel as relocatable device code
+and device-linked into the library).
 
 usage: python drmlt-dpt_gb300/build.py [--force]
 """
@@ -20,8 +21,16 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I" + os.path.join(REPO, "include")]
 # The derivative kernel is instruction-fetch bound on its long hyper-dual code;
 # fast-math intrinsics keep the transcendental calls short. Its outputs are
-# derivatives (checked to 1e-3) and never a path contribution.
-TU_FLAGS = {"derivs.cu": ["--use_fast_math"]}
+# derivatives (checked to 1e-3) and never a path contribution. The persistent
+# kernel (persist.cu, compiled without fast math like the path code) calls the
+# same derivative code compiled with the same flags in derivs_dev.cu: those two
+# are relocatable device code (device-linked into the library), held to the
+# 128 registers of the kernel; the other translation units are whole-program
+# code (relocatable code changes their register allocation: k_gauss 56 -> 95).
+FAST = ["--use_fast_math"]
+TU_FLAGS = {"derivs.cu": FAST, "derivs_dev.cu": FAST + ["-rdc=true", "-maxrregcount=128"],
+            "persist.cu": ["-rdc=true"]}
+SOURCES = ("drmlt.cu", "persist.cu", "derivs.cu", "derivs_dev.cu", "bvh.cpp", "image_io.cpp")
 
 
 def _sources():
@@ -41,7 +50,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     objs = []
     jobs = []
-    for src in ("drmlt.cu", "derivs.cu", "bvh.cpp", "image_io.cpp"):
+    for src in SOURCES:
         obj = os.path.join(LIBDIR, src + ".o")
         cmd = [NVCC] + ARCH + FLAGS + TU_FLAGS.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):

@@ -97,6 +97,8 @@ struct RunParams {
     int lanes2;          // chains per warp in the second-stage list kernels (1..32)
     const int *iterp;    // the group's current iteration (device memory)
     int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
+    int lists;           // 1: the stage epilogues append the chain to the group's work lists (the
+                         // staged schedule); 0: they only set the chain's flags (persistent schedule)
     int wave;            // 1: path tracing in wavefront rounds (wave.cuh), 0: one chain per lane
     int waveRounds;      // rounds of a wavefront stage pass (max_depth + 1)
     unsigned long long seed;

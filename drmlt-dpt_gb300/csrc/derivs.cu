@@ -4,39 +4,9 @@
 // mode on the AD path function of pathad.cuh.
 #include "chain.cuh"
 #include "derivs.h"
+#include "derivs_path.cuh"
 
 namespace drmlt {
-
-// One warp per listed chain: lanes stride over the D(D+1)/2 Hessian entries.
-// which: 0 = current state, 2 = second proposal.
-__device__ void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H,
-                                int member = threadIdx.x & 31, int team = 32) {
-    const int lane = member;
-    const int L = r.c + r.l - 1;
-    const int dim = 2 * L;
-    if (!(L <= maxDerv && ss > 1e-15f)) {
-        for (int k = lane; k < dim; k += team) g[k] = 0.0f;
-        for (int k = lane; k < dim * dim; k += team) H[k] = 0.0f;
-        return;
-    }
-    const int npairs = dim * (dim + 1) / 2;
-    for (int pidx = lane; pidx < npairs; pidx += team) {
-        // decode pidx -> (i0, j0), i0 <= j0, row-major over the upper triangle
-        int i0 = 0, rem = pidx;
-        while (rem >= dim - i0) {
-            rem -= dim - i0;
-            i0++;
-        }
-        const int j0 = i0 + rem;
-        HyperDual u[kMaxDim];
-        for (int k = 0; k < dim; k++)
-            u[k] = HyperDual(r.u[k], k == i0 ? 1.0f : 0.0f, k == j0 ? 1.0f : 0.0f, 0.0f);
-        const HyperDual f = ad_eval_path<HyperDual>(s, r, u);
-        H[i0 * dim + j0] = f.ab;
-        H[j0 * dim + i0] = f.ab;
-        if (i0 == j0) g[i0] = f.a;
-    }
-}
 
 // A team of p.derivWarps warps per listed chain shares its Hessian entries. The
 // grid is sized for the GPU: team t takes list entries t, t + teams, ...
@@ -72,7 +42,8 @@ __global__ void __launch_bounds__(128) k_gradhess_paths(SceneView s, const PathR
     const int dim = path_dim(r.c, r.l);
     for (int k = 0; k < dim; k++) r.u[k] = u[size_t(w) * kMaxDim + k];
     // derivatives are always taken here (no ss / depth gate)
-    derivs_for_path(s, r, 1.0f, kMaxLen, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim);
+    derivs_for_path(s, r, 1.0f, kMaxLen, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim,
+                    threadIdx.x & 31, 32);
 }
 
 // Gradient + Hessian at each path's own primary vector, gated as in the chain
@@ -82,7 +53,8 @@ __global__ void __launch_bounds__(128) k_gradhess_gated(SceneView s, const PathR
                                                         int maxDerv, float *grad, float *hess) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (w >= n) return;
-    derivs_for_path(s, paths[w], ss[w], maxDerv, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim);
+    derivs_for_path(s, paths[w], ss[w], maxDerv, grad + size_t(w) * kMaxDim, hess + size_t(w) * kMaxDim * kMaxDim,
+                    threadIdx.x & 31, 32);
 }
 
 void launch_gradhess_gated(const SceneView &s, const PathRec *paths, const float *ss, int n, int maxDerv, float *grad,

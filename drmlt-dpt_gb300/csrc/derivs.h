@@ -9,6 +9,14 @@ struct RunParams;
 struct SceneView;
 struct PathRec;
 
+// Gradient + Hessian of log f of path r (ss its score) for a team of `team`
+// threads, `member` the caller's index in it: zero (the isotropic fallback)
+// for a path longer than maxDerv segments or with ss <= 1e-15. g: kMaxDim
+// floats, H: kMaxDim^2. Defined in derivs_dev.cu (relocatable device code,
+// the derivative kernels' flags) for the persistent schedule.
+__device__ void persist_derivs(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H,
+                               int member, int team);
+
 // Gradient + Hessian of log f for the chains of list `which` (0: listX at the
 // current states, 2: listZ at the second proposals) of one chain group.
 void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s);

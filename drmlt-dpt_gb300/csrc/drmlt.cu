@@ -2,6 +2,7 @@
 // iteration schedule and the C ABI declared in include/drmlt_capi.h.
 #include "drmlt_capi.h"
 #include "wave.cuh"
+#include "persist.h"
 #include "bvh.h"
 #include "errors.h"
 
@@ -140,6 +141,12 @@ struct Renderer {
     float4 *waveRayO[2] = {nullptr, nullptr}, *waveRayD[2] = {nullptr, nullptr};
     int *waveHit = nullptr;
     int *waveCount = nullptr;  // per group: 3 stage passes x kWaveCountStride
+    // persistent schedule (persist.cu): queues, per-chain counters and the team
+    // workers' derivative rows, allocated on its first run
+    PersistBuffers pb{};
+    bool pbReady = false;
+    int persistGrid = 0, persistRegs = 0, numSms = 0;
+    int lastTeamSms = 0;
 
     template <class T>
     int alloc(T **p, size_t n) {
@@ -191,7 +198,8 @@ struct Renderer {
         p.lanes2 = opt.stage2_lanes > 0 ? std::min(opt.stage2_lanes, 32) : std::min(p.lanes, 4);
         p.iterp = dIters;
         p.derivWarps = opt.deriv_warps > 0 ? std::min(opt.deriv_warps, 4) : 2;
-        p.wave = opt.wavefront != 0 ? 1 : 0;
+        p.lists = 1;
+        p.wave = opt.wavefront > 0 ? 1 : 0;
         p.waveRounds = std::min(std::min(opt.max_depth, kMaxLen) + 1, kWaveMaxRounds);
         p.seed = opt.seed;
         return p;
@@ -798,9 +806,65 @@ struct Renderer {
 
     long long total_iterations() const { return samplesPerChain + (extraChains > 0 ? 1 : 0); }
 
+    bool persistent_schedule() const { return opt.persistent > 0 && opt.integrator == DRMLT_INTEGRATOR_DRMLT; }
+    size_t persist_smem() const { return gauss_smem_bytes(params().gaussDim); }
+
+    int persist_setup() {
+        if (pbReady) return DRMLT_OK;
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&numSms, cudaDevAttrMultiProcessorCount, dev));
+        int coop = 0;
+        CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop) return fail(DRMLT_E_CUDA, "the persistent schedule needs cooperative launches");
+        const int occ = persist_blocks_per_sm(persist_smem(), &persistRegs);
+        if (occ < 1) return fail(DRMLT_E_CUDA, "the persistent kernel does not fit on an SM");
+        persistGrid = occ * numSms;
+        int rc;
+        if ((rc = alloc(reinterpret_cast<float4 **>(&pb.laneCells), size_t(N)))) return rc;
+        if ((rc = alloc(reinterpret_cast<float4 **>(&pb.teamCells), size_t(N)))) return rc;
+        if ((rc = alloc(&pb.ctl, size_t(8)))) return rc;
+        if ((rc = alloc(&pb.status, size_t(1)))) return rc;
+        if ((rc = alloc(&pb.chainIter, size_t(N)))) return rc;
+        if ((rc = alloc(&pb.chainPhase, size_t(N)))) return rc;
+        if ((rc = alloc(&pb.rows, size_t(persistGrid) * (kMaxDim + kMaxDim * kMaxDim)))) return rc;
+        pb.ystar = waveYstar;
+        pb.rowBlocks = persistGrid;
+        pbReady = true;
+        return DRMLT_OK;
+    }
+
+    // Iterations iterDone .. end of every chain in one persistent launch.
+    int run_persistent(long long end, long long *done) {
+        if (int rc = persist_setup()) return rc;
+        const int teamSms = opt.team_sms > 0 ? std::min(opt.team_sms, numSms - 1) : std::max(1, numSms / 4);
+        const long long waitLimit = opt.wait_limit > 0 ? opt.wait_limit : (1ll << 22);
+        RunParams p = params();
+        p.lists = 0;
+        CK(cudaEventRecord(ev0, stream));
+        const cudaError_t e = persist_run(p, pb, iterDone, end, persistGrid, teamSms, waitLimit, persist_smem(), stream);
+        if (e != cudaSuccess) return fail(DRMLT_E_CUDA, std::string("persistent launch: ") + cudaGetErrorString(e));
+        CK(cudaEventRecord(ev1, stream));
+        CK(cudaEventSynchronize(ev1));
+        CK(cudaEventElapsedTime(&lastRunMs, ev0, ev1));
+        launches += 2;
+        lastTeamSms = teamSms;
+        int status = 0;
+        CK(cudaMemcpy(&status, pb.status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (status)
+            return fail(DRMLT_E_TIMEOUT, "persistent schedule: a device wait gave up (status " + std::to_string(status) +
+                                             "); the chain state is undefined");
+        long long mutations = 0;
+        for (long long it = iterDone; it < end; it++) mutations += (it < samplesPerChain) ? N : extraChains;
+        iterDone = end;
+        if (done) *done = mutations;
+        return DRMLT_OK;
+    }
+
     int run(long long iterations, long long *done) {
         if (!prepassDone) return fail(DRMLT_E_STATE, "run before prepass");
         const long long end = std::min(iterDone + iterations, total_iterations());
+        if (persistent_schedule()) return run_persistent(end, done);
         long long mutations = 0;
         if (opt.use_graph && !graph) {
             if (int rc = build_graph()) return rc;

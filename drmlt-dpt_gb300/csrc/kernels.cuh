@@ -37,7 +37,7 @@ DEV int plan_key(const RunParams &p, int i, int iter) {
     return 1 + 16 * (cur.rec.c + cur.rec.l) + cur.rec.c;
 }
 
-__global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p) {
+static __global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p) {
     const int iter = *p.iterp;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.N) return;
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kStageBlock) k_plan(RunParams p) {
 }
 
 constexpr int kScatterBlock = 256;
-__global__ void __launch_bounds__(kScatterBlock) k_scatter(RunParams p) {
+static __global__ void __launch_bounds__(kScatterBlock) k_scatter(RunParams p) {
     __shared__ int start[kPlanBins];
     __shared__ int warpSum[kScatterBlock / 32];
     // exclusive scan of the class counts (two bins per thread)
@@ -140,9 +140,11 @@ DEV int stage1_begin(const RunParams &p, int i, int iter, Rng &rng, float *off, 
         // run by the second-stage kernels
         flags |= kSecond | kAniso | kSingle;
         acc.c[kStatH2mc]++;
-        p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
-        if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
-        p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+        if (p.lists) {
+            p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
+            if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+            p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+        }
         sc.flags = flags;
         sc.a1 = 0.0f;
         sc.a2 = 0.0f;
@@ -199,12 +201,14 @@ DEV void stage1_end(const RunParams &p, int i, int mode, int flags, Rng &rng, in
     const bool doSecond = !accept1 && !(flags & kLarge) && cur.valid && p.integrator == 0;
     if (doSecond) {
         flags |= kSecond;
-        p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
+        if (p.lists) p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
         if (flip_coin(p.anisoProb, rng.uniform())) {
             flags |= kAniso;
             acc.c[kStatH2mc]++;
-            if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
-            p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+            if (p.lists) {
+                if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+                p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+            }
         } else {
             acc.c[kStatIso]++;
         }
@@ -228,7 +232,7 @@ DEV int run_perturb(const SceneView &s, const PathRec &in, const float *off, J &
     return st;
 }
 
-__global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
+static __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes, on);
@@ -258,16 +262,18 @@ __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
 constexpr int kGaussTeamWarps = 4;
 inline size_t gauss_smem_bytes(int maxDim) { return size_t(gauss_smem_doubles(maxDim)) * sizeof(double); }
 
-DEV void gauss_for_entry(const RunParams &p, int which, int w, double *gsm) {
-    const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
+// The Gaussian of chain `chain` at its slot `which` (0 current state, 2 second
+// proposal) from the gradient / Hessian rows grad / hess, by the whole block
+// (a team of kGaussTeamWarps warps) with gauss_smem_doubles(gaussDim) doubles of
+// shared scratch at gsm; at the second proposal also the H2MC kernel ratio.
+DEV void gauss_for_chain(const RunParams &p, int chain, int which, const float *grad, const float *hess, double *gsm) {
     Slot &st = slot_of(p.d, chain, which);
     const int dim = path_dim(st.rec.c, st.rec.l);
     GaussSmem sm(gsm, p.gaussDim);
     const Team tm(gauss_reduction(gsm, p.gaussDim));
     // dim <= gaussDim holds by construction (max_depth bounds every path); the
     // isotropic branch needs no scratch, so an impossible larger dim stays in bounds
-    const int kind = compute_gaussian_team(dim, H2mcParam(p.sigma1), dim <= sm.m ? st.ss : 0.0f,
-                                           p.d.grad + size_t(w) * kMaxDim, p.d.hess + size_t(w) * kMaxDim * kMaxDim, sm,
+    const int kind = compute_gaussian_team(dim, H2mcParam(p.sigma1), dim <= sm.m ? st.ss : 0.0f, grad, hess, sm,
                                            GaussView(gauss_of(p.d, chain, which)), tm);
     if (which == 2) {
         // the H2MC kernel ratio of PH2MCSmallStep::Mutate (drsmallstep.cpp:191-196), FP64
@@ -284,10 +290,15 @@ DEV void gauss_for_entry(const RunParams &p, int which, int w, double *gsm) {
     }
 }
 
+DEV void gauss_for_entry(const RunParams &p, int which, int w, double *gsm) {
+    const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
+    gauss_for_chain(p, chain, which, p.d.grad + size_t(w) * kMaxDim, p.d.hess + size_t(w) * kMaxDim * kMaxDim, gsm);
+}
+
 // The grid is sized for the GPU, not the list: each block takes list entries
 // blockIdx.x, blockIdx.x + gridDim.x, ... (the list's length is known only on
 // the device).
-__global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int which) {
+static __global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int which) {
     extern __shared__ double gsm[];
     const int n = p.d.counters[which == 0 ? 0 : 1];
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -301,28 +312,35 @@ __global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int
 // anisotropic second stage, one warp per chain: offset = mean + V diag(p^-1/2) n
 // in FP64, with n the first dim normals of the chain's stage-2 stream (which
 // k_stage2 then skips).
-__global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p) {
-    const int iter = *p.iterp;
-    __shared__ double zs[4][kMaxDim];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= p.d.counters[3]) return;
-    const int i = p.d.listA[w];
+// One warp: the H2MC offset of chain i at iteration iter (zs: kMaxDim doubles of
+// the warp's shared scratch).
+DEV void h2mc_offset_warp(const RunParams &p, int i, int iter, double *zs) {
+    const int lane = threadIdx.x & 31;
     const Slot &cur = slot_of(p.d, i, 0);
     const int dim = path_dim(cur.rec.c, cur.rec.l);
     const GaussView g(gauss_of(p.d, i, 0));
     if (lane == 0) {
         Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
-        for (int k = 0; k < dim; k++) zs[wib][k] = double(rng.normal());
+        for (int k = 0; k < dim; k++) zs[k] = double(rng.normal());
     }
     __syncwarp();
-    if (lane < dim) zs[wib][lane] /= ::sqrt(g.p[lane]);
+    if (lane < dim) zs[lane] /= ::sqrt(g.p[lane]);
     __syncwarp();
     if (lane < dim) {
         double o = g.mean[lane];
-        for (int k = 0; k < dim; k++) o = ::fma(g.V[lane * dim + k], zs[wib][k], o);
+        for (int k = 0; k < dim; k++) o = ::fma(g.V[lane * dim + k], zs[k], o);
         p.d.scr[i].offset[lane] = float(o);
     }
+    __syncwarp();
+}
+
+static __global__ void __launch_bounds__(128) k_h2mc_offset(RunParams p) {
+    const int iter = *p.iterp;
+    __shared__ double zs[4][kMaxDim];
+    const int wib = threadIdx.x >> 5;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= p.d.counters[3]) return;
+    h2mc_offset_warp(p, p.d.listA[w], iter, zs[wib]);
 }
 
 // ------------------------------------------------------------- stage 2 proposal
@@ -368,7 +386,7 @@ DEV void stage2_end(const RunParams &p, int i, int st, const Emit &e) {
         S.ss = e.ss;
         if (!aniso || (e.ls > 0.0f && isfinite(e.ls))) set_contrib(S, e, p.b); else S.hasSplat = 0;
         if (aniso) {
-            p.d.listZ[atomicAdd(&p.d.counters[1], 1)] = i;
+            if (p.lists) p.d.listZ[atomicAdd(&p.d.counters[1], 1)] = i;
         } else {
             a2 = clamp01(e.ss / cur.ss);
         }
@@ -377,7 +395,7 @@ DEV void stage2_end(const RunParams &p, int i, int st, const Emit &e) {
 }
 
 // Over the group's second-stage list only (compacted by stage 1).
-__global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
+static __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes2, on);
@@ -414,7 +432,7 @@ DEV void ystar_end(const RunParams &p, int i, int st, const Emit &e) {
     p.d.scr[i].aStar = st == kStepDone ? clamp01(e.ss / S.ss) : 0.0f;
 }
 
-__global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p) {
+static __global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes2, on);
@@ -478,98 +496,103 @@ DEV float dr_second_acceptance(int drType, float a1, float a2, float aStarGreen,
 }
 
 // ------------------------------------------------------------- finish
-__global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
+// The end of chain i's iteration `iter` (delayed.cpp:466-606): Green or Mira
+// second-stage acceptance, the weighted splats (returned in sp[0..2] as
+// pending splats; pixel -1 = none), accept / swap and the statistics.
+DEV void finish_chain(const RunParams &p, int i, int iter, StatAcc &acc, PendingSplat *sp) {
+    const int W = p.s.cam.width, H = p.s.cam.height;
+    Scratch &sc = p.d.scr[i];
+    const int flags = sc.flags;
+    const float a1 = sc.a1;
+    float a2 = sc.a2;
+    bool accept2 = false;
+    Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 2ull);
+    Slot &cur = slot_of(p.d, i, 0);
+    Slot &F = slot_of(p.d, i, 1);
+    Slot &S = slot_of(p.d, i, 2);
+    const bool aniso = flags & kAniso;
+    if (flags & kSecond) {
+        const int dim = path_dim(cur.rec.c, cur.rec.l);
+        if (aniso) {
+            if (flags & kZValid) {
+                a2 = float(::exp(sc.logRatio)) * S.ss / cur.ss;
+            } else {
+                a2 = 0.0f;
+            }
+        }
+        if (is_invalid(a2)) {
+            a2 = 0.0f;
+        } else if (flags & kSingle) {
+            // the usual MH acceptance, Clamp(a, 0, 1) (h2mc.cpp:580-584, 220)
+            a2 = clamp01(a2);
+            accept2 = flip_coin(a2, rng.uniform());
+        } else {
+            bool draw;
+            a2 = dr_second_acceptance(p.drType, a1, a2, sc.aStar, F.ss, S.ss, dim, cur.rec.u, F.rec.u, S.rec.u,
+                                      p.sigma1, draw);
+            if (draw) accept2 = flip_coin(a2, rng.uniform());
+        }
+        if (accept2) acc.c[aniso ? kStatH2mcAcc : kStatIsoAcc]++;
+    }
+    // weighted splats (delayed.cpp:547-561)
+    const float w1 = a1;
+    const float w2 = (1.0f - w1) * a2;
+    const float wc = 1.0f - w1 - w2;
+    if (!p.accMap) {
+        if (cur.valid && wc > 0.0f && cur.hasSplat) sp[0] = weighted_splat_of(W, H, cur.splat, wc);
+        if (w1 > 0.0f && F.hasSplat) sp[1] = weighted_splat_of(W, H, F.splat, w1);
+        if (w2 > 0.0f && S.hasSplat) sp[2] = weighted_splat_of(W, H, S.splat, w2);
+    }
+    // accept / swap (delayed.cpp:563-606)
+    int *perm = p.d.perm + 3 * i;
+    if (flags & kAccept1) {
+        const int t = perm[0];
+        perm[0] = perm[1];
+        perm[1] = t;
+        Slot &nc = slot_of(p.d, i, 0);
+        nc.gaussInit = 0;
+        nc.valid = 1;
+        const Slot &old = slot_of(p.d, i, 1);
+        if (p.accMap && !(flags & kLarge) && old.hasSplat)
+            sp[0] = PendingSplat{splat_pixel(W, H, old.splat[0], old.splat[1], 1.0f, 0.0f, 0.0f), 1.0f, 0.0f, 0.0f};
+    } else if (accept2) {
+        const int t = perm[0];
+        perm[0] = perm[2];
+        perm[2] = t;
+        Slot &nc = slot_of(p.d, i, 0);
+        if (!aniso) nc.gaussInit = 0;
+        nc.valid = 1;
+        const Slot &old = slot_of(p.d, i, 2);
+        if (p.accMap && old.hasSplat)
+            sp[0] = PendingSplat{splat_pixel(W, H, old.splat[0], old.splat[1], 0.0f, 1.0f, 0.0f), 0.0f, 1.0f, 0.0f};
+    }
+    sc.flags = flags | (accept2 ? kAccept2 : 0);
+    sc.a2 = a2;
+}
+
+static __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes, on);
     const int i = p.c0 + t;
     StatAcc acc;
-    const int W = p.s.cam.width, H = p.s.cam.height;
     // up to three splats per chain, added warp-aggregated after the chain's work
     PendingSplat sp[3] = {{-1, 0.0f, 0.0f, 0.0f}, {-1, 0.0f, 0.0f, 0.0f}, {-1, 0.0f, 0.0f, 0.0f}};
-    if (on && t < p.N && (p.d.scr[i].flags & kActive)) {
-        Scratch &sc = p.d.scr[i];
-        const int flags = sc.flags;
-        const float a1 = sc.a1;
-        float a2 = sc.a2;
-        bool accept2 = false;
-        Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 2ull);
-        Slot &cur = slot_of(p.d, i, 0);
-        Slot &F = slot_of(p.d, i, 1);
-        Slot &S = slot_of(p.d, i, 2);
-        const bool aniso = flags & kAniso;
-        if (flags & kSecond) {
-            const int dim = path_dim(cur.rec.c, cur.rec.l);
-            if (aniso) {
-                if (flags & kZValid) {
-                    a2 = float(::exp(sc.logRatio)) * S.ss / cur.ss;
-                } else {
-                    a2 = 0.0f;
-                }
-            }
-            if (is_invalid(a2)) {
-                a2 = 0.0f;
-            } else if (flags & kSingle) {
-                // the usual MH acceptance, Clamp(a, 0, 1) (h2mc.cpp:580-584, 220)
-                a2 = clamp01(a2);
-                accept2 = flip_coin(a2, rng.uniform());
-            } else {
-                bool draw;
-                a2 = dr_second_acceptance(p.drType, a1, a2, sc.aStar, F.ss, S.ss, dim, cur.rec.u, F.rec.u, S.rec.u,
-                                          p.sigma1, draw);
-                if (draw) accept2 = flip_coin(a2, rng.uniform());
-            }
-            if (accept2) acc.c[aniso ? kStatH2mcAcc : kStatIsoAcc]++;
-        }
-        // weighted splats (delayed.cpp:547-561)
-        const float w1 = a1;
-        const float w2 = (1.0f - w1) * a2;
-        const float wc = 1.0f - w1 - w2;
-        if (!p.accMap) {
-            if (cur.valid && wc > 0.0f && cur.hasSplat) sp[0] = weighted_splat_of(W, H, cur.splat, wc);
-            if (w1 > 0.0f && F.hasSplat) sp[1] = weighted_splat_of(W, H, F.splat, w1);
-            if (w2 > 0.0f && S.hasSplat) sp[2] = weighted_splat_of(W, H, S.splat, w2);
-        }
-        // accept / swap (delayed.cpp:563-606)
-        int *perm = p.d.perm + 3 * i;
-        if (flags & kAccept1) {
-            const int t = perm[0];
-            perm[0] = perm[1];
-            perm[1] = t;
-            Slot &nc = slot_of(p.d, i, 0);
-            nc.gaussInit = 0;
-            nc.valid = 1;
-            const Slot &old = slot_of(p.d, i, 1);
-            if (p.accMap && !(flags & kLarge) && old.hasSplat)
-                sp[0] = PendingSplat{splat_pixel(W, H, old.splat[0], old.splat[1], 1.0f, 0.0f, 0.0f), 1.0f, 0.0f, 0.0f};
-        } else if (accept2) {
-            const int t = perm[0];
-            perm[0] = perm[2];
-            perm[2] = t;
-            Slot &nc = slot_of(p.d, i, 0);
-            if (!aniso) nc.gaussInit = 0;
-            nc.valid = 1;
-            const Slot &old = slot_of(p.d, i, 2);
-            if (p.accMap && old.hasSplat)
-                sp[0] = PendingSplat{splat_pixel(W, H, old.splat[0], old.splat[1], 0.0f, 1.0f, 0.0f), 0.0f, 1.0f, 0.0f};
-        }
-        sc.flags = flags | (accept2 ? kAccept2 : 0);
-        sc.a2 = a2;
-    }
+    if (on && t < p.N && (p.d.scr[i].flags & kActive)) finish_chain(p, i, iter, acc, sp);
     for (int k = 0; k < 3; k++) warp_splat(p.d.film, sp[k]);
     flush_stats(acc, p.d.stats);
 }
 
 // One chain group's iteration counter, advanced after each of its iterations
 // on the group's stream (so a captured iteration replays as the next one).
-__global__ void k_advance_iter(int *iterp) { *iterp += 1; }
-__global__ void k_set_iters(int *iters, int n, int value) {
+static __global__ void k_advance_iter(int *iterp) { *iterp += 1; }
+static __global__ void k_set_iters(int *iters, int n, int value) {
     for (int g = threadIdx.x; g < n; g += blockDim.x) iters[g] = value;
 }
 
 // A chain group's list counters, work-class histogram and (nWave > 0) the
 // queue counters of its wavefront stage passes, at the start of an iteration.
-__global__ void k_reset_counters(int *counters, int *hist, int *waveCount, int nWave) {
+static __global__ void k_reset_counters(int *counters, int *hist, int *waveCount, int nWave) {
     if (threadIdx.x < 4) counters[threadIdx.x] = 0;
     for (int k = threadIdx.x; k < kPlanBins; k += blockDim.x) hist[k] = 0;
     for (int k = threadIdx.x; k < nWave; k += blockDim.x) waveCount[k] = 0;
@@ -613,7 +636,7 @@ struct SinkTarget {
     }
 };
 
-__global__ void __launch_bounds__(128) k_bootstrap(SceneView s, unsigned long long seed, int numSamples, int minDepth,
+static __global__ void __launch_bounds__(128) k_bootstrap(SceneView s, unsigned long long seed, int numSamples, int minDepth,
                                                    int maxDepth, BootRecord *out, int *count, int cap, int *overflow) {
     const int sidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (sidx >= numSamples) return;
@@ -623,7 +646,7 @@ __global__ void __launch_bounds__(128) k_bootstrap(SceneView s, unsigned long lo
     generate_path_bidir(s, minDepth, maxDepth, rng, f, sink);
 }
 
-__global__ void __launch_bounds__(128) k_seed(RunParams p, unsigned long long bootSeed, const int *sampleOf,
+static __global__ void __launch_bounds__(128) k_seed(RunParams p, unsigned long long bootSeed, const int *sampleOf,
                                               const int *techC, const int *techL, int minDepth, int maxDepth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.N) return;
@@ -661,7 +684,7 @@ struct SinkSplat {
     DEV void operator()(const Emit &e) { splat(film, W, H, e.screen[0], e.screen[1], e.rgb.x, e.rgb.y, e.rgb.z); }
 };
 
-__global__ void __launch_bounds__(128) k_direct(SceneView s, unsigned long long seed, int spp, int minDepth,
+static __global__ void __launch_bounds__(128) k_direct(SceneView s, unsigned long long seed, int spp, int minDepth,
                                                 int maxDepth, float4 *film) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long npix = (long long)s.cam.width * s.cam.height;

@@ -62,7 +62,8 @@ class Options(C.Structure):
                 ("seed", C.c_uint64), ("device", C.c_int32), ("use_graph", C.c_int32),
                 ("chain_groups", C.c_int32), ("stage_lanes", C.c_int32), ("deriv_warps", C.c_int32),
                 ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32),
-                ("graph_iters", C.c_int32), ("wavefront", C.c_int32)]
+                ("graph_iters", C.c_int32), ("wavefront", C.c_int32), ("persistent", C.c_int32),
+                ("team_sms", C.c_int32), ("wait_limit", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -143,7 +144,11 @@ _lib = None
 
 
 class DrmltError(RuntimeError):
-    pass
+    """A libdrmlt call failed: `code` is its DRMLT_E_* return value."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 def lib():
@@ -163,7 +168,7 @@ def lib():
 
 def check(rc: int):
     if rc != 0:
-        raise DrmltError("libdrmlt error %d: %s" % (rc, lib().drmlt_last_error().decode()))
+        raise DrmltError("libdrmlt error %d: %s" % (rc, lib().drmlt_last_error().decode()), rc)
 
 
 def ptr(a: np.ndarray):

@@ -28,6 +28,8 @@ extern "C" {
 #define DRMLT_E_STATE (-3)     /* call out of order (e.g. run before prepass) */
 #define DRMLT_E_OVERFLOW (-4)  /* a fixed-capacity buffer overflowed */
 #define DRMLT_E_IO (-5)        /* a file could not be written */
+#define DRMLT_E_TIMEOUT (-6)   /* a bounded device-side wait ran out (persistent schedule); the
+                                  handle's chain state is undefined afterwards: destroy it */
 
 #define DRMLT_MAX_LEN 12           /* longest path (segments) a chain may hold */
 #define DRMLT_MAX_DIM 24           /* 2 * DRMLT_MAX_LEN */
@@ -138,8 +140,22 @@ typedef struct drmlt_options {
     int32_t wavefront;            /* path tracing of stage 1, stage 2 and Green's y*: 1 = wavefront
                                      rounds (rays of all chains queued per bounce and traced by a
                                      separate full-warp traversal kernel), 0 = one chain per lane
-                                     traces its whole path; -1 = default (1). Both take identical
+                                     traces its whole path; -1 = default (0). Both take identical
                                      steps; drmlt_autotune times both. */
+    int32_t persistent;           /* chain-loop schedule of drmlt_run for integrator=drmlt: 1 = one
+                                     persistent cooperative kernel per run, in which every chain moves
+                                     through its iterations on its own (work queues between path
+                                     tracing and the H2MC derivative / Gaussian workers, no barrier
+                                     between stages or iterations); 0 = staged (one kernel per stage
+                                     and chain group). Both take identical steps. Default 0;
+                                     drmlt_autotune times both. The h2mc and mcmc integrators are
+                                     always staged. */
+    int32_t team_sms;             /* persistent schedule: SMs that run the derivative / Gaussian
+                                     workers; the others run path tracing (0 = a quarter of the SMs;
+                                     drmlt_autotune picks it) */
+    int32_t wait_limit;           /* persistent schedule: idle polls (about 0.2-0.5 us each) a device
+                                     worker makes without seeing any progress before it gives up and
+                                     the run fails with DRMLT_E_TIMEOUT (0 = 4194304, seconds) */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
