@@ -257,6 +257,16 @@ def config3(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
                          sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5))
 
 
+def config3_deep(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
+    """Config 3 at max depth 10: the derivative check batch's scene (the
+    Lambertian box with the rough-dielectric sphere, paths of up to 20 primary
+    dimensions)."""
+    alpha = float(np.random.default_rng(1003).uniform(0.05, 0.5))
+    return write_cornell(outdir, seed=3, width=256, height=256, phong=False,
+                         options=SceneOptions(maxdepth=10, numchains=4096, spp=spp, type=dr_type),
+                         sphere=dict(center=(-0.45, -0.6, 0.45), radius=0.3, alpha=alpha, ior=1.5))
+
+
 def config_lights(outdir: str, spp: int = 16, dr_type: str = "green") -> str:
     """Config 3 (seed 5) plus a point light of intensity 3 under the ceiling: area
     light, point light and the rough-dielectric sphere together."""

@@ -58,7 +58,7 @@ def _dpt_seconds(spp: int, threads: int, lib: str) -> float:
 
 def main():
     threads = int(sys.argv[1]) if len(sys.argv) > 1 else (os.cpu_count() or 1)
-    lib = os.path.join(REF_OUT, "lib_d%d" % DEPTH, "pathlibbidir.so")
+    lib = os.path.join(REF_OUT, "single", "lib_d%d" % DEPTH, "pathlibbidir.so")
     if not (os.path.exists(DPT) and os.path.exists(lib)):
         sys.exit("build the reference first: make -C oracle/ref, and its depth-%d chad library "
                  "(tests/golden/make_golden.py cfg2)" % DEPTH)

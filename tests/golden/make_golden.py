@@ -15,6 +15,8 @@ synthetic Cornell-box scenes of drmlt/scenegen.py and writes gzipped JSON lines:
                           on a recorded stream, SmallStep::Mutate (both sigmas),
                           PH2MCSmallStep::Mutate, SmallStep::Trace (Green's y*), with
                           their offsets, and Green / Mira second-stage acceptances
+  cfg3d_tech.jsonl.gz     technique paths of config 3 at max depth 10 with the FP64
+                          chad library's log f, gradient and Hessian
   <cfg>_render*.json.gz   a full `dpt -d` render of the scene (the reference's
                           DRIntegrator::Render): its printed acceptance counters
                           and the final image averaged over 16 x 16 blocks
@@ -25,6 +27,7 @@ usage (in a container that has the reference at /root/reference):
   python tests/golden/make_golden.py [--render] [cfg1] [cfg2]   (--render: only the renders)
   python tests/golden/make_golden.py --mesh                     (only cfgM_mesh)
   python tests/golden/make_golden.py --accept [cfg1] ...        (only the acceptance fixtures)
+  python tests/golden/make_golden.py --double                    (cfg3d_tech: FP64 chad, depth 10)
 """
 from __future__ import annotations
 
@@ -165,6 +168,34 @@ def accept(cfg: str):
         shutil.rmtree(tmp)
 
 
+DEEP_COUNT = 240
+
+
+def double_tech():
+    """cfg3d_tech: technique paths of the depth-10 config-3 scene with the FP64
+    chad library's log f, gradient and Hessian (the reference built with
+    PREC=DOUBLE, commondef.h:54-60, chad.h:41-46) and central differences of
+    that gradient."""
+    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "PREC=DOUBLE", "-j8"],
+                          stdout=subprocess.DEVNULL)
+    ref_double = os.path.join(REPO, "oracle", "_ref", "double")
+    libdir = os.path.join(ref_double, "lib_d10")
+    os.makedirs(libdir, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    try:
+        xml = scenegen.config3_deep(os.path.join(tmp, "scene"))
+        out = os.path.join(tmp, "tech.jsonl")
+        subprocess.check_call([os.path.join(ref_double, "ref_harness"), xml, libdir, "10", out, "tech", "1",
+                               str(DEEP_COUNT), "0"], stdout=subprocess.DEVNULL)
+        dst = os.path.join(HERE, "cfg3d_tech.jsonl.gz")
+        with open(out, "rb") as f, open(dst, "wb") as raw:
+            with gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as g:
+                shutil.copyfileobj(f, g)
+        print(dst, os.path.getsize(dst))
+    finally:
+        shutil.rmtree(tmp)
+
+
 def mesh():
     subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
     tmp = tempfile.mkdtemp()
@@ -185,6 +216,9 @@ if __name__ == "__main__":
     args = sys.argv[1:]
     if "--mesh" in args:
         mesh()
+        sys.exit(0)
+    if "--double" in args:
+        double_tech()
         sys.exit(0)
     if "--accept" in args:
         for c in [a for a in args if not a.startswith("--")] or list(CONFIGS):

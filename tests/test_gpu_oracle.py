@@ -153,14 +153,49 @@ def test_random_derivatives_vs_fp64_oracle(renderers, oracles, cfg):
             bad_h.append(i)
     n = len(paths)
     assert n > 100
-    # In the miniature config 4 a few deep paths graze the tessellated sphere
-    # from inside, where the single-precision path function itself is not smooth
-    # at the 1e-3 level (central differences of the FP32 gradient change sign
-    # with the step while the FP64 oracle's do not): up to 2% of paths there.
-    tol = max(2, n // (50 if cfg == "cfg4s" else 100))
+    tol = max(2, n // 100)
     assert len(bad_f) <= tol, "log f: %d / %d" % (len(bad_f), n)
     assert len(bad_g) <= tol, "gradient: %d / %d" % (len(bad_g), n)
-    assert len(bad_h) <= tol, "Hessian: %d / %d" % (len(bad_h), n)
+    # The Hessians that miss the bar are explained path by path: the
+    # single-precision path function is not smooth at the 1e-3 level there
+    # (deep paths that graze the tessellated sphere from inside, in the
+    # miniature config 4): central differences of the GPU's own FP32 gradient
+    # at steps 1e-3 and 2e-3 disagree by more than the bar, while the FP64
+    # function's do not. At most 1% of the paths may miss without that reason.
+    rough = _fp32_not_smooth(r, ora, paths, u, bad_h)
+    unexplained = [i for i in bad_h if not rough[i]]
+    assert len(unexplained) <= tol, "Hessian: %d / %d (%d with a non-smooth FP32 gradient)" % (
+        len(unexplained), n, len(bad_h) - len(unexplained))
+    assert len(bad_h) <= max(2, n // 50), "Hessian: %d / %d" % (len(bad_h), n)
+
+
+def _fp32_not_smooth(r, ora, paths, u, idx, steps=(1e-3, 2e-3)):
+    """Whether the FP32 path function of each listed path is not smooth at the
+    1e-3 level where the FP64 one is: central-difference Hessians of the GPU's
+    FP32 gradient at the two steps disagree by more than 1e-3 of their largest
+    entry, while the oracle's FP64 central-difference Hessians at the same
+    steps agree to 1e-3."""
+    out = {}
+    for i in idx:
+        d = 2 * (paths[i]["c"] + paths[i]["l"] - 1)
+        f32, f64 = [], []
+        for h in steps:
+            pp = np.repeat(paths[i:i + 1], 2 * d)
+            uu = np.repeat(u[i:i + 1], 2 * d, axis=0)
+            for j in range(d):
+                uu[2 * j, j] += h
+                uu[2 * j + 1, j] -= h
+            for k in range(2 * d):
+                pp[k]["u"] = uu[k]
+            gp, _ = r.path_grad_hess(pp, uu)
+            f32.append(np.stack([(gp[2 * j, :d] - gp[2 * j + 1, :d]) / (2 * h) for j in range(d)]))
+            _, _, h64 = ora.fd_derivs(paths[i:i + 1], u[i:i + 1].astype(np.float64), h)
+            f64.append(h64[0, :d * d].reshape(d, d))
+        top32 = max(np.max(np.abs(f32[0])), 1e-6)
+        top64 = max(np.max(np.abs(f64[0])), 1e-6)
+        out[i] = bool(np.max(np.abs(f32[0] - f32[1])) > 1e-3 * top32 and
+                      np.max(np.abs(f64[0] - f64[1])) <= 1e-3 * top64)
+    return out
 
 
 @pytest.mark.parametrize("cfg", CFGS)
@@ -208,3 +243,73 @@ def test_ray_hits_vs_oracle(renderers, oracles, cfg):
     og, _ = r.trace_rays(org, d, tmax=1.0, any_hit=True)
     oo, _ = o.trace_rays(org, d, tmax=1.0, any_hit=True)
     assert np.mean((og >= 0) == (oo >= 0)) >= 0.9999
+
+
+def test_ray_hits_at_scale_vs_oracle_bvh(built_lib):
+    """BVH hit parity on the 3.0 M-triangle procedural scene (displaced sphere over a
+    ground grid): 2^20 camera-like rays (from the camera position towards random
+    points of the scene's box), 2^20 bounce rays (from their hits, random
+    directions) and the shadow rays between those hits and random points
+    (src/scene.cpp:80-111: closest hit, and occlusion over t in [tmin, tmax]),
+    the CUDA BVH (binned SAH, csrc/bvh.cpp) against the oracle's own
+    object-median BVH (itself pinned to brute force in tests/test_oracle.py).
+    Bar: the same triangle on >= 99.99% of the rays of each kind, where a
+    different triangle at the same distance (a tie between triangles sharing
+    the hit point: an edge or a vertex of the tessellation) is counted apart."""
+    import oracle_dr
+    from drmlt import procedural
+    from drmlt.integrator import Renderer
+    sd = procedural.config4(chains=256)
+    assert len(sd.positions) > 2_900_000
+    r = Renderer(sd, num_chains=256)
+    o = oracle_dr.Oracle(sd)
+    try:
+        rng = np.random.default_rng(44)
+        n = 1 << 20
+        P = sd.positions.reshape(-1, 3)
+        lo, hi = P.min(0), P.max(0)
+        eye = np.array([0.0, 1.2, 5.5], np.float32)
+        tgt = lo + rng.random((n, 3)) * (hi - lo)
+        d = tgt - eye
+        d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+        org = np.broadcast_to(eye, (n, 3)).astype(np.float32)
+        report = {}
+
+        def closest(org, d, tmin=1e-3):
+            tg, thg = r.trace_rays(org, d, tmin=tmin)
+            to, tho = o.trace_rays(org, d, tmin=tmin, mode="bvh")
+            tie = (tg != to) & (tg >= 0) & (to >= 0) & (np.abs(thg - tho) <= 1e-5 * np.abs(tho))
+            same = tg == to
+            both = same & (tg >= 0)
+            # same triangle: the same distance up to float rounding of the two
+            # Moller-Trumbore evaluations (FMA contraction on the GPU), which
+            # grows where the ray grazes the triangle's plane (t is ill-conditioned
+            # there: 7 of 458,894 camera-ray hits differ by more than 1e-5)
+            rel = np.abs(thg[both] - tho[both]) / np.maximum(np.abs(tho[both]), 1e-6)
+            assert np.mean(rel <= 1e-5) >= 0.9999, np.mean(rel <= 1e-5)
+            return tg, thg, float(np.mean(same)), float(np.mean(tie)), float(np.mean(to >= 0))
+
+        tg, th, same, tie, hits = closest(org, d)
+        report["camera"] = (same, tie, hits)
+        assert hits > 0.3 and same + tie >= 0.9999, report
+        # bounce rays from the hits (offset back along the ray by tmin's scale)
+        h = tg >= 0
+        p = (org[h] + th[h, None] * d[h]).astype(np.float32)
+        d2 = rng.standard_normal(p.shape)
+        d2 = (d2 / np.linalg.norm(d2, axis=1, keepdims=True)).astype(np.float32)
+        tg2, th2, same, tie, hits2 = closest(p, d2)
+        report["bounce"] = (same, tie, hits2)
+        assert hits2 > 0.1 and same + tie >= 0.9999, report
+        # shadow rays of length 1 from the hits towards random points of the box
+        q = (lo + rng.random(p.shape) * (hi - lo)).astype(np.float32)
+        ds = q - p
+        ds = (ds / np.linalg.norm(ds, axis=1, keepdims=True)).astype(np.float32)
+        og, _ = r.trace_rays(p, ds, tmin=1e-3, tmax=1.0, any_hit=True)
+        oo, _ = o.trace_rays(p, ds, tmin=1e-3, tmax=1.0, any_hit=True, mode="bvh")
+        agree = float(np.mean((og >= 0) == (oo >= 0)))
+        report["shadow"] = (agree, float(np.mean(oo >= 0)))
+        assert 0.05 < np.mean(oo >= 0) < 0.95 and agree >= 0.9999, report
+        print(report)
+    finally:
+        r.close()
+        o.close()
