@@ -26,11 +26,15 @@ Keys of the JSON line (ours):
                    and for the plain per-stage-launch drop-in
   roofline         the slowest chain-loop stage against the HBM peak
   cpu_baseline     the oracle's CPU chain loop (all host cores, the oracle's
-                   own BVH) on a bounded sample of the same scene
+                   own BVH) on a bounded sample of the same scene, with its
+                   calibration against the reference's own dpt chain loop
+  schedule_ms_per_iteration
+                   the staged (default), wavefront and persistent schedules of
+                   the same steps, a few iterations each
 
 --impl reference times that CPU chain loop alone on the same workload (the
-reference's own dpt does not build on this Arm host: Embree 2.17 and its SSE
-intrinsics are x86-only). Under torchrun (N > 1) every rank renders its own
+reference's sources, from which its dpt is built, are not on the GPU host; the
+calibration factor relates the two). Under torchrun (N > 1) every rank renders its own
 replica of the chains (different random streams); there is no collective in
 the timed region, and --gpus must equal the torchrun world size.
 """
@@ -252,7 +256,7 @@ def run_ours(args, world, rank, local):
     r2 = Renderer(sd, device=local, seed=seed + 1, autotune=0, stage_lanes=shape["chains_per_warp"],
                   stage2_lanes=shape["stage2_chains_per_warp"], deriv_warps=shape["derivative_warps"],
                   use_graph=1 if shape["graph_iterations"] else 0, graph_iters=max(1, shape["graph_iterations"]),
-                  wavefront=shape["wavefront"])
+                  wavefront=shape["wavefront"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"])
     r2.prepass()
     t1 = time.perf_counter()
     e_done = 0
@@ -325,6 +329,7 @@ def run_ours(args, world, rank, local):
             relmse = time_to_relmse(sd, local, ref, ref_spp, spp=spp)
             relmse_plain = time_to_relmse(sd, local, ref, ref_spp, spp=spp, plain=True)
         cpu = None if args.no_cpu else cpu_baseline_sample(sd, seconds=15.0)
+        schedules = None if args.no_schedules else schedule_times(sd, local, seed + 2, shape)
         gb = (3 * SLOT_B + 3 * GAUSS_B + SCRATCH_B) * N / 1e9
         out = {
             "metric": METRIC, "value": value, "unit": "mutations/s", "n_gpus": world, "steps": args.steps,
@@ -344,6 +349,7 @@ def run_ours(args, world, rank, local):
             "rays": rays,
             "time_to_relmse": relmse,
             "time_to_relmse_plain": relmse_plain,
+            "schedule_ms_per_iteration": schedules,
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "wall_s_timed_region": wall,
@@ -449,6 +455,18 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False)
             "checkpoints": checkpoints}
 
 
+# The port against the reference's own chain loop on the same scene and
+# threads, measured where the reference builds (x86, 8 threads, the config-2
+# scene; oracle/ref/calibrate_cpu.py): the reference's dpt ran its chain loop
+# at 0.416 M mutations/s (two renders differing only in spp, so prepass and
+# direct pass cancel), the port at 0.181 M/s. The port is the slower of the
+# two: CPU ratios against it overstate the GPU's lead by about 1 / 0.435.
+CPU_CALIBRATION = {"port_over_reference": 0.435, "reference_mutations_per_s": 416343.0,
+                   "port_mutations_per_s": 180926.0,
+                   "measured": "x86_64, 8 threads, Phong Cornell box 1024x1024 depth 8 16384 chains mira; "
+                               "reference dpt -d chain loop (spp 3 minus spp 1) vs the oracle port"}
+
+
 def cpu_baseline_sample(sd, seconds: float = 15.0):
     """The oracle's CPU restatement of the chain loop (its own BVH) on this
     host's cores, on a bounded sample of the same workload."""
@@ -457,7 +475,28 @@ def cpu_baseline_sample(sd, seconds: float = 15.0):
         import oracle_dr  # noqa: WPS433
     except Exception as e:  # oracle not built on this machine
         return {"value": None, "unit": "mutations/s", "cores": 0, "kind": "port", "sample": "unavailable: %s" % e}
-    return oracle_dr.cpu_throughput_scene(sd, seconds=seconds)
+    out = oracle_dr.cpu_throughput_scene(sd, seconds=seconds)
+    out["calibration"] = CPU_CALIBRATION
+    return out
+
+
+def schedule_times(sd, device, seed, shape, iterations=8):
+    """ms per iteration of the three chain-loop schedules (they take identical
+    steps): staged at the tuned shape, wavefront rounds, and the persistent
+    cooperative kernel (a quarter and half of the SMs as team workers)."""
+    from drmlt.integrator import Renderer
+    base = dict(autotune=0, stage_lanes=shape["chains_per_warp"], stage2_lanes=shape["stage2_chains_per_warp"],
+                deriv_warps=shape["derivative_warps"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"])
+    out = {}
+    for name, kw in (("staged", {}), ("wavefront", dict(wavefront=1)), ("persistent_quarter", dict(persistent=1)),
+                     ("persistent_half", dict(persistent=1, team_sms=76))):
+        r = Renderer(sd, device=device, seed=seed, **base, **kw)
+        r.prepass()
+        r.run(4)
+        r.run(iterations)
+        out[name] = r.last_run_ms() / iterations
+        r.close()
+    return out
 
 
 def run_reference(args, world, rank):
@@ -483,6 +522,7 @@ def run_reference(args, world, rank):
     v = statistics.median([x["value"] for x in vals])
     cpu = dict(vals[0])
     cpu["value"] = v
+    cpu["calibration"] = CPU_CALIBRATION
     cpu["sample"] = "median of %d samples of %.1f s: %s" % (len(vals), per, vals[0]["sample"])
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "mutations/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -499,6 +539,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE measurement")
+    ap.add_argument("--no-schedules", action="store_true", help="skip the wavefront / persistent schedule timings")
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--ref-spp", type=int, default=0, help="samples per pixel of the relMSE reference render")
     ap.add_argument("--relmse-spp", type=int, default=0, help="spp budget of the time-to-relMSE renders")

@@ -95,6 +95,8 @@ struct RunParams {
     int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch
     int lanes;           // chains per warp in the per-chain stage kernels (1..32)
     int lanes2;          // chains per warp in the second-stage list kernels (1..32)
+    int headChains;      // k_stage1: the first headChains chains of the stage-1 order (the
+    int headLanes;       // longest work classes) run headLanes to a warp, the rest `lanes`
     const int *iterp;    // the group's current iteration (device memory)
     int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
     int lists;           // 1: the stage epilogues append the chain to the group's work lists (the
@@ -118,6 +120,29 @@ DEV int sparse_index(int lanes, bool &active) {
 }
 inline int sparse_blocks(int n, int lanes) {
     const int warps = (n + lanes - 1) / lanes;
+    return (warps + kStageBlock / 32 - 1) / (kStageBlock / 32);
+}
+
+// Stage 1 in two tiers: the chains are in descending work-class order, so the
+// first headChains are the longest traces; they get headLanes chains per warp
+// (fewer lanes whose divergent work a warp serialises on the iteration's
+// critical path), the rest `lanes` per warp.
+HD int head_warps(int headChains, int headLanes) { return headChains > 0 ? (headChains + headLanes - 1) / headLanes : 0; }
+DEV int stage1_index(int headChains, int headLanes, int lanes, bool &active) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int hw = head_warps(headChains, headLanes);
+    if (warp < hw) {
+        const int t = warp * headLanes + lane;
+        active = lane < headLanes && t < headChains;
+        return t;
+    }
+    active = lane < lanes;
+    return headChains + (warp - hw) * lanes + lane;
+}
+inline int stage1_blocks(int n, int headChains, int headLanes, int lanes) {
+    const int head = headChains < n ? headChains : n;
+    const int warps = head_warps(head, headLanes) + (n - head + lanes - 1) / lanes;
     return (warps + kStageBlock / 32 - 1) / (kStageBlock / 32);
 }
 

@@ -19,7 +19,8 @@ __global__ void __launch_bounds__(128, 4) k_derivs(RunParams p, int which) {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int teams = (gridDim.x * blockDim.x >> 5) / p.derivWarps;
     const int n = p.d.counters[which == 0 ? 0 : 1];
-    for (int w = gw / p.derivWarps; w < n; w += teams) {
+    for (int k = gw / p.derivWarps; k < n; k += teams) {
+        const int w = n - 1 - k;  // longest paths first: the lists fill in the order their stage finishes
         const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
         const Slot &st = slot_of(p.d, chain, which);
         derivs_for_path(p.s, st.rec, st.ss, p.maxDerv, p.d.grad + size_t(w) * kMaxDim,

@@ -8,34 +8,41 @@
 
 namespace drmlt {
 
+// Hessian entry `pidx` (row-major over the upper triangle) of log f of path r
+// (dimension dim) by one hyper-dual evaluation seeded in u_i and u_j; the
+// diagonal entries also give the gradient.
+DEV void derivs_entry(const SceneView &s, const PathRec &r, int dim, int pidx, float *g, float *H) {
+    int i0 = 0, rem = pidx;
+    while (rem >= dim - i0) {
+        rem -= dim - i0;
+        i0++;
+    }
+    const int j0 = i0 + rem;
+    HyperDual u[kMaxDim];
+    for (int k = 0; k < dim; k++) u[k] = HyperDual(r.u[k], k == i0 ? 1.0f : 0.0f, k == j0 ? 1.0f : 0.0f, 0.0f);
+    const HyperDual f = ad_eval_path<HyperDual>(s, r, u);
+    H[i0 * dim + j0] = f.ab;
+    H[j0 * dim + i0] = f.ab;
+    if (i0 == j0) g[i0] = f.a;
+}
+
+// Whether the chain loop takes derivatives of a path of L segments and score ss
+// (else the isotropic fallback of drsmallstep.cpp:133-163 with zero rows).
+DEV bool derivs_wanted(int L, float ss, int maxDerv) { return L <= maxDerv && ss > 1e-15f; }
+
 // A team of `team` threads strides over the D(D+1)/2 Hessian entries.
 DEV void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H, int member,
                          int team) {
     const int lane = member;
     const int L = r.c + r.l - 1;
     const int dim = 2 * L;
-    if (!(L <= maxDerv && ss > 1e-15f)) {
+    if (!derivs_wanted(L, ss, maxDerv)) {
         for (int k = lane; k < dim; k += team) g[k] = 0.0f;
         for (int k = lane; k < dim * dim; k += team) H[k] = 0.0f;
         return;
     }
     const int npairs = dim * (dim + 1) / 2;
-    for (int pidx = lane; pidx < npairs; pidx += team) {
-        // decode pidx -> (i0, j0), i0 <= j0, row-major over the upper triangle
-        int i0 = 0, rem = pidx;
-        while (rem >= dim - i0) {
-            rem -= dim - i0;
-            i0++;
-        }
-        const int j0 = i0 + rem;
-        HyperDual u[kMaxDim];
-        for (int k = 0; k < dim; k++)
-            u[k] = HyperDual(r.u[k], k == i0 ? 1.0f : 0.0f, k == j0 ? 1.0f : 0.0f, 0.0f);
-        const HyperDual f = ad_eval_path<HyperDual>(s, r, u);
-        H[i0 * dim + j0] = f.ab;
-        H[j0 * dim + i0] = f.ab;
-        if (i0 == j0) g[i0] = f.a;
-    }
+    for (int pidx = lane; pidx < npairs; pidx += team) derivs_entry(s, r, dim, pidx, g, H);
 }
 
 }  // namespace drmlt

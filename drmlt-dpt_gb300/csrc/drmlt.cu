@@ -196,6 +196,8 @@ struct Renderer {
         // the second-stage lists are compacted and short: fewer chains per warp,
         // more warps (config 2: 0.843 ms per iteration at 4 against 0.871 at 16)
         p.lanes2 = opt.stage2_lanes > 0 ? std::min(opt.stage2_lanes, 32) : std::min(p.lanes, 4);
+        p.headChains = opt.head_chains > 0 ? opt.head_chains : 0;
+        p.headLanes = opt.head_lanes > 0 ? std::min(opt.head_lanes, 32) : 2;
         p.iterp = dIters;
         p.derivWarps = opt.deriv_warps > 0 ? std::min(opt.deriv_warps, 4) : 2;
         p.lists = 1;
@@ -511,6 +513,7 @@ struct Renderer {
             if ((rc = alloc(&waveRayD[b], size_t(N)))) return rc;
         }
         if ((rc = alloc(&waveHit, size_t(N)))) return rc;
+
         if ((rc = alloc(&waveCount, size_t(3) * kWaveCountStride * G))) return rc;
         CK(cudaMemset(waveCount, 0, size_t(3) * kWaveCountStride * G * sizeof(int)));
         if ((rc = alloc(&cv.counters, 4 * size_t(G)))) return rc;
@@ -669,6 +672,7 @@ struct Renderer {
         const RunParams p = params(g);
         const int nb = (p.N + kStageBlock - 1) / kStageBlock;
         const int nbS = sparse_blocks(p.N, p.lanes);
+        const int nbS1 = stage1_blocks(p.N, p.headChains, p.headLanes, p.lanes);
         const int nbS2 = sparse_blocks(p.N, p.lanes2);
         const int nbWarp = std::min((p.N * 32 * p.derivWarps + 127) / 128, derivsGrid);
         const int nbG = std::min(p.N, gaussGrid);
@@ -682,7 +686,7 @@ struct Renderer {
                 k_plan<<<nb, kStageBlock, 0, s>>>(p);
                 k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
                 if (p.wave) return 3 + launch_wave<1>(p, g, s);
-                k_stage1<<<nbS, kStageBlock, 0, s>>>(p);
+                k_stage1<<<nbS1, kStageBlock, 0, s>>>(p);
                 return 4;
             case 1: launch_derivs(p, 0, nbWarp, s); return 1;
             case 2:
@@ -904,10 +908,11 @@ struct Renderer {
     // Launch-shape autotuner: after `per` untimed iterations (past the first
     // iterations' transient), times `per` real iterations under each candidate
     // in two passes of opposite order (so that a drift of the iteration cost
-    // over the render cancels) and keeps the fastest: first wavefront against
-    // per-lane path tracing, then the number of chains per warp in the
+    // over the render cancels) and keeps the fastest: the number of chains per warp in the
     // per-chain stage kernels, then the number of warps sharing one chain's
-    // derivatives, then (graphs on, `per` a multiple of 4) the number of
+    // derivatives, then the stage-1 head tier (none, or the longest half of the
+    // chains at half as many per warp, the rest at the tuned count or twice it),
+    // then (graphs on, `per` a multiple of 4) the number of
     // iterations per graph launch. The iterations are part of the render:
     // the launch shape never changes which steps the chains take. Stops early
     // when the render runs out of iterations.
@@ -935,17 +940,6 @@ struct Renderer {
         };
         float warm = 0.0f;
         if (int rc = trial(bestL, bestW, warm)) return rc;
-        // path tracing: wavefront rounds or one chain per lane
-        {
-            float tv[2] = {0, 0};
-            for (int pass = 0; pass < 2 && !out; pass++)
-                for (int k = 0; k < 2 && !out; k++) {
-                    const int i = pass == 0 ? k : 1 - k;
-                    opt.wavefront = i;
-                    if (int rc = trial(bestL, bestW, tv[i])) return rc;
-                }
-            if (!out) opt.wavefront = tv[1] <= tv[0] ? 1 : 0;
-        }
         // chains per warp
         float tl[5] = {0, 0, 0, 0, 0};
         for (int pass = 0; pass < 2 && !out; pass++)
@@ -971,6 +965,30 @@ struct Renderer {
             for (int i = 1; i < 3; i++)
                 if (tw[i] < tw[bi]) bi = i;
             bestW = kWarps[bi];
+        }
+        // two-tier stage 1: no head tier; the longest half of each group's
+        // chains at half the chains per warp; the same with twice the chains
+        // per warp for the shorter half (config 4: 4.21, 4.21, 4.02 ms per
+        // iteration at 16 chains per warp)
+        {
+            const int hl = std::max(1, bestL / 2);
+            const int heads[3] = {0, chunk / 2, chunk / 2};
+            const int tails[3] = {bestL, bestL, std::min(32, 2 * bestL)};
+            float th[3] = {0, 0, 0};
+            for (int pass = 0; pass < 2 && !out; pass++)
+                for (int k = 0; k < 3 && !out; k++) {
+                    const int i = pass == 0 ? k : 2 - k;
+                    opt.head_chains = heads[i];
+                    opt.head_lanes = hl;
+                    if (int rc = trial(tails[i], bestW, th[i])) return rc;
+                }
+            int bi = 0;
+            if (!out)
+                for (int i = 1; i < 3; i++)
+                    if (th[i] < th[bi]) bi = i;
+            opt.head_chains = heads[bi];
+            opt.head_lanes = hl;
+            bestL = tails[bi];
         }
         // iterations per graph launch
         if (opt.use_graph && per % 4 == 0) {
@@ -1138,6 +1156,14 @@ int drmlt_get_launch_shape(void *handle, int *stage_lanes, int *stage2_lanes, in
     if (stage2_lanes) *stage2_lanes = p.lanes2;
     if (deriv_warps) *deriv_warps = p.derivWarps;
     if (graph_iters) *graph_iters = r->opt.use_graph ? r->graphIters : 0;
+    return DRMLT_OK;
+}
+
+int drmlt_get_head_tier(void *handle, int *head_chains, int *head_lanes) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    const RunParams p = static_cast<const Renderer *>(handle)->params();
+    if (head_chains) *head_chains = p.headChains;
+    if (head_lanes) *head_lanes = p.headLanes;
     return DRMLT_OK;
 }
 

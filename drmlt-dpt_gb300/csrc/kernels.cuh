@@ -235,7 +235,7 @@ DEV int run_perturb(const SceneView &s, const PathRec &in, const float *off, J &
 static __global__ void __launch_bounds__(kStageBlock) k_stage1(RunParams p) {
     const int iter = *p.iterp;
     bool on;
-    const int t = sparse_index(p.lanes, on);
+    const int t = stage1_index(p.headChains < p.N ? p.headChains : p.N, p.headLanes, p.lanes, on);
     StatAcc acc;
     if (on && t < p.N) {
         const int i = p.d.order[t];
@@ -301,8 +301,8 @@ DEV void gauss_for_entry(const RunParams &p, int which, int w, double *gsm) {
 static __global__ void __launch_bounds__(32 * kGaussTeamWarps) k_gauss(RunParams p, int which) {
     extern __shared__ double gsm[];
     const int n = p.d.counters[which == 0 ? 0 : 1];
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        gauss_for_entry(p, which, w, gsm);
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        gauss_for_entry(p, which, n - 1 - k, gsm);  // longest paths first (the lists fill shortest first)
         __syncthreads();  // the block's shared scratch is reused by its next entry
     }
 }
@@ -395,12 +395,18 @@ DEV void stage2_end(const RunParams &p, int i, int st, const Emit &e) {
 }
 
 // Over the group's second-stage list only (compacted by stage 1).
+// The second-stage list fills in the order stage 1 finishes its chains, so the
+// longest traces come last; the list kernels take it from the back, longest
+// first, so that the slowest chains start first and the short ones fill in.
+DEV int longest_first(const int *list, int n, int t) { return list[n - 1 - t]; }
+
 static __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes2, on);
-    if (!on || t >= p.d.counters[2]) return;
-    const int i = p.d.listS[t];
+    const int n = p.d.counters[2];
+    if (!on || t >= n) return;
+    const int i = longest_first(p.d.listS, n, t);
     Rng rng;
     float off[kMaxDim];
     PathM m;
@@ -436,8 +442,9 @@ static __global__ void __launch_bounds__(kStageBlock) k_ystar(RunParams p) {
     const int iter = *p.iterp;
     bool on;
     const int t = sparse_index(p.lanes2, on);
-    if (!on || t >= p.d.counters[2]) return;
-    const int i = p.d.listS[t];
+    const int n = p.d.counters[2];
+    if (!on || t >= n) return;
+    const int i = longest_first(p.d.listS, n, t);
     Rng rng;
     float off[kMaxDim];
     PathM m;

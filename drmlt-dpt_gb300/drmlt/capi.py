@@ -62,7 +62,8 @@ class Options(C.Structure):
                 ("seed", C.c_uint64), ("device", C.c_int32), ("use_graph", C.c_int32),
                 ("chain_groups", C.c_int32), ("stage_lanes", C.c_int32), ("deriv_warps", C.c_int32),
                 ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32),
-                ("graph_iters", C.c_int32), ("wavefront", C.c_int32), ("persistent", C.c_int32),
+                ("graph_iters", C.c_int32), ("wavefront", C.c_int32), ("head_chains", C.c_int32),
+                ("head_lanes", C.c_int32), ("persistent", C.c_int32),
                 ("team_sms", C.c_int32), ("wait_limit", C.c_int32)]
 
 
@@ -114,6 +115,7 @@ _SIGS = {
                                           C.POINTER(C.c_int)]),
     "drmlt_get_partial_film": (C.c_int, [C.c_void_p, C.c_void_p]),
     "drmlt_get_wavefront": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "drmlt_get_head_tier": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "drmlt_write_exr": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_void_p]),
     "drmlt_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "drmlt_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),

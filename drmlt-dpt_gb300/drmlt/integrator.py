@@ -142,6 +142,10 @@ class Renderer:
         w = C.c_int()
         capi.check(capi.lib().drmlt_get_wavefront(self.handle, C.byref(w)))
         shape["wavefront"] = w.value
+        hc, hl = C.c_int(), C.c_int()
+        capi.check(capi.lib().drmlt_get_head_tier(self.handle, C.byref(hc), C.byref(hl)))
+        shape["head_chains"] = hc.value
+        shape["head_lanes"] = hl.value
         return shape
 
     def fma_benchmark(self, fp64: bool = False, iterations: int | None = None) -> dict:

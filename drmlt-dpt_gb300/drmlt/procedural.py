@@ -264,22 +264,28 @@ def config5(seed: int = 5, spp: int = 16, dr_type: str = "mira", width: int = 20
 def main(argv=None):
     """Renders a few chain-loop iterations of a procedural scene (and optionally
     one ray-benchmark pass) -- a small driver for profiling runs:
-    python -m drmlt.procedural config4 --iterations 4 --lanes 4 --warps 4 --rays bounce"""
+    python -m drmlt.procedural config4 --iterations 4 --lanes 16 --warps 2 --graph 1
+    (--wavefront 1 or --persistent 1 --team-sms T select the other schedules)"""
     import argparse
     from .integrator import Renderer
     ap = argparse.ArgumentParser()
     ap.add_argument("scene", choices=["config4", "config5"])
     ap.add_argument("--iterations", type=int, default=4)
     ap.add_argument("--lanes", type=int, default=0, help="chains per warp (0: library default)")
+    ap.add_argument("--lanes2", type=int, default=0, help="chains per warp of the second-stage kernels")
     ap.add_argument("--warps", type=int, default=0, help="derivative warps per chain (0: library default)")
     ap.add_argument("--graph", type=int, default=0, help="replay iterations as CUDA graphs")
+    ap.add_argument("--wavefront", type=int, default=0, help="path tracing in wavefront rounds")
+    ap.add_argument("--persistent", type=int, default=0, help="the persistent cooperative schedule")
+    ap.add_argument("--team-sms", type=int, default=0, help="persistent schedule: SMs of the team workers")
     ap.add_argument("--rays", default="", choices=["", "primary", "bounce", "shadow"])
     a = ap.parse_args(argv)
     sd = globals()[a.scene]()
-    r = Renderer(sd, seed=77, use_graph=a.graph, stage_lanes=a.lanes, deriv_warps=a.warps)
+    r = Renderer(sd, seed=77, use_graph=a.graph, stage_lanes=a.lanes, stage2_lanes=a.lanes2, deriv_warps=a.warps,
+                 wavefront=a.wavefront, persistent=a.persistent, team_sms=a.team_sms)
     r.prepass()
     r.run(a.iterations)
-    out = {"mutations": r.stats()["mutations"]}
+    out = {"mutations": r.stats()["mutations"], "run_ms": r.last_run_ms()}
     if a.rays:
         out["rays"] = r.ray_benchmark(a.rays, 1 << 21, 1)
     r.close()

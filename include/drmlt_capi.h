@@ -141,18 +141,20 @@ typedef struct drmlt_options {
                                      rounds (rays of all chains queued per bounce and traced by a
                                      separate full-warp traversal kernel), 0 = one chain per lane
                                      traces its whole path; -1 = default (0). Both take identical
-                                     steps; drmlt_autotune times both. */
+                                     steps. */
+    int32_t head_chains;          /* stage 1 of the staged schedule: the first head_chains chains of
+                                     each group's work-class order (the longest traces) run
+                                     head_lanes to a warp, the others stage_lanes (0 = off) */
+    int32_t head_lanes;           /* chains per warp of those head chains, 1..32 (0 = 2) */
     int32_t persistent;           /* chain-loop schedule of drmlt_run for integrator=drmlt: 1 = one
                                      persistent cooperative kernel per run, in which every chain moves
                                      through its iterations on its own (work queues between path
                                      tracing and the H2MC derivative / Gaussian workers, no barrier
                                      between stages or iterations); 0 = staged (one kernel per stage
-                                     and chain group). Both take identical steps. Default 0;
-                                     drmlt_autotune times both. The h2mc and mcmc integrators are
-                                     always staged. */
+                                     and chain group). Both take identical steps. Default 0. The h2mc
+                                     and mcmc integrators are always staged. */
     int32_t team_sms;             /* persistent schedule: SMs that run the derivative / Gaussian
-                                     workers; the others run path tracing (0 = a quarter of the SMs;
-                                     drmlt_autotune picks it) */
+                                     workers; the others run path tracing (0 = a quarter of the SMs) */
     int32_t wait_limit;           /* persistent schedule: idle polls (about 0.2-0.5 us each) a device
                                      worker makes without seeing any progress before it gives up and
                                      the run fails with DRMLT_E_TIMEOUT (0 = 4194304, seconds) */
@@ -237,18 +239,21 @@ int drmlt_last_run_ms(void *handle, float *ms);
 /* Kernels launched by drmlt_run on this handle so far (all chain groups). */
 int drmlt_kernel_launches(void *handle, int64_t *n);
 
-/* Launch-shape autotuner (after drmlt_prepass): after one untimed run of
- * `iterations_per_candidate` iterations, times that many iterations of the
- * render under wavefront and per-lane path tracing, then under each candidate
- * chains-per-warp count of the per-chain kernels (2, 4, 8, 16, 32), then each
- * derivative team size (1, 2, 4 warps), every choice in two passes of opposite
- * order (CUDA events), and keeps the fastest (chains per warp and team size
- * written to the outputs, which may be NULL; the wavefront choice is reported
- * by drmlt_get_launch_shape): 21 runs. With
- * CUDA graphs on and iterations_per_candidate a multiple of 4 it then times
- * graphs of 1 and of 4 iterations (4 more runs) and keeps the faster.
- * The iterations count toward the render; the launch shape does not change the
- * chains' steps. */
+/* Launch-shape autotuner (after drmlt_prepass) of the staged schedule: after
+ * one untimed run of `iterations_per_candidate` iterations, times that many
+ * iterations of the render under each candidate chains-per-warp count of the
+ * per-chain kernels (2, 4, 8, 16, 32), then each derivative team size (1, 2, 4
+ * warps), then the stage-1 head tier (head_chains 0, or half of a chain
+ * group at half the chains per warp with the other half at the tuned count or
+ * twice it), every choice in two passes of
+ * opposite order (CUDA events), and keeps the fastest (chains per warp and
+ * team size written to the outputs, which may be NULL; the head tier is
+ * reported by drmlt_get_head_tier): 23 runs. With CUDA graphs on and
+ * iterations_per_candidate a multiple of 4 it then times graphs of 1 and of 4
+ * iterations (4 more runs) and keeps the faster. The wavefront and persistent
+ * schedules are not candidates (both measured slower on every benchmark scene;
+ * they stay selectable through drmlt_options). The iterations count toward the
+ * render; the launch shape does not change the chains' steps. */
 int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes, int *deriv_warps);
 
 /* The launch shape the next drmlt_run uses (after drmlt_autotune: the tuned
@@ -258,6 +263,10 @@ int drmlt_autotune(void *handle, int iterations_per_candidate, int *stage_lanes,
  * tracing schedule (1 wavefront rounds, 0 one chain per lane). */
 int drmlt_get_launch_shape(void *handle, int *stage_lanes, int *stage2_lanes, int *deriv_warps, int *graph_iters);
 int drmlt_get_wavefront(void *handle, int *wavefront);
+/* The stage-1 head tier the next drmlt_run uses: head_chains (0 = none) and
+ * head_lanes (drmlt_options.head_chains / head_lanes, or the autotuner's
+ * choice). Either output may be NULL. */
+int drmlt_get_head_tier(void *handle, int *head_chains, int *head_lanes);
 
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
  * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,

@@ -25,6 +25,7 @@ SCENE_WRITERS = {
     "cfgL": lambda d: scenegen.config_lights(d),
     "cfgE": lambda d: scenegen.config_env(d),
     "cfg4s": lambda d: scenegen.config4_small(d),
+    "cfg3d": lambda d: scenegen.config3_deep(d),
 }
 
 

@@ -119,15 +119,16 @@ def test_render_statistics_match_reference(built_lib, scene_root, cfg, name, dr_
 
 
 def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
-    """Graph replay, chain groups, chains per warp (stage 1 and stage 2) and derivative-team size only
-    change the scheduling: the chains take the same steps (integer counters identical,
+    """Graph replay, chain groups, chains per warp (stage 1 and stage 2, two-tier stage 1)
+    and derivative-team size only change the scheduling: the chains take the same steps (integer counters identical,
     film equal up to the order of the floating-point splat additions)."""
     from drmlt import scene as dscene
     from drmlt.integrator import Renderer
     sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
     out = []
     for kw in (dict(), dict(use_graph=0), dict(chain_groups=4, stage_lanes=4, deriv_warps=1, stage2_lanes=32),
-               dict(chain_groups=3, stage_lanes=32, deriv_warps=4, use_graph=0)):
+               dict(chain_groups=3, stage_lanes=32, deriv_warps=4, use_graph=0),
+               dict(head_chains=300, head_lanes=2), dict(head_chains=5000, head_lanes=8, chain_groups=3, use_graph=0)):
         with Renderer(sd, num_chains=4096, **kw) as r:
             r.prepass()
             r.run(12)
@@ -207,11 +208,13 @@ def test_autotuner_keeps_the_chains(built_lib, scene_root):
         # drmlt_get_launch_shape reports the tuned shape; 2 iterations per
         # candidate leave the graph length at 1
         shape = a.launch_shape()
-        assert shape["wavefront"] in (0, 1)
+        assert shape["head_chains"] in (0, 4096 // 2 // 2) and 1 <= shape["head_lanes"] <= 16
         assert shape == {"chains_per_warp": lanes, "stage2_chains_per_warp": min(lanes, 4),
-                         "derivative_warps": warps, "graph_iterations": 1, "wavefront": shape["wavefront"]}
+                         "derivative_warps": warps, "graph_iterations": 1, "wavefront": 0,
+                         "head_chains": shape["head_chains"], "head_lanes": shape["head_lanes"]}
+        # one untimed run, then 5 chains-per-warp, 3 team-size and 3 head-tier candidates in two passes
         tuned = a.stats()["mutations"] // 4096
-        assert tuned == 2 * 21
+        assert tuned == 2 * 23
         a.run(48 - tuned)
         b.prepass()
         b.run(48)

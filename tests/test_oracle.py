@@ -158,6 +158,35 @@ def test_oracle_derivatives(oracles, cfg):
     assert n_defect <= 0.2 * len(recs), n_defect
 
 
+def test_oracle_derivatives_vs_fp64_chad(oracles):
+    """The oracle's FP64 derivatives against the reference's chad library built in
+    FP64 (fixture cfg3d_tech: config 3 at max depth 10, paths of up to 20
+    primary coordinates): log f to 1e-5 relative, gradient and Hessian to 1e-4
+    of their largest entry (wherever chad's Hessian is the derivative of its
+    own gradient) -- ten times tighter than against the single-precision chad
+    (measured: log f median 1.3e-7, max 2.7e-6; gradient max 3.3e-5; Hessian
+    max 4.1e-5);
+    what is left is the scene itself (the FP64 reference reads the mesh files'
+    9-digit coordinates in double, the oracle in float) and the fixture's 9
+    printed digits."""
+    if golden("cfg3d", "tech") is None:
+        pytest.skip("no golden fixture cfg3d_tech")
+    o = oracles("cfg3d")
+    recs, P, U = _deriv_records("cfg3d", o)
+    f, _, _ = o.fd_derivs(P, U, 1e-4)
+    g, h = o.tape_derivs(P, U.astype(np.float32))
+    n = 0
+    for i, r in enumerate(recs):
+        d = r["dim"]
+        assert abs(f[i] - r["logf"]) <= 1e-5 * max(1.0, abs(r["logf"])), (i, f[i], r["logf"])
+        assert np.max(np.abs(g[i, :d] - r["grad"])) <= 1e-4 * np.max(np.abs(r["grad"])), i
+        if chad_hessian_consistent(r):
+            n += 1
+            hr = np.array(r["hess"])
+            assert np.max(np.abs(h[i, :d * d] - hr)) <= 1e-4 * np.max(np.abs(hr)), i
+    assert n >= len(recs) // 2 and max(r["dim"] for r in recs) == 20, (n, len(recs))
+
+
 @pytest.mark.parametrize("cfg", CFGS)
 def test_oracle_gaussian(oracles, cfg):
     recs = golden(cfg, "tech")
