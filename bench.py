@@ -256,7 +256,8 @@ def run_ours(args, world, rank, local):
     r2 = Renderer(sd, device=local, seed=seed + 1, autotune=0, stage_lanes=shape["chains_per_warp"],
                   stage2_lanes=shape["stage2_chains_per_warp"], deriv_warps=shape["derivative_warps"],
                   use_graph=1 if shape["graph_iterations"] else 0, graph_iters=max(1, shape["graph_iterations"]),
-                  wavefront=shape["wavefront"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"])
+                  wavefront=shape["wavefront"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"],
+                  adjoint_min_dim=shape["adjoint_min_dim"])
     r2.prepass()
     t1 = time.perf_counter()
     e_done = 0
@@ -391,9 +392,10 @@ def rel_mse(img, ref):
 
 # The plain per-stage-launch GPU drop-in: the chain loop's stages launched one
 # at a time on one stream without CUDA graphs, one chain per lane tracing its
-# whole path (no wavefront rounds), one warp per chain's derivatives, no
-# launch autotuning.
-PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, stage2_lanes=32, deriv_warps=1, wavefront=0)
+# whole path (no wavefront rounds), one warp per chain's derivatives by
+# hyper-dual forward mode (no reverse-mode adjoint), no launch autotuning.
+PLAIN = dict(use_graph=0, chain_groups=1, stage_lanes=32, stage2_lanes=32, deriv_warps=1, wavefront=0,
+             adjoint_min_dim=-1)
 
 
 def render_reference(sd, device, spp):
@@ -486,7 +488,8 @@ def schedule_times(sd, device, seed, shape, iterations=8):
     cooperative kernel (a quarter and half of the SMs as team workers)."""
     from drmlt.integrator import Renderer
     base = dict(autotune=0, stage_lanes=shape["chains_per_warp"], stage2_lanes=shape["stage2_chains_per_warp"],
-                deriv_warps=shape["derivative_warps"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"])
+                deriv_warps=shape["derivative_warps"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"],
+                adjoint_min_dim=shape["adjoint_min_dim"])
     out = {}
     for name, kw in (("staged", {}), ("wavefront", dict(wavefront=1)), ("persistent_quarter", dict(persistent=1)),
                      ("persistent_half", dict(persistent=1, team_sms=76))):

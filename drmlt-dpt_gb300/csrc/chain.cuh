@@ -99,6 +99,8 @@ struct RunParams {
     int headLanes;       // longest work classes) run headLanes to a warp, the rest `lanes`
     const int *iterp;    // the group's current iteration (device memory)
     int derivWarps;      // warps sharing one chain's Hessian in k_derivs (1..4)
+    int adjMinDim;       // paths of this dimension and up take the reverse-mode adjoint, the others
+                         // hyper-dual forward mode
     int lists;           // 1: the stage epilogues append the chain to the group's work lists (the
                          // staged schedule); 0: they only set the chain's flags (persistent schedule)
     int wave;            // 1: path tracing in wavefront rounds (wave.cuh), 0: one chain per lane

@@ -9,20 +9,39 @@ struct RunParams;
 struct SceneView;
 struct PathRec;
 
+// adjMinDim that selects hyper-dual forward mode for every path; the chain
+// loop's default (drmlt_options.adjoint_min_dim = 0) is that, and
+// drmlt_autotune times the reverse-mode adjoint from dimension 12, 8 or 1 on
+// beside it.
+constexpr int kNoAdjoint = 1 << 20;
+constexpr int kDefaultAdjMinDim = kNoAdjoint;
+
 // Gradient + Hessian of log f of path r (ss its score) for a team of `team`
-// threads, `member` the caller's index in it: zero (the isotropic fallback)
-// for a path longer than maxDerv segments or with ss <= 1e-15. g: kMaxDim
-// floats, H: kMaxDim^2. Defined in derivs_dev.cu (relocatable device code,
-// the derivative kernels' flags) for the persistent schedule.
+// threads, `member` the caller's index in it, by hyper-dual forward mode: zero
+// (the isotropic fallback) for a path longer than maxDerv segments or with
+// ss <= 1e-15. g: kMaxDim floats, H: kMaxDim^2. Defined in derivs_dev.cu
+// (relocatable device code,
+// the derivative kernels' flags) for the persistent schedule, which takes
+// hyper-dual derivatives for every path.
 __device__ void persist_derivs(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H,
                                int member, int team);
 
+// Threads per block and resident blocks per SM of the adjoint derivative kernel.
+constexpr int kAdjBlock = 128;
+constexpr int kAdjBlocksPerSm = 2;
+
 // Gradient + Hessian of log f for the chains of list `which` (0: listX at the
-// current states, 2: listZ at the second proposals) of one chain group.
-void launch_derivs(const RunParams &p, int which, int blocks, cudaStream_t s);
-// The same for caller-supplied paths and primary samples (u: n x kMaxDim).
+// current states, 2: listZ at the second proposals) of one chain group: the
+// hyper-dual kernel (`blocks` blocks) for paths shorter than p.adjMinDim, then
+// the adjoint kernel (`adjBlocks` blocks) for the others.
+void launch_derivs(const RunParams &p, int which, int blocks, int adjBlocks, cudaStream_t s);
+// Resident blocks of the adjoint derivative kernel per SM.
+int derivs_adj_blocks_per_sm();
+// The same for caller-supplied paths and primary samples (u: n x kMaxDim),
+// by the adjoint for paths of dimension adjMinDim and up (0: every path,
+// kNoAdjoint: none).
 void launch_gradhess_paths(const SceneView &s, const PathRec *paths, const float *u, int n, float *grad,
-                           float *hess, cudaStream_t st);
+                           float *hess, int adjMinDim, cudaStream_t st);
 // The same at each path's own primary vector, gated by path length and ss as the chain loop gates it.
 void launch_gradhess_gated(const SceneView &s, const PathRec *paths, const float *ss, int n, int maxDerv, float *grad,
                            float *hess, cudaStream_t st);

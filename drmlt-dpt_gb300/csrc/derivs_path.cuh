@@ -5,6 +5,7 @@
 // intrinsics), so both give the same values.
 #pragma once
 #include "chain.cuh"
+#include "pathadj.cuh"
 
 namespace drmlt {
 
@@ -30,15 +31,32 @@ DEV void derivs_entry(const SceneView &s, const PathRec &r, int dim, int pidx, f
 // (else the isotropic fallback of drsmallstep.cpp:133-163 with zero rows).
 DEV bool derivs_wanted(int L, float ss, int maxDerv) { return L <= maxDerv && ss > 1e-15f; }
 
-// A team of `team` threads strides over the D(D+1)/2 Hessian entries.
+// The rows of the adjoint (pathadj.cuh) of a path of dimension dim, strided
+// over a team of `team` threads.
+DEV void derivs_adj_for_path(const SceneView &s, const PathRec &r, int dim, float *g, float *H, int member,
+                             int team) {
+    for (int row = member; row < dim; row += team) adj_row(s, r, dim, row, row == 0 ? g : nullptr, H);
+}
+
+// A team of `team` threads strides over the D(D+1)/2 Hessian entries
+// (hyper-dual forward mode), or, for a path of dimension D >= adjMinDim, over
+// the D rows of the reverse-mode adjoint (pathadj.cuh: one forward and one
+// backward sweep per row, D sweeps for the whole Hessian against D(D+1)/2
+// hyper-dual evaluations).
+// kAdjoint = false compiles the hyper-dual form alone (adjMinDim ignored).
+template <bool kAdjoint = true>
 DEV void derivs_for_path(const SceneView &s, const PathRec &r, float ss, int maxDerv, float *g, float *H, int member,
-                         int team) {
+                         int team, int adjMinDim) {
     const int lane = member;
     const int L = r.c + r.l - 1;
     const int dim = 2 * L;
     if (!derivs_wanted(L, ss, maxDerv)) {
         for (int k = lane; k < dim; k += team) g[k] = 0.0f;
         for (int k = lane; k < dim * dim; k += team) H[k] = 0.0f;
+        return;
+    }
+    if (kAdjoint && dim >= adjMinDim) {
+        derivs_adj_for_path(s, r, dim, g, H, member, team);
         return;
     }
     const int npairs = dim * (dim + 1) / 2;

@@ -129,7 +129,7 @@ struct Renderer {
     int *dIters = nullptr;  // per chain group: its current iteration
     // chain groups, each stepped on its own stream
     int G = 1, chunk = 0;
-    int gaussGrid = 1, derivsGrid = 1;  // blocks of the list-driven kernels (grid-stride over their lists)
+    int gaussGrid = 1, derivsGrid = 1, derivsAdjGrid = 1;  // blocks of the list-driven kernels (grid-stride over their lists)
     std::vector<cudaStream_t> gstreams;
     std::vector<cudaEvent_t> gevents;
     unsigned long long bootSeed = 0;
@@ -200,6 +200,8 @@ struct Renderer {
         p.headLanes = opt.head_lanes > 0 ? std::min(opt.head_lanes, 32) : 2;
         p.iterp = dIters;
         p.derivWarps = opt.deriv_warps > 0 ? std::min(opt.deriv_warps, 4) : 2;
+        p.adjMinDim = opt.adjoint_min_dim > 0 ? opt.adjoint_min_dim
+                                              : (opt.adjoint_min_dim < 0 ? kNoAdjoint : kDefaultAdjMinDim);
         p.lists = 1;
         p.wave = opt.wavefront > 0 ? 1 : 0;
         p.waveRounds = std::min(std::min(opt.max_depth, kMaxLen) + 1, kWaveMaxRounds);
@@ -265,6 +267,7 @@ struct Renderer {
                                                              gauss_smem_bytes(std::min(2 * opt.max_depth, kMaxDim))));
             gaussGrid = std::max(1, 4 * sms * std::max(perSm, 1));
             derivsGrid = std::max(1, 4 * sms * derivs_blocks_per_sm());
+            derivsAdjGrid = std::max(1, 4 * sms * derivs_adj_blocks_per_sm());
         }
         if (opt.smem_carveout >= 0) {
             // one shared-memory carveout for every chain-loop kernel, so that
@@ -675,6 +678,8 @@ struct Renderer {
         const int nbS1 = stage1_blocks(p.N, p.headChains, p.headLanes, p.lanes);
         const int nbS2 = sparse_blocks(p.N, p.lanes2);
         const int nbWarp = std::min((p.N * 32 * p.derivWarps + 127) / 128, derivsGrid);
+        const int nbAdj = std::min((p.N * 32 + kAdjBlock - 1) / kAdjBlock, derivsAdjGrid);
+        const int nDerivs = p.adjMinDim <= kMaxDim ? 2 : 1;
         const int nbG = std::min(p.N, gaussGrid);
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
         const bool ystar = p.drType == 0 && p.integrator == 0;
@@ -688,7 +693,7 @@ struct Renderer {
                 if (p.wave) return 3 + launch_wave<1>(p, g, s);
                 k_stage1<<<nbS1, kStageBlock, 0, s>>>(p);
                 return 4;
-            case 1: launch_derivs(p, 0, nbWarp, s); return 1;
+            case 1: launch_derivs(p, 0, nbWarp, nbAdj, s); return nDerivs;
             case 2:
                 k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0);
                 k_h2mc_offset<<<(p.N * 32 + 127) / 128, 128, 0, s>>>(p);
@@ -697,7 +702,7 @@ struct Renderer {
                 if (p.wave) return launch_wave<2>(p, g, s);
                 k_stage2<<<nbS2, kStageBlock, 0, s>>>(p);
                 return 1;
-            case 4: launch_derivs(p, 2, nbWarp, s); return 1;
+            case 4: launch_derivs(p, 2, nbWarp, nbAdj, s); return nDerivs;
             case 5: k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 2); return 1;
             default: {
                 int n = 2;
@@ -1089,6 +1094,7 @@ void drmlt_default_options(drmlt_options *o) {
     o->stage2_lanes = 0;
     o->graph_iters = 0;
     o->wavefront = -1;
+    o->adjoint_min_dim = 0;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }
@@ -1164,6 +1170,13 @@ int drmlt_get_head_tier(void *handle, int *head_chains, int *head_lanes) {
     const RunParams p = static_cast<const Renderer *>(handle)->params();
     if (head_chains) *head_chains = p.headChains;
     if (head_lanes) *head_lanes = p.headLanes;
+    return DRMLT_OK;
+}
+
+int drmlt_get_adjoint_min_dim(void *handle, int *adjoint_min_dim) {
+    if (!handle || !adjoint_min_dim) return fail(DRMLT_E_ARG, "null argument");
+    const int a = static_cast<const Renderer *>(handle)->params().adjMinDim;
+    *adjoint_min_dim = a > kMaxDim ? -1 : a;
     return DRMLT_OK;
 }
 

@@ -236,7 +236,25 @@ int drmlt_path_grad_hess(void *handle, const drmlt_path *paths, const float *u, 
     if ((rc = dp.put(reinterpret_cast<const PathRec *>(paths), n)) || (rc = du.put(u, size_t(n) * kMaxDim)) ||
         (rc = dg.alloc(size_t(n) * kMaxDim)) || (rc = dh.alloc(size_t(n) * kMaxDim * kMaxDim)))
         return rc;
-    launch_gradhess_paths(r->sv, dp.p, du.p, n, dg.p, dh.p, 0);
+    launch_gradhess_paths(r->sv, dp.p, du.p, n, dg.p, dh.p, kNoAdjoint, 0);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if ((rc = dg.get(grad, size_t(n) * kMaxDim))) return rc;
+    return dh.get(hess, size_t(n) * kMaxDim * kMaxDim);
+}
+
+int drmlt_path_adjoint(void *handle, const drmlt_path *paths, const float *u, int n, float *grad, float *hess) {
+    if (!handle || n < 0 || (n && (!paths || !u || !grad || !hess))) return fail(DRMLT_E_ARG, "bad argument");
+    if (n == 0) return DRMLT_OK;
+    int rc = check_paths(paths, n);
+    if (rc) return rc;
+    Renderer *r = static_cast<Renderer *>(handle);
+    DevBuf<PathRec> dp;
+    DevBuf<float> du, dg, dh;
+    if ((rc = dp.put(reinterpret_cast<const PathRec *>(paths), n)) || (rc = du.put(u, size_t(n) * kMaxDim)) ||
+        (rc = dg.alloc(size_t(n) * kMaxDim)) || (rc = dh.alloc(size_t(n) * kMaxDim * kMaxDim)))
+        return rc;
+    launch_gradhess_paths(r->sv, dp.p, du.p, n, dg.p, dh.p, 0, 0);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
     if ((rc = dg.get(grad, size_t(n) * kMaxDim))) return rc;

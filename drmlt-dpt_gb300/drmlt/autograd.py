@@ -1,11 +1,12 @@
 """torch.autograd view of the C-ABI derivative pair (check harness only).
 
 `path_log_f(renderer, paths, u)` returns log f of each technique path at its
-primary sample vector (drmlt_path_eval); its gradient is drmlt_path_grad_hess's
-gradient, and the gradient of that gradient (double backward,
-create_graph=True) is the Hessian-vector product with drmlt_path_grad_hess's
-Hessian -- the PathFuncDerv pair of the reference's chad library
-(src/path.h:145-160) seen as a differentiable function. The library computes
+primary sample vector (drmlt_path_eval, the forward call); its gradient is the
+gradient of drmlt_path_adjoint (the backward call: the reverse-mode adjoint),
+and the gradient of that gradient (double backward, create_graph=True) is the
+Hessian-vector product with the adjoint's forward-over-reverse Hessian -- the
+PathFuncDerv pair of the reference's chad library (src/path.h:145-160) seen as
+a differentiable function. The library computes
 on the GPU from host arrays; tensors here live on the CPU.
 """
 from __future__ import annotations
@@ -42,7 +43,7 @@ class _PathLogF(torch.autograd.Function):
         d = u.shape[1]
         uh = _host(u)
         logf = renderer.path_eval(paths, uh)
-        g, h = renderer.path_grad_hess(paths, uh)
+        g, h = renderer.path_adjoint(paths, uh)
         grad = torch.from_numpy(np.ascontiguousarray(g[:, :d])).to(u.dtype)
         # each path's Hessian: d x d row-major at the start of its MAX_DIM^2 block
         hess = torch.from_numpy(np.ascontiguousarray(h.reshape(-1, MAX_DIM * MAX_DIM)[:, :d * d].reshape(-1, d, d)))

@@ -64,7 +64,7 @@ class Options(C.Structure):
                 ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32),
                 ("graph_iters", C.c_int32), ("wavefront", C.c_int32), ("head_chains", C.c_int32),
                 ("head_lanes", C.c_int32), ("persistent", C.c_int32),
-                ("team_sms", C.c_int32), ("wait_limit", C.c_int32)]
+                ("team_sms", C.c_int32), ("wait_limit", C.c_int32), ("adjoint_min_dim", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -116,6 +116,7 @@ _SIGS = {
     "drmlt_get_partial_film": (C.c_int, [C.c_void_p, C.c_void_p]),
     "drmlt_get_wavefront": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "drmlt_get_head_tier": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "drmlt_get_adjoint_min_dim": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "drmlt_write_exr": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_void_p]),
     "drmlt_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "drmlt_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
@@ -127,6 +128,7 @@ _SIGS = {
     "drmlt_total_iterations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "drmlt_path_eval": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "drmlt_path_grad_hess": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "drmlt_path_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "drmlt_perturb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "drmlt_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -146,6 +146,9 @@ class Renderer:
         capi.check(capi.lib().drmlt_get_head_tier(self.handle, C.byref(hc), C.byref(hl)))
         shape["head_chains"] = hc.value
         shape["head_lanes"] = hl.value
+        a = C.c_int()
+        capi.check(capi.lib().drmlt_get_adjoint_min_dim(self.handle, C.byref(a)))
+        shape["adjoint_min_dim"] = a.value
         return shape
 
     def fma_benchmark(self, fp64: bool = False, iterations: int | None = None) -> dict:
@@ -201,6 +204,17 @@ class Renderer:
         h = np.zeros((n, capi.MAX_DIM * capi.MAX_DIM), np.float32)
         capi.check(capi.lib().drmlt_path_grad_hess(self.handle, capi.ptr(paths), capi.ptr(u), n, capi.ptr(g),
                                                     capi.ptr(h)))
+        return g, h
+
+    def path_adjoint(self, paths: np.ndarray, u: np.ndarray):
+        """Gradient and Hessian of log f by the reverse-mode adjoint (drmlt_path_adjoint)."""
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        u = np.ascontiguousarray(u, np.float32).reshape(n, capi.MAX_DIM)
+        g = np.zeros((n, capi.MAX_DIM), np.float32)
+        h = np.zeros((n, capi.MAX_DIM * capi.MAX_DIM), np.float32)
+        capi.check(capi.lib().drmlt_path_adjoint(self.handle, capi.ptr(paths), capi.ptr(u), n, capi.ptr(g),
+                                                  capi.ptr(h)))
         return g, h
 
     def perturb(self, paths: np.ndarray, offsets: np.ndarray):

@@ -158,6 +158,15 @@ typedef struct drmlt_options {
     int32_t wait_limit;           /* persistent schedule: idle polls (about 0.2-0.5 us each) a device
                                      worker makes without seeing any progress before it gives up and
                                      the run fails with DRMLT_E_TIMEOUT (0 = 4194304, seconds) */
+    int32_t adjoint_min_dim;      /* H2MC path derivatives: paths of this primary-sample dimension and
+                                     up take the reverse-mode adjoint (one forward and one backward
+                                     sweep per Hessian row, D sweeps), shorter ones hyper-dual forward
+                                     mode (D(D+1)/2 evaluations); 0 = default (hyper-dual for every
+                                     path, as -1), 1 = the adjoint for every path. The two agree to
+                                     FP32 rounding; drmlt_autotune does not change this setting (a
+                                     switch of method mid-render would change later accept
+                                     decisions). The persistent schedule takes hyper-dual
+                                     derivatives for every path. */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
@@ -267,6 +276,10 @@ int drmlt_get_wavefront(void *handle, int *wavefront);
  * head_lanes (drmlt_options.head_chains / head_lanes, or the autotuner's
  * choice). Either output may be NULL. */
 int drmlt_get_head_tier(void *handle, int *head_chains, int *head_lanes);
+/* The derivative method the next drmlt_run uses: paths of this primary-sample
+ * dimension and up take the reverse-mode adjoint (-1: none, hyper-dual for
+ * every path). */
+int drmlt_get_adjoint_min_dim(void *handle, int *adjoint_min_dim);
 
 /* drmlt_run with CUDA events around each stage kernel (same work, serialised
  * per stage): stage_ms[7] accumulates stage1, derivs(x), gauss(x), stage2,
@@ -289,6 +302,15 @@ int drmlt_path_eval(void *handle, const drmlt_path *paths, const float *u, int n
  * dim = 2(c+l-1)) of log f, the PathFuncDerv call of drsmallstep.cpp:128-158. */
 int drmlt_path_grad_hess(void *handle, const drmlt_path *paths, const float *u, int n, float *grad,
                          float *hess);
+
+/* The same backward pair by the reverse-mode adjoint: per path, D forward and
+ * backward sweeps (forward-over-reverse, one Hessian row each) that keep each
+ * vertex's carried state and recompute its operations instead of recording a
+ * tape -- the reverse pass and forward-over-reverse Hessian that chad builds
+ * over its recorded expression graph (src/chad.cpp:342-418, 492-552). Same
+ * layout as drmlt_path_grad_hess; the Hessian is symmetric by construction
+ * (entry (i, j), i < j, from row i). */
+int drmlt_path_adjoint(void *handle, const drmlt_path *paths, const float *u, int n, float *grad, float *hess);
 
 /* PerturbPathBidir (src/path.cpp:1480-1628) with discrete jitter off:
  * offsets (DRMLT_MAX_DIM stride) -> perturbed paths and contributions. */

@@ -169,6 +169,52 @@ def test_random_derivatives_vs_fp64_oracle(renderers, oracles, cfg):
     assert len(bad_h) <= max(2, n // 50), "Hessian: %d / %d" % (len(bad_h), n)
 
 
+@pytest.mark.parametrize("cfg", CFGS)
+def test_random_adjoint_vs_fp64_oracle(renderers, oracles, cfg):
+    """The reverse-mode adjoint (drmlt_path_adjoint: forward and backward sweeps
+    in Dual numbers, one Hessian row each) on the random paths of the test
+    above: against the hyper-dual derivatives of the same FP32 function (1e-3
+    of the largest entry; both are exact derivatives, so they differ by FP32
+    rounding), and against the oracle's FP64 forward-over-reverse tape with the
+    same bars and the same explanation of the misses."""
+    tapes, cam, lgt, g, o, keep = _valid_paths(cfg, renderers, oracles)
+    paths = g[2][keep]
+    ss = g[1][keep, 0]["ss"]
+    paths = paths[np.nonzero(ss > 1e-15)[0]]
+    u = np.zeros((len(paths), 24), np.float32)
+    for i in range(len(paths)):
+        u[i] = paths[i]["u"]
+    r, ora = renderers(cfg), oracles(cfg)
+    ga, ha = r.path_adjoint(paths, u)
+    gh, hh = r.path_grad_hess(paths, u)
+    go, ho = ora.tape_derivs(paths, u)
+    bad_hd, bad_g, bad_h = [], [], []
+    for i in range(len(paths)):
+        d = 2 * (paths[i]["c"] + paths[i]["l"] - 1)
+        H = ha[i, :d * d].reshape(d, d)
+        assert np.array_equal(H, H.T), "adjoint Hessian not symmetric"
+        if not (np.isfinite(gh[i, :d]).all() and np.isfinite(hh[i, :d * d]).all()):
+            continue
+        e_g = np.max(np.abs(ga[i, :d] - gh[i, :d])) / max(np.max(np.abs(gh[i, :d])), 1e-6)
+        e_h = np.max(np.abs(ha[i, :d * d] - hh[i, :d * d])) / max(np.max(np.abs(hh[i, :d * d])), 1e-6)
+        if not (e_g <= 1e-3 and e_h <= 1e-3):
+            bad_hd.append(i)
+        if np.max(np.abs(ga[i, :d] - go[i, :d])) > 1e-3 * max(np.max(np.abs(go[i, :d])), 1e-6):
+            bad_g.append(i)
+        if np.max(np.abs(ha[i, :d * d] - ho[i, :d * d])) > 1e-3 * max(np.max(np.abs(ho[i, :d * d])), 1e-6):
+            bad_h.append(i)
+    n = len(paths)
+    assert n > 100
+    tol = max(2, n // 100)
+    assert len(bad_hd) <= tol, "adjoint vs hyper-dual: %d / %d" % (len(bad_hd), n)
+    assert len(bad_g) <= tol, "gradient: %d / %d" % (len(bad_g), n)
+    rough = _fp32_not_smooth(r, ora, paths, u, bad_h)
+    unexplained = [i for i in bad_h if not rough[i]]
+    assert len(unexplained) <= tol, "Hessian: %d / %d (%d with a non-smooth FP32 gradient)" % (
+        len(unexplained), n, len(bad_h) - len(unexplained))
+    assert len(bad_h) <= max(2, n // 50), "Hessian: %d / %d" % (len(bad_h), n)
+
+
 def _fp32_not_smooth(r, ora, paths, u, idx, steps=(1e-3, 2e-3)):
     """Whether the FP32 path function of each listed path is not smooth at the
     1e-3 level where the FP64 one is: central-difference Hessians of the GPU's

@@ -138,9 +138,13 @@ def test_small_step_perturbation(renderers, cfg):
     assert bad <= max(1, len(refs) // 50), "%d / %d perturbations differ" % (bad, len(refs))
 
 
+@pytest.mark.parametrize("method", ["hyperdual", "adjoint"])
 @pytest.mark.parametrize("cfg", CFGS)
-def test_path_derivatives_vs_chad(renderers, cfg):
-    """log f, gradient and Hessian vs the chad-generated library on the same paths.
+def test_path_derivatives_vs_chad(renderers, cfg, method):
+    """log f, gradient and Hessian vs the chad-generated library on the same paths,
+    by both derivative methods (hyper-dual forward mode: drmlt_path_grad_hess;
+    the reverse-mode adjoint with forward-over-reverse Hessian rows:
+    drmlt_path_adjoint).
 
     Tolerances: f 1e-4, gradient and Hessian 1e-3 relative to the largest
     reference entry. Exception: where chad's Hessian is not the derivative of
@@ -166,7 +170,7 @@ def test_path_derivatives_vs_chad(renderers, cfg):
     paths = np.array(paths)
     us = np.array(us)
     logf = r.path_eval(paths, us)
-    g, h = r.path_grad_hess(paths, us)
+    g, h = r.path_grad_hess(paths, us) if method == "hyperdual" else r.path_adjoint(paths, us)
     env = env_light_index(r.scene)
     bad_fg, bad_h, n_cam, n_defect = [], [], 0, 0
     for i, rec in enumerate(recs):
@@ -272,7 +276,9 @@ def test_fma_benchmark(renderers, fp64):
 
 def test_autograd_wrapper_matches_the_derivative_pair(renderers):
     """drmlt.autograd: torch's first and second derivatives of log f through the
-    C-ABI pair equal drmlt_path_grad_hess's gradient and Hessian."""
+    C-ABI pair (drmlt_path_eval forward, drmlt_path_adjoint backward) equal the
+    adjoint's gradient and Hessian, and those equal the hyper-dual
+    drmlt_path_grad_hess's to 1e-4 of the largest entry."""
     import torch
     from drmlt.autograd import path_log_f
     recs = [rec for rec in _need("cfg2", "tech") if rec["dim"] == 8 and rec["contrib"][0]["ss"] > 1e-15][:16]
@@ -283,7 +289,11 @@ def test_autograd_wrapper_matches_the_derivative_pair(renderers):
     f = path_log_f(r, paths, u)
     uh = np.zeros((len(recs), 24), np.float32)
     uh[:, :8] = u.detach().numpy()
-    g_ref, h_ref = r.path_grad_hess(paths, uh)
+    g_ref, h_ref = r.path_adjoint(paths, uh)
+    g_hd, h_hd = r.path_grad_hess(paths, uh)
+    for i in range(len(recs)):
+        assert np.max(np.abs(g_ref[i, :8] - g_hd[i, :8])) <= 1e-4 * max(np.max(np.abs(g_hd[i, :8])), 1e-6)
+        assert np.max(np.abs(h_ref[i, :64] - h_hd[i, :64])) <= 1e-4 * max(np.max(np.abs(h_hd[i, :64])), 1e-6)
     np.testing.assert_allclose(f.detach().numpy(), r.path_eval(paths, uh), rtol=1e-6)
     (g,) = torch.autograd.grad(f.sum(), u, create_graph=True)
     np.testing.assert_allclose(g.detach().numpy(), g_ref[:, :8], rtol=1e-6, atol=1e-6)

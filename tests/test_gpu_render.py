@@ -138,6 +138,40 @@ def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
         np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
 
 
+def test_adjoint_derivatives_in_the_chain_loop(built_lib, scene_root):
+    """The chain loop with every H2MC derivative by the reverse-mode adjoint
+    (adjoint_min_dim=1), by hyper-dual forward mode alone (-1, the default) and
+    mixed (the adjoint from dimension 10 on). The two methods give the same
+    derivatives up to FP32 rounding, so the chains' H2MC acceptance and the
+    images agree statistically: acceptance ratios within 0.01, and the runs'
+    images as close to each other as two runs of one method with other
+    random streams are."""
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
+    out = {}
+    for name, kw in (("hd", dict(adjoint_min_dim=-1)), ("adj", dict(adjoint_min_dim=1)), ("mixed", dict(adjoint_min_dim=10)),
+                     ("hd2", dict(adjoint_min_dim=-1, seed=0x5151))):
+        with Renderer(sd, num_chains=4096, **kw) as r:
+            r.prepass()
+            r.run(24)
+            st = r.stats()
+            out[name] = (st, r.film().astype(np.float64))
+            assert st["stage2_h2mc"] > 1000
+    rate = {k: v[0]["stage2_h2mc_accepted"] / v[0]["stage2_h2mc"] for k, v in out.items()}
+    for k in ("adj", "mixed"):
+        assert abs(rate[k] - rate["hd"]) < 0.01, rate
+    def blocks(img):
+        H, W, _ = img.shape
+        return img.reshape(8, H // 8, 8, W // 8, 3).mean(axis=(1, 3))
+
+    def dist(a, b):
+        return float(np.mean(np.abs(blocks(a) - blocks(b))) / np.mean(np.abs(blocks(b))))
+    noise = dist(out["hd2"][1], out["hd"][1])
+    for k in ("adj", "mixed"):
+        assert dist(out[k][1], out["hd"][1]) < 1.5 * noise + 1e-3, (k, dist(out[k][1], out["hd"][1]), noise)
+
+
 def test_multi_iteration_graphs_keep_the_chains(built_lib, scene_root):
     """Graphs of 4 iterations (graph_iters=4: the chain groups run free inside a
     graph and join only at its end) step the chains exactly as stage-by-stage
@@ -211,7 +245,8 @@ def test_autotuner_keeps_the_chains(built_lib, scene_root):
         assert shape["head_chains"] in (0, 4096 // 2 // 2) and 1 <= shape["head_lanes"] <= 16
         assert shape == {"chains_per_warp": lanes, "stage2_chains_per_warp": min(lanes, 4),
                          "derivative_warps": warps, "graph_iterations": 1, "wavefront": 0,
-                         "head_chains": shape["head_chains"], "head_lanes": shape["head_lanes"]}
+                         "head_chains": shape["head_chains"], "head_lanes": shape["head_lanes"],
+                         "adjoint_min_dim": -1}
         # one untimed run, then 5 chains-per-warp, 3 team-size and 3 head-tier candidates in two passes
         tuned = a.stats()["mutations"] // 4096
         assert tuned == 2 * 23
