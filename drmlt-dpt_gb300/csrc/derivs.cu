@@ -37,15 +37,22 @@ __global__ void __launch_bounds__(128, 4) k_derivs(RunParams p, int which) {
 // The list entries of dimension p.adjMinDim and up by the reverse-mode
 // adjoint: one warp per chain, one Hessian row (a forward and a backward sweep
 // in Dual numbers) per lane. A separate kernel, so that the hyper-dual kernel
-// keeps its register bound: the adjoint sweeps hold the Dual vertex state,
-// its adjoint and the carried checkpoints.
+// keeps its register bound. At 4 blocks per SM (128 registers, the adjoint's
+// Dual state, adjoints and checkpoints partly spilled) it runs faster than at
+// 2 (255 registers) or 5-8 (more spills): config 4, every derivative by the
+// adjoint, 0.72 / 0.63 / 0.55 / 0.57 / 0.62 / 0.68 ms at x for 2 / 3 / 4 / 5 /
+// 6 / 8 blocks. Two chains per warp (a half-warp each when both have at most
+// 16 rows) measured slower still (0.78 ms): the two paths diverge. So did
+// out-of-line copies of the BSDF adjoints and of the forward BSDF calls (0.68
+// ms: the Dual arguments go through the stack; ncu had shown instruction-fetch
+// stalls, 14 a issued instruction, as the kernel's first limiter).
 __global__ void __launch_bounds__(kAdjBlock, kAdjBlocksPerSm) k_derivs_adj(RunParams p, int which) {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int warps = gridDim.x * blockDim.x >> 5;
     const int n = p.d.counters[which == 0 ? 0 : 1];
     const int lane = threadIdx.x & 31;
     for (int k = gw; k < n; k += warps) {
-        const int w = n - 1 - k;
+        const int w = n - 1 - k;  // longest paths first: the lists fill in the order their stage finishes
         const int chain = (which == 0 ? p.d.listX : p.d.listZ)[w];
         const Slot &st = slot_of(p.d, chain, which);
         const int L = st.rec.c + st.rec.l - 1;

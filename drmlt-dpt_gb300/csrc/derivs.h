@@ -28,7 +28,7 @@ __device__ void persist_derivs(const SceneView &s, const PathRec &r, float ss, i
 
 // Threads per block and resident blocks per SM of the adjoint derivative kernel.
 constexpr int kAdjBlock = 128;
-constexpr int kAdjBlocksPerSm = 2;
+constexpr int kAdjBlocksPerSm = 4;
 
 // Gradient + Hessian of log f for the chains of list `which` (0: listX at the
 // current states, 2: listZ at the second proposals) of one chain group: the

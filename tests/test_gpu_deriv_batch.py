@@ -12,6 +12,9 @@ scene at max depth 10 (the Lambertian box with the rough-dielectric sphere).
   checked against the oracle's FP64 forward-over-reverse derivatives (1e-3),
   the first 512 also against FP64 central differences of log f with h = 1e-4
   (1e-2: the differences' own truncation and rounding error).
+
+Both derivative methods are held to these bars: the reverse-mode adjoint
+(drmlt_path_adjoint) and hyper-dual forward mode (drmlt_path_grad_hess).
 """
 import os
 import sys
@@ -40,7 +43,8 @@ def deep(built_lib, scene_root):
     o.close()
 
 
-def test_derivatives_vs_fp64_chad(deep):
+@pytest.mark.parametrize("method", ["adjoint", "hyperdual"])
+def test_derivatives_vs_fp64_chad(deep, method):
     recs = golden("cfg3d", "tech")
     if recs is None:
         pytest.skip("no golden fixture cfg3d_tech")
@@ -54,7 +58,7 @@ def test_derivatives_vs_fp64_chad(deep):
         us.append(u)
     paths = np.array(paths)
     logf = r.path_eval(paths, np.array(us))
-    g, h = r.path_grad_hess(paths, np.array(us))
+    g, h = (r.path_adjoint if method == "adjoint" else r.path_grad_hess)(paths, np.array(us))
     bad, n = [], 0
     depths = set()
     for i, rec in enumerate(recs):
@@ -87,33 +91,36 @@ def test_derivative_batch_of_2e20_vectors(deep):
     assert len(valid) > n // 100
     paths = pth[valid]
     u = np.stack([p["u"] for p in paths]).astype(np.float32)
-    g, h = r.path_grad_hess(paths, u)
     dims = 2 * (paths["c"] + paths["l"] - 1)
     assert dims.max() >= 16
-    for i in range(0, len(paths), max(1, len(paths) // 20000)):
-        d = dims[i]
-        H = h[i, :d * d].reshape(d, d)
-        assert np.all(np.isfinite(g[i, :d])) and np.all(np.isfinite(H)), i
-        assert np.array_equal(H, H.T), i
     # a seeded sample against the FP64 oracle
     pick = np.sort(np.random.default_rng(21).choice(len(paths), size=min(4096, len(paths)), replace=False))
     go, ho = o.tape_derivs(paths[pick], u[pick])
     # central differences (they also difference the Hessian: d^2 evaluations a path) on the first 512
     nfd = min(512, len(pick))
     _, gfd, hfd = o.fd_derivs(paths[pick[:nfd]], u[pick[:nfd]].astype(np.float64), 1e-4)
-    bad_g, bad_h, bad_fd = [], [], []
-    for k, i in enumerate(pick):
-        d = dims[i]
-        top_g = max(np.max(np.abs(go[k, :d])), 1e-6)
-        top_h = max(np.max(np.abs(ho[k, :d * d])), 1e-6)
-        if np.max(np.abs(g[i, :d] - go[k, :d])) > 1e-3 * top_g:
-            bad_g.append(i)
-        if np.max(np.abs(h[i, :d * d] - ho[k, :d * d])) > 1e-3 * top_h:
-            bad_h.append(i)
-        if k < nfd and (np.max(np.abs(g[i, :d] - gfd[k, :d])) > 1e-2 * top_g or
-                        np.max(np.abs(h[i, :d * d] - hfd[k, :d * d])) > 1e-2 * top_h):
-            bad_fd.append(i)
-    m = len(pick)
-    assert len(bad_g) <= max(2, m // 100), "gradient: %d / %d" % (len(bad_g), m)
-    assert len(bad_h) <= max(2, m // 100), "Hessian: %d / %d" % (len(bad_h), m)
-    assert len(bad_fd) <= max(2, nfd // 50), "GPU vs FP64 central differences: %d / %d" % (len(bad_fd), nfd)
+    for method in ("adjoint", "hyperdual"):
+        g, h = (r.path_adjoint if method == "adjoint" else r.path_grad_hess)(paths, u)
+        for i in range(0, len(paths), max(1, len(paths) // 20000)):
+            d = dims[i]
+            H = h[i, :d * d].reshape(d, d)
+            assert np.all(np.isfinite(g[i, :d])) and np.all(np.isfinite(H)), (method, i)
+            assert np.array_equal(H, H.T), (method, i)
+        bad_g, bad_h, bad_fd = [], [], []
+        for k, i in enumerate(pick):
+            d = dims[i]
+            top_g = max(np.max(np.abs(go[k, :d])), 1e-6)
+            top_h = max(np.max(np.abs(ho[k, :d * d])), 1e-6)
+            if np.max(np.abs(g[i, :d] - go[k, :d])) > 1e-3 * top_g:
+                bad_g.append(i)
+            if np.max(np.abs(h[i, :d * d] - ho[k, :d * d])) > 1e-3 * top_h:
+                bad_h.append(i)
+            if k < nfd and (np.max(np.abs(g[i, :d] - gfd[k, :d])) > 1e-2 * top_g or
+                            np.max(np.abs(h[i, :d * d] - hfd[k, :d * d])) > 1e-2 * top_h):
+                bad_fd.append(i)
+        m = len(pick)
+        assert len(bad_g) <= max(2, m // 100), "%s gradient: %d / %d" % (method, len(bad_g), m)
+        assert len(bad_h) <= max(2, m // 100), "%s Hessian: %d / %d" % (method, len(bad_h), m)
+        assert len(bad_fd) <= max(2, nfd // 50), "%s vs FP64 central differences: %d / %d" % (method, len(bad_fd),
+                                                                                            nfd)
+        del g, h

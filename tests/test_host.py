@@ -43,7 +43,7 @@ def _declared_symbols():
 def test_header_declares_entry_points():
     names = _declared_symbols()
     for n in ("drmlt_create", "drmlt_prepass", "drmlt_run", "drmlt_get_film", "drmlt_path_grad_hess",
-              "drmlt_compute_gaussian", "drmlt_compute_gaussian_noalloc"):
+              "drmlt_path_eval", "drmlt_path_adjoint", "drmlt_compute_gaussian", "drmlt_compute_gaussian_noalloc"):
         assert n in names
 
 
