@@ -112,6 +112,13 @@ template <class T> DEV void tlum_adj(const T &yb, TV3<T> &vb) {
     vb = vb + TV3<T>(yb * 0.212671f, yb * 0.715160f, yb * 0.072169f);
 }
 
+// The adjoint of the path contribution that f = log Luminance(contrib) seeds.
+template <class T> DEV TV3<T> logf_seed(const TV3<T> &contrib) {
+    TV3<T> cb = tzero<T>();
+    tlum_adj(1.0f / tlum(contrib), cb);
+    return cb;
+}
+
 // tframe(n) -> (b1, b2), src/utils.h:222-232 as the AD builder writes it.
 template <class T> DEV void tframe_adj(const TV3<T> &n, const TV3<T> &b1b, const TV3<T> &b2b, TV3<T> &nb) {
     if (val(n.z) < float(-1.0 + 1e-6)) return;  // constant frame
@@ -169,6 +176,17 @@ struct TBsdfAdj {
         contrib = tzero<T>();
         cosWo = pdf = revPdf = T(0.0f);
     }
+};
+
+// The BSDF adjoints below compute the forward outputs first and then ask the
+// caller for their adjoints: obf(o, wo, wob) returns the adjoints of `o` and
+// may add to wob, the adjoint of the direction wo. A caller that needs `o` to
+// form them (the sampling step's MIS and throughput updates) gets it without
+// a second forward evaluation; FixedOb serves callers that already know them.
+template <class T>
+struct FixedOb {
+    TBsdfAdj<T> ob;
+    DEV TBsdfAdj<T> operator()(const TBsdf<T> &, const TV3<T> &, TV3<T> &) const { return ob; }
 };
 
 // ad_beckmann_d(h, alpha), alpha a path-dependent roughness (a constant one
@@ -254,9 +272,9 @@ DEV void snc_adj(const TV3<T> &wi, const TIsect<T> &is, const TV3<T> &wo, const 
 }
 
 // Rough dielectric evaluation (ad_rough_dielectric_evaluate).
-template <class T>
+template <class T, class ObF>
 DEV void rough_dielectric_evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo,
-                                       const TBsdfAdj<T> &ob, bool adjoint, TV3<T> &wib, TV3<T> &nb, TV3<T> &wob) {
+                                       const ObF &obf, bool adjoint, TV3<T> &wib, TV3<T> &nb, TV3<T> &wob) {
     const T cosWi = dot(wi, normal);
     const T cosWo = dot(wo, normal);
     const bool reflect = val(cosWi) * val(cosWo) > 0.0f;
@@ -283,6 +301,23 @@ DEV void rough_dielectric_evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV
     const T rsA = alpha * (1.2f - 0.2f * sqrt(aWo));
     const T bdR = ad_beckmann_d(lH, rsA);
     const T revProb = lH.z * bdR;
+    TBsdf<T> o;
+    o.cosWo = cosWo;
+    if (reflect) {
+        o.contrib = tv<T>(ks_of(b)) * fabs(F * D * G / (4.0f * cosWi));
+        o.pdf = fabs(prob * F / (4.0f * cHo));
+        o.revPdf = fabs(revProb * F / (4.0f * cHi));
+    } else {
+        const T sd = cHi + eta_ * cHo;
+        const T rsd = cHo + revEta_ * cHi;
+        const float factor = adjoint ? 1.0f : (1.0f / eta_) * (1.0f / eta_);
+        const float e2 = eta_ * eta_, re2 = revEta_ * revEta_;
+        const T omF = 1.0f - F;
+        o.contrib = tv<T>(kt_of(b)) * fabs(factor * ((omF * D * G * e2 * cHi * cHo) / (cosWi * (sd * sd))));
+        o.pdf = fabs(prob * omF * (e2 * cHo) / (sd * sd));
+        o.revPdf = fabs(revProb * omF * (re2 * cHi) / (rsd * rsd));
+    }
+    const TBsdfAdj<T> ob = obf(o, wo, wob);
     T Fb(0.0f), Db(0.0f), Gb(0.0f), probb(0.0f), revProbb(0.0f), cHib(0.0f), cHob(0.0f), cosWib(0.0f);
     T cosWob = ob.cosWo;
     if (reflect) {
@@ -373,10 +408,11 @@ DEV void rough_dielectric_evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV
 }
 
 // Rough dielectric sampling (ad_rough_dielectric_sample, fixDiscrete = false).
-template <class T>
+// wob: on entry the adjoint of the sampled direction from its later uses.
+template <class T, class ObF>
 DEV void rough_dielectric_sample_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const T &r0, const T &r1,
-                                     float uDiscrete, const TV3<T> &wob_, const TBsdfAdj<T> &ob, bool adjoint,
-                                     TV3<T> &wib, TV3<T> &nb, T &r0b, T &r1b) {
+                                     float uDiscrete, TV3<T> &wob, const ObF &obf, bool adjoint, TV3<T> &wib,
+                                     TV3<T> &nb, T &r0b, T &r1b) {
     const T cosWi = dot(wi, normal);
     const float alpha = b.alpha;
     const T aWi = fabs(cosWi);
@@ -419,12 +455,27 @@ DEV void rough_dielectric_sample_adj(const Bsdf &b, const TV3<T> &wi, const TV3<
     // contrib = reflc |D G cHi / (mPdf aWi)|
     const T num = D * G * cHi, den = mPdf * aWi;
     const T Cx = num / den;
+    TBsdf<T> o;
+    o.contrib = tv<T>(reflc) * fabs(Cx);
+    o.cosWo = cosWo;
+    if (refl) {
+        o.pdf = fabs(mPdf * F / (4.0f * cHo));
+        o.revPdf = fabs(F * bdR * lH.z * (1.0f / (4.0f * cHi)));
+    } else {
+        const T sd = cHi + eta_ * cHo;
+        const T dwh = ((eta_ * eta_) * cHo) / (sd * sd);
+        const T omF = 1.0f - F;
+        o.pdf = fabs(mPdf * omF * fabs(dwh));
+        const float revEta_ = val(cosWo) > 0.0f ? b.eta : b.invEta;
+        const T rsd = cHo + revEta_ * cHi;
+        o.revPdf = fabs(omF * bdR * lH.z * (((revEta_ * revEta_) * cHi) / (rsd * rsd)));
+    }
+    const TBsdfAdj<T> ob = obf(o, wo, wob);
     const T Cxb = dot(tv<T>(reflc), ob.contrib) * sgn_of(Cx);
     const T numb = Cxb / den, denb = -Cxb * Cx / den;
     T Db = numb * G * cHi, Gb = numb * D * cHi, cHib = numb * D * G;
     T mPdfb = denb * aWi, aWib = denb * mPdf;
     T Fb(0.0f), cTb(0.0f), cHob(0.0f), lHzb(0.0f), bdRb(0.0f), cosWob = ob.cosWo;
-    TV3<T> wob = wob_;
     if (refl) {
         const T Px = mPdf * F / (4.0f * cHo);
         const T Pxb = ob.pdf * sgn_of(Px);
@@ -525,11 +576,11 @@ DEV void rough_dielectric_sample_adj(const Bsdf &b, const TV3<T> &wi, const TV3<
 }
 
 // ad_evaluate: Lambertian, Phong and rough dielectric.
-template <class T>
-DEV void evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo, const TBsdfAdj<T> &ob,
+template <class T, class ObF>
+DEV void evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const TV3<T> &wo, const ObF &obf,
                       bool adjoint, TV3<T> &wib, TV3<T> &nb, TV3<T> &wob) {
     if (b.type == kBsdfRoughDielectric) {
-        rough_dielectric_evaluate_adj(b, wi, normal, wo, ob, adjoint, wib, nb, wob);
+        rough_dielectric_evaluate_adj(b, wi, normal, wo, obf, adjoint, wib, nb, wob);
         return;
     }
     const T cosWiRaw = dot(normal, wi);
@@ -538,17 +589,24 @@ DEV void evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, con
     const T cosWi = cosWiRaw * sg;
     const T cosWo = dot(n, wo);
     const V3 kd = kd_of(b);
-    T cosWob = ob.cosWo, cosWib(0.0f);
+    T cosWib(0.0f);
     TV3<T> nbl = tzero<T>();
+    TBsdf<T> o;
+    o.cosWo = cosWo;
+    T cosWob;
     if (b.type == kBsdfLambertian) {
-        const T fwdb = dot(tv<T>(kd), ob.contrib) + ob.pdf;
-        cosWob = cosWob + fwdb * kInvPi;
+        const T fwd = cosWo * kInvPi;
+        o.contrib = fwd * tv<T>(kd);
+        o.pdf = fwd;
+        o.revPdf = cosWi * kInvPi;
+        const TBsdfAdj<T> ob = obf(o, wo, wob);
+        cosWob = ob.cosWo + (dot(tv<T>(kd), ob.contrib) + ob.pdf) * kInvPi;
         cosWib = cosWib + ob.revPdf * kInvPi;
     } else {
         // contrib = (spec + kd / pi) cosWo
         TV3<T> c0 = tzero<T>();
         TV3<T> R = tzero<T>();
-        T alpha(0.0f), weight(0.0f);
+        T alpha(0.0f), weight(0.0f), specPdf(0.0f);
         bool spec = false;
         if (b.ksWeight > 0.0f) {
             R = treflect(wi, n);
@@ -558,13 +616,22 @@ DEV void evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, con
                 spec = true;
                 weight = pow(alpha, b.exponent) * kInvTwoPi;
                 c0 = tv<T>(ks_of(b)) * ((b.exponent + 2.0f) * weight);
+                specPdf = b.ksWeight * (b.exponent + 1.0f) * weight;
             }
         }
-        if (b.ksWeight < 1.0f) c0 = c0 + tv<T>(kd * kInvPi);
-        cosWob = cosWob + dot(c0, ob.contrib);
+        o.pdf = specPdf;
+        o.revPdf = specPdf;
+        const float tmp = (1.0f - b.ksWeight) * kInvPi;
+        if (b.ksWeight < 1.0f) {
+            c0 = c0 + tv<T>(kd * kInvPi);
+            o.pdf = o.pdf + tmp * cosWo;
+            o.revPdf = o.revPdf + tmp * cosWi;
+        }
+        o.contrib = c0 * cosWo;
+        const TBsdfAdj<T> ob = obf(o, wo, wob);
+        cosWob = ob.cosWo + dot(c0, ob.contrib);
         const TV3<T> c0b = ob.contrib * cosWo;
         if (b.ksWeight < 1.0f) {
-            const float tmp = (1.0f - b.ksWeight) * kInvPi;
             cosWob = cosWob + tmp * ob.pdf;
             cosWib = cosWib + tmp * ob.revPdf;
         }
@@ -585,23 +652,29 @@ DEV void evaluate_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, con
 }
 
 // ad_sample: Lambertian, Phong and rough dielectric (fixDiscrete = false).
-template <class T>
+// wob: on entry the adjoint of the sampled direction from its later uses.
+template <class T, class ObF>
 DEV void sample_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const T &r0, const T &r1, float uDiscrete,
-                    const TV3<T> &wob_, const TBsdfAdj<T> &ob, bool adjoint, TV3<T> &wib, TV3<T> &nb, T &r0b,
-                    T &r1b) {
+                    TV3<T> &wob, const ObF &obf, bool adjoint, TV3<T> &wib, TV3<T> &nb, T &r0b, T &r1b) {
     if (b.type == kBsdfRoughDielectric) {
-        rough_dielectric_sample_adj(b, wi, normal, r0, r1, uDiscrete, wob_, ob, adjoint, wib, nb, r0b, r1b);
+        rough_dielectric_sample_adj(b, wi, normal, r0, r1, uDiscrete, wob, obf, adjoint, wib, nb, r0b, r1b);
         return;
     }
-    TV3<T> wob = wob_;
     const T cosWiRaw = dot(wi, normal);
     const float sg = val(cosWiRaw) > 0.0f ? 1.0f : -1.0f;
     const TV3<T> n = normal * sg;
     const T cosWi = cosWiRaw * sg;
     T cosWib(0.0f);
     TV3<T> nbl = tzero<T>();
+    TBsdf<T> o;
     if (b.type == kBsdfLambertian) {
         const TV3<T> l = tcos_hemisphere(r0, r1);
+        const TV3<T> wo = frame_apply(l, n);
+        o.cosWo = l.z;
+        o.pdf = l.z * kInvPi;
+        o.contrib = tv<T>(kd_of(b));
+        o.revPdf = cosWi * kInvPi;
+        const TBsdfAdj<T> ob = obf(o, wo, wob);
         TV3<T> lb = tzero<T>();
         lb.z = ob.cosWo + ob.pdf * kInvPi;
         cosWib = ob.revPdf * kInvPi;
@@ -637,14 +710,20 @@ DEV void sample_adj(const Bsdf &b, const TV3<T> &wi, const TV3<T> &normal, const
             }
         }
         T pdf = specPdf;
+        o.revPdf = specPdf;
         const float tmp = (1.0f - b.ksWeight) * kInvPi;
         if (b.ksWeight < 1.0f) {
             c0 = c0 + tv<T>(kd_of(b) * kInvPi);
             pdf = pdf + tmp * cosWo;
+            o.revPdf = o.revPdf + tmp * cosWi;
         }
         // contrib = c0 cosWo / pdf
         const TV3<T> c1 = c0 * cosWo;
         const T ipdf = 1.0f / pdf;
+        o.cosWo = cosWo;
+        o.pdf = pdf;
+        o.contrib = c1 * ipdf;
+        const TBsdfAdj<T> ob = obf(o, wo, wob);
         const TV3<T> c1b = ob.contrib * ipdf;
         const T pdfb = ob.pdf - dot(c1, ob.contrib) * ipdf * ipdf;
         T cosWob = ob.cosWo + dot(c0, c1b);
@@ -759,21 +838,58 @@ DEV void sphere_dir_adj(const T &r0, const T &r1, const TV3<T> &db, const T &sin
 }
 
 // ---------------------------------------------------------------- BSDF sampling step
-// ad_bsdf_sampling<T, adjoint>: the vertex state (isect, wi, MIS accumulators,
-// throughput) and (r0, r1) -> the next direction and the updated state. The
-// adjoint takes the updated state's adjoints in `nb` (isect and wi unused) and
-// the direction's in dirb, and accumulates the input state's into `ib`.
-template <class T, bool adjoint>
-DEV void bsdf_sampling_adj(const SceneView &s, int tri, const T &r0, const T &r1, float disc, bool useAbs,
-                           int lcsTri, const TState<T> &ps, const TV3<T> &dirb_, const TState<T> &nb,
-                           TState<T> &ib, T &r0b, T &r1b) {
+// ad_bsdf_sampling<T, adjoint> with the adjoint flag (light subpaths) as an
+// argument: the vertex state (isect, wi, MIS accumulators, throughput) and
+// (r0, r1) -> the next direction and the updated state.
+template <class T>
+DEV void bsdf_sampling_fwd(const SceneView &s, int tri, const T &r0, const T &r1, float disc, bool useAbs,
+                           int lcsTri, bool adjoint, TState<T> &ps, TV3<T> &dir) {
     const Bsdf &b = bsdf_of_tri(s, tri);
     TBsdf<T> o;
     T jacobian(1.0f);
-    TV3<T> dir;
-    // forward recompute (as ad_bsdf_sampling)
+    if (lcsTri >= 0) {
+        TV3<T> nextPos, nextNormal;
+        ad_sample_triangle(s, lcsTri, r0, r1, nextPos, nextNormal);
+        const float shapePdf = s.lights[area_light_of_tri(s, lcsTri)].invTotalArea;
+        dir = nextPos - ps.isect.position;
+        const T distSq = dot(dir, dir);
+        const T invDistSq = 1.0f / distSq;
+        const T invDist = sqrt(invDistSq);
+        dir = dir * invDist;
+        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o);
+        jacobian = fabs(dot(nextNormal, dir) * invDistSq) / shapePdf;
+    } else if (!useAbs) {
+        ad_sample(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dir, o, adjoint);
+    } else {
+        const T scaledTheta = kTwoPi * r0;
+        const T scaledPhi = kPi * r1;
+        const T sinPhi = sin(scaledPhi);
+        const T cosPhi = cos(scaledPhi);
+        jacobian = fabs(sinPhi);
+        dir = TV3<T>(sinPhi * cos(scaledTheta), sinPhi * sin(scaledTheta), cosPhi);
+        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o, adjoint);
+    }
+    TV3<T> contrib = o.contrib;
+    if (adjoint) contrib = contrib * ad_snc(ps.wi, ps.isect, dir);
+    contrib = contrib * jacobian;
+    ps.cur = tmis(o.cosWo / o.pdf) * (ps.cur * tmis(o.revPdf) + ps.prev);
+    ps.prev = tmis(1.0f / o.pdf);
+    ps.throughput = cmul(ps.throughput, contrib);
+}
+
+// Its adjoint: the updated state's adjoints in `nb` (isect and wi unused), the
+// direction's in dirb_; the input state's accumulate into `ib`. The BSDF's
+// forward outputs reach the MIS and throughput adjoints through the BSDF
+// adjoint's callback, so each vertex evaluates its BSDF once here.
+template <class T>
+DEV void bsdf_sampling_adj(const SceneView &s, int tri, const T &r0, const T &r1, float disc, bool useAbs,
+                           int lcsTri, bool adjoint, const TState<T> &ps, const TV3<T> &dirb_, const TState<T> &nb,
+                           TState<T> &ib, T &r0b, T &r1b) {
+    const Bsdf &b = bsdf_of_tri(s, tri);
+    T jacobian(1.0f);
+    TV3<T> dir = tzero<T>();
     TV3<T> nextPos, nextNormal, d0;
-    T distSq(0.0f), invDistSq(0.0f), invDist(0.0f), J0(0.0f);
+    T distSq(0.0f), invDistSq(0.0f), invDist(0.0f), J0(0.0f), sinP(0.0f);
     float shapePdf = 1.0f;
     if (lcsTri >= 0) {
         ad_sample_triangle(s, lcsTri, r0, r1, nextPos, nextNormal);
@@ -783,56 +899,59 @@ DEV void bsdf_sampling_adj(const SceneView &s, int tri, const T &r0, const T &r1
         invDistSq = 1.0f / distSq;
         invDist = sqrt(invDistSq);
         dir = d0 * invDist;
-        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o);
         J0 = dot(nextNormal, dir) * invDistSq;
         jacobian = fabs(J0) / shapePdf;
-    } else if (!useAbs) {
-        ad_sample(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dir, o, adjoint);
-    } else {
+    } else if (useAbs) {
         const T sP = kPi * r1;
-        const T sinP = sin(sP);
+        sinP = sin(sP);
         jacobian = fabs(sinP);
         dir = TV3<T>(sinP * cos(kTwoPi * r0), sinP * sin(kTwoPi * r0), cos(sP));
-        ad_evaluate(b, ps.wi, ps.isect.shadingNormal, dir, o, adjoint);
     }
-    T sncv(1.0f);
-    if (adjoint) sncv = ad_snc(ps.wi, ps.isect, dir);
-    const TV3<T> cs = o.contrib * sncv;
-    const TV3<T> contrib = cs * jacobian;
-    // reverse
-    const TV3<T> tpb = cmul(nb.throughput, contrib);
-    ib.throughput = ib.throughput + tpb;
-    const TV3<T> contribb = cmul(nb.throughput, ps.throughput);
-    const T k = o.cosWo / o.pdf;
-    const T rp2 = o.revPdf * o.revPdf;
-    const T A = ps.cur * rp2 + ps.prev;
-    const T m = k * k;
-    TBsdfAdj<T> ob;
-    ob.contrib = tzero<T>();
-    const T mb = nb.cur * A;
-    ib.cur = ib.cur + nb.cur * m * rp2;
-    ib.prev = ib.prev + nb.cur * m;
-    ob.revPdf = nb.cur * m * ps.cur * 2.0f * o.revPdf;
-    const T kb = 2.0f * k * mb;
-    ob.cosWo = kb / o.pdf;
-    const T ip = 1.0f / o.pdf;
-    ob.pdf = -kb * k / o.pdf - nb.prev * 2.0f * ip * ip * ip;
-    const T jacb = dot(cs, contribb);
-    const TV3<T> csb = contribb * jacobian;
+    T jacb(0.0f);
+    // the adjoints of the BSDF outputs o (and the snc factor's share of wo's adjoint)
+    auto obf = [&](const TBsdf<T> &o, const TV3<T> &wo, TV3<T> &wob) -> TBsdfAdj<T> {
+        T sncv(1.0f);
+        if (adjoint) sncv = ad_snc(ps.wi, ps.isect, wo);
+        const TV3<T> cs = o.contrib * sncv;
+        const TV3<T> contrib = cs * jacobian;
+        ib.throughput = ib.throughput + cmul(nb.throughput, contrib);
+        const TV3<T> contribb = cmul(nb.throughput, ps.throughput);
+        const T k = o.cosWo / o.pdf;
+        const T rp2 = o.revPdf * o.revPdf;
+        const T A = ps.cur * rp2 + ps.prev;
+        const T m = k * k;
+        TBsdfAdj<T> ob;
+        const T mb = nb.cur * A;
+        ib.cur = ib.cur + nb.cur * m * rp2;
+        ib.prev = ib.prev + nb.cur * m;
+        ob.revPdf = nb.cur * m * ps.cur * 2.0f * o.revPdf;
+        const T kb = 2.0f * k * mb;
+        ob.cosWo = kb / o.pdf;
+        const T ip = 1.0f / o.pdf;
+        ob.pdf = -kb * k / o.pdf - nb.prev * 2.0f * ip * ip * ip;
+        jacb = dot(cs, contribb);
+        const TV3<T> csb = contribb * jacobian;
+        if (adjoint) {
+            ob.contrib = csb * sncv;
+            snc_adj(ps.wi, ps.isect, wo, dot(o.contrib, csb), ib.wi, ib.isect.shadingNormal, wob);
+        } else {
+            ob.contrib = csb;
+        }
+        return ob;
+    };
     TV3<T> dirb = dirb_;
-    if (adjoint) {
-        const T sncb = dot(o.contrib, csb);
-        ob.contrib = csb * sncv;
-        snc_adj(ps.wi, ps.isect, dir, sncb, ib.wi, ib.isect.shadingNormal, dirb);
-    } else {
-        ob.contrib = csb;
+    if (lcsTri < 0 && !useAbs) {
+        sample_adj(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dirb, obf, adjoint, ib.wi, ib.isect.shadingNormal,
+                   r0b, r1b);
+        return;
     }
+    evaluate_adj(b, ps.wi, ps.isect.shadingNormal, dir, obf, lcsTri >= 0 ? false : adjoint, ib.wi,
+                 ib.isect.shadingNormal, dirb);
     if (lcsTri >= 0) {
         const T J0b = jacb * sgn_of(J0) / shapePdf;
-        TV3<T> nnb = dir * (J0b * invDistSq);
+        const TV3<T> nnb = dir * (J0b * invDistSq);
         dirb = dirb + nextNormal * (J0b * invDistSq);
         T invDistSqb = J0b * dot(nextNormal, dir);
-        evaluate_adj(b, ps.wi, ps.isect.shadingNormal, dir, ob, false, ib.wi, ib.isect.shadingNormal, dirb);
         TV3<T> d0b = dirb * invDist;
         const T invDistb = dot(d0, dirb);
         invDistSqb = invDistSqb + invDistb * (0.5f / invDist);
@@ -840,12 +959,7 @@ DEV void bsdf_sampling_adj(const SceneView &s, int tri, const T &r0, const T &r1
         d0b = d0b + d0 * (2.0f * distSqb);
         ib.isect.position = ib.isect.position - d0b;
         sample_triangle_adj(s, lcsTri, r0, r1, d0b, nnb, r0b, r1b);
-    } else if (!useAbs) {
-        sample_adj(b, ps.wi, ps.isect.shadingNormal, r0, r1, disc, dirb, ob, adjoint, ib.wi, ib.isect.shadingNormal,
-                   r0b, r1b);
     } else {
-        evaluate_adj(b, ps.wi, ps.isect.shadingNormal, dir, ob, adjoint, ib.wi, ib.isect.shadingNormal, dirb);
-        const T sinP = sin(kPi * r1);
         sphere_dir_adj(r0, r1, dirb, jacb * sgn_of(sinP), r0b, r1b);
     }
 }
@@ -1069,13 +1183,14 @@ DEV void hit_adj(const SceneView &s, int tri, int kind, const Carry<T> &C, const
     Cb.dir = Cb.dir + dirb;
 }
 
-// One BSDF sampling step at vertex vi: vertex state + (r0, r1) -> the next carry.
-template <class T, bool adjoint>
-DEV void step_fwd(const SceneView &s, const PathRec &r, int vi, int lcsTri, const T &r0, const T &r1,
+// One BSDF sampling step at vertex vi: vertex state + (r0, r1) -> the next
+// carry (adjoint: the light subpath's EvaluateBSDF(true, ...) forms).
+template <class T>
+DEV void step_fwd(const SceneView &s, const PathRec &r, int vi, int lcsTri, bool adjoint, const T &r0, const T &r1,
                   const TState<T> &V, Carry<T> &Cn) {
     TState<T> ps = V;
     TV3<T> dir;
-    ad_bsdf_sampling<T, adjoint>(s, r.tri[vi], r0, r1, r.disc[vi], (r.useAbs >> vi) & 1u, lcsTri, ps, dir);
+    bsdf_sampling_fwd(s, r.tri[vi], r0, r1, r.disc[vi], (r.useAbs >> vi) & 1u, lcsTri, adjoint, ps, dir);
     Cn.tp = ps.throughput * r.rr[vi];
     Cn.org = V.isect.position;
     Cn.dir = dir;
@@ -1083,8 +1198,8 @@ DEV void step_fwd(const SceneView &s, const PathRec &r, int vi, int lcsTri, cons
     Cn.cur = ps.cur;
 }
 
-template <class T, bool adjoint>
-DEV void step_adj(const SceneView &s, const PathRec &r, int vi, int lcsTri, const T &r0, const T &r1,
+template <class T>
+DEV void step_adj(const SceneView &s, const PathRec &r, int vi, int lcsTri, bool adjoint, const T &r0, const T &r1,
                   const TState<T> &V, const Carry<T> &Cnb, TState<T> &Vb, T &r0b, T &r1b) {
     TState<T> nb;
     state_zero(nb);
@@ -1092,8 +1207,8 @@ DEV void step_adj(const SceneView &s, const PathRec &r, int vi, int lcsTri, cons
     nb.prev = Cnb.prev;
     nb.cur = Cnb.cur;
     Vb.isect.position = Vb.isect.position + Cnb.org;
-    bsdf_sampling_adj<T, adjoint>(s, r.tri[vi], r0, r1, r.disc[vi], (r.useAbs >> vi) & 1u, lcsTri, V, Cnb.dir, nb, Vb,
-                                  r0b, r1b);
+    bsdf_sampling_adj(s, r.tri[vi], r0, r1, r.disc[vi], (r.useAbs >> vi) & 1u, lcsTri, adjoint, V, Cnb.dir, nb, Vb,
+                      r0b, r1b);
 }
 
 // Light emission (EmitAreaLight / EmitEnvLight / EmitPointLight, AD forms):
@@ -1225,31 +1340,7 @@ DEV void camera_adj(const SceneView &s, const T &sx, const T &sy, const Carry<T>
 
 // ConnectToCamera (AD) at the last light vertex V (technique c = 1).
 template <class T>
-DEV TV3<T> connect_camera_fwd(const SceneView &s, int tri, const TState<T> &V) {
-    const float pixelCount = float(s.cam.width * s.cam.height);
-    TV3<T> camOrg, camDir;
-    ad_sample_primary(s.cam, T(0.5f), T(0.5f), camOrg, camDir);
-    TV3<T> dtc = camOrg - V.isect.position;
-    const T distSq = dot(dtc, dtc);
-    const T dist = sqrt(distSq);
-    dtc = dtc * (1.0f / dist);
-    TBsdf<T> o;
-    ad_evaluate(bsdf_of_tri(s, tri), V.wi, V.isect.shadingNormal, dtc, o, true);
-    const TV3<T> bsdfContrib = o.contrib * ad_snc(V.wi, V.isect, dtc);
-    const T ic = -(1.0f / dot(camDir, dtc));
-    const T ip = s.cam.dist * ic;
-    const T i2sa = (ip * ip) * ic;
-    const T i2s = i2sa * fabs(o.cosWo) / distSq;
-    const T wLight = tmis(i2s / pixelCount) * (V.prev + V.cur * tmis(o.revPdf));
-    const T mis = 1.0f / (wLight + 1.0f);
-    const T s2i = o.cosWo / i2s;
-    const T denom = pixelCount * s2i;
-    const TV3<T> cc = (mis * bsdfContrib) * (1.0f / denom);
-    return cmul(cc, V.throughput);
-}
-
-template <class T>
-DEV void connect_camera_adj(const SceneView &s, int tri, const TState<T> &V, const TV3<T> &contribb, TState<T> &Vb) {
+DEV void connect_camera_adj(const SceneView &s, int tri, const TState<T> &V, TState<T> &Vb) {
     const float pixelCount = float(s.cam.width * s.cam.height);
     const Bsdf &b = bsdf_of_tri(s, tri);
     TV3<T> camOrg, camDir;
@@ -1278,6 +1369,7 @@ DEV void connect_camera_adj(const SceneView &s, int tri, const TState<T> &V, con
     const T idn = 1.0f / denom;
     const TV3<T> mbc = mis * bsdfContrib;
     const TV3<T> cc = mbc * idn;
+    const TV3<T> contribb = logf_seed(cmul(cc, V.throughput));
     // reverse
     const TV3<T> ccb = cmul(contribb, V.throughput);
     Vb.throughput = Vb.throughput + cmul(contribb, cc);
@@ -1308,7 +1400,7 @@ DEV void connect_camera_adj(const SceneView &s, int tri, const TState<T> &V, con
     ob.contrib = bcb * sncv;
     const T sncb = dot(o.contrib, bcb);
     snc_adj(V.wi, V.isect, dtc, sncb, Vb.wi, Vb.isect.shadingNormal, dtcb);
-    evaluate_adj(b, V.wi, V.isect.shadingNormal, dtc, ob, true, Vb.wi, Vb.isect.shadingNormal, dtcb);
+    evaluate_adj(b, V.wi, V.isect.shadingNormal, dtc, FixedOb<T>{ob}, true, Vb.wi, Vb.isect.shadingNormal, dtcb);
     TV3<T> dtc0b = dtcb * idist;
     const T idistb = dot(dtc0, dtcb);
     const T distb = -idistb * idist * idist;
@@ -1319,21 +1411,7 @@ DEV void connect_camera_adj(const SceneView &s, int tri, const TState<T> &V, con
 
 // The camera ray leaves the scene: HandleHitLight with EmissionEnvLight (AD).
 template <class T>
-DEV TV3<T> env_exit_fwd(const SceneView &s, const Carry<T> &C) {
-    const Light &L = s.lights[s.envLight];
-    TV3<T> emission;
-    T directPdf, emissionPdf;
-    ad_env_emission(s, L, C.dir, emission, directPdf, emissionPdf);
-    TV3<T> tp = cmul(C.tp, emission);
-    const float pick = pick_light_prob(s, s.envLight);
-    directPdf = directPdf * pick;
-    emissionPdf = emissionPdf * pick;
-    const T wCamera = tmis(directPdf) * C.prev + tmis(emissionPdf) * C.cur;
-    return tp * (1.0f / (1.0f + wCamera));
-}
-
-template <class T>
-DEV void env_exit_adj(const SceneView &s, const Carry<T> &C, const TV3<T> &contribb, Carry<T> &Cb) {
+DEV void env_exit_adj(const SceneView &s, const Carry<T> &C, Carry<T> &Cb) {
     const Light &L = s.lights[s.envLight];
     TV3<T> emission;
     T dp, ep;
@@ -1343,6 +1421,7 @@ DEV void env_exit_adj(const SceneView &s, const Carry<T> &C, const TV3<T> &contr
     const T dP = dp * pick, eP = ep * pick;
     const T wC = dP * dP * C.prev + eP * eP * C.cur;
     const T iS = 1.0f / (1.0f + wC);
+    const TV3<T> contribb = logf_seed(tpE * iS);
     const TV3<T> tpEb = contribb * iS;
     const T wCb = -dot(tpE, contribb) * iS * iS;
     Cb.prev = Cb.prev + wCb * dP * dP;
@@ -1356,23 +1435,8 @@ DEV void env_exit_adj(const SceneView &s, const Carry<T> &C, const TV3<T> &contr
 // A camera ray that ends on an area light: HandleHitLight (AD), after the
 // arrival's MIS conversion (hit kind kHitAreaLight).
 template <class T>
-DEV TV3<T> area_hit_fwd(const SceneView &s, int tri, const TState<T> &V, const TV3<T> &dir) {
-    const int li = area_light_of_tri(s, tri);
-    const Light &L = s.lights[li];
-    const T cosAtLight = -dot(V.isect.shadingNormal, dir);
-    T directPdf(L.invTotalArea);
-    T emissionPdf = cosAtLight * directPdf * kInvPi;
-    TV3<T> tp = cmul(V.throughput, tv<T>(V3(L.emission[0], L.emission[1], L.emission[2])));
-    const float pick = pick_light_prob(s, li);
-    directPdf = directPdf * pick;
-    emissionPdf = emissionPdf * pick;
-    const T wCamera = tmis(directPdf) * V.prev + tmis(emissionPdf) * V.cur;
-    return tp * (1.0f / (1.0f + wCamera));
-}
-
-template <class T>
-DEV void area_hit_adj(const SceneView &s, int tri, const TState<T> &V, const TV3<T> &dir, const TV3<T> &contribb,
-                      TState<T> &Vb, TV3<T> &dirb) {
+DEV void area_hit_adj(const SceneView &s, int tri, const TState<T> &V, const TV3<T> &dir, TState<T> &Vb,
+                      TV3<T> &dirb) {
     const int li = area_light_of_tri(s, tri);
     const Light &L = s.lights[li];
     const float pick = pick_light_prob(s, li);
@@ -1383,6 +1447,7 @@ DEV void area_hit_adj(const SceneView &s, int tri, const TState<T> &V, const TV3
     const T wC = dP * dP * V.prev + eP * eP * V.cur;
     const T iS = 1.0f / (1.0f + wC);
     const TV3<T> tpE = cmul(V.throughput, E);
+    const TV3<T> contribb = logf_seed(tpE * iS);
     const T wCb = -dot(tpE, contribb) * iS * iS;
     Vb.throughput = Vb.throughput + cmul(contribb * iS, E);
     Vb.prev = Vb.prev + wCb * dP * dP;
@@ -1394,51 +1459,8 @@ DEV void area_hit_adj(const SceneView &s, int tri, const TState<T> &V, const TV3
 
 // DirectLighting (AD) at the last camera vertex V, (r0, r1) the light sample.
 template <class T>
-DEV TV3<T> direct_fwd(const SceneView &s, const PathRec &r, int tri, const TState<T> &V, const T &r0, const T &r1) {
-    const Light &L = s.lights[r.dlLight];
-    TV3<T> dirToLight, lightContrib;
-    T cosAtLight, directPdf, emissionPdf;
-    if (L.type == kLightArea) {
-        TV3<T> pl, nl2;
-        ad_sample_triangle(s, light_tri(s, L, r.dlPrim), r0, r1, pl, nl2);
-        dirToLight = pl - V.isect.position;
-        const T distSq = dot(dirToLight, dirToLight);
-        const T dist = sqrt(distSq);
-        dirToLight = TV3<T>(dirToLight.x / dist, dirToLight.y / dist, dirToLight.z / dist);
-        cosAtLight = -dot(dirToLight, nl2);
-        directPdf = L.invTotalArea * distSq / cosAtLight;
-        const TV3<T> E = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2]));
-        lightContrib = TV3<T>(E.x / directPdf, E.y / directPdf, E.z / directPdf);
-        emissionPdf = L.invTotalArea * cosAtLight * kInvPi;
-    } else if (L.type == kLightEnv) {
-        TV3<T> value;
-        ad_env_sample_direction(s, r0, r1, dirToLight, value, directPdf);
-        lightContrib = value * (1.0f / directPdf) * L.samplingWeight;
-        cosAtLight = T(1.0f);
-        emissionPdf = directPdf * env_position_pdf(s);
-    } else {
-        dirToLight = tv<T>(V3(L.pos[0], L.pos[1], L.pos[2])) - V.isect.position;
-        const T distSq = dot(dirToLight, dirToLight);
-        directPdf = distSq;
-        const T dist = sqrt(distSq);
-        dirToLight = TV3<T>(dirToLight.x / dist, dirToLight.y / dist, dirToLight.z / dist);
-        lightContrib = tv<T>(V3(L.emission[0], L.emission[1], L.emission[2])) * (1.0f / distSq);
-        emissionPdf = T(1.0f / (4.0f * kPi));
-        cosAtLight = T(1.0f);
-    }
-    TBsdf<T> o;
-    ad_evaluate(bsdf_of_tri(s, tri), V.wi, V.isect.shadingNormal, dirToLight, o);
-    const float pick = pick_light_prob(s, r.dlLight);
-    TV3<T> tp = cmul(V.throughput, o.contrib);
-    tp = cmul(tp, lightContrib) * (1.0f / pick);
-    const T wLight = L.type == kLightPoint ? T(0.0f) : tmis(o.pdf / (pick * directPdf));
-    const T wCamera = tmis(emissionPdf * o.cosWo / (directPdf * cosAtLight)) * (V.prev + V.cur * tmis(o.revPdf));
-    return tp * (1.0f / (wLight + 1.0f + wCamera));
-}
-
-template <class T>
 DEV void direct_adj(const SceneView &s, const PathRec &r, int tri, const TState<T> &V, const T &r0, const T &r1,
-                    const TV3<T> &contribb, TState<T> &Vb, T &r0b, T &r1b) {
+                    TState<T> &Vb, T &r0b, T &r1b) {
     const Light &L = s.lights[r.dlLight];
     const Bsdf &b = bsdf_of_tri(s, tri);
     TV3<T> dtl, lc, dtl0, pl, nl2;
@@ -1487,6 +1509,7 @@ DEV void direct_adj(const SceneView &s, const PathRec &r, int tri, const TState<
     const T wC = kk * kk * A;
     const T iS = 1.0f / (wL + 1.0f + wC);
     // reverse
+    const TV3<T> contribb = logf_seed(tp2 * iS);
     const TV3<T> tp2b = contribb * iS;
     const T Sb = -dot(tp2, contribb) * iS * iS;
     const T kkb = Sb * A * 2.0f * kk;
@@ -1510,7 +1533,7 @@ DEV void direct_adj(const SceneView &s, const PathRec &r, int tri, const TState<
     Vb.throughput = Vb.throughput + cmul(tp1b, o.contrib);
     ob.contrib = cmul(tp1b, V.throughput);
     TV3<T> dtlb = tzero<T>();
-    evaluate_adj(b, V.wi, V.isect.shadingNormal, dtl, ob, false, Vb.wi, Vb.isect.shadingNormal, dtlb);
+    evaluate_adj(b, V.wi, V.isect.shadingNormal, dtl, FixedOb<T>{ob}, false, Vb.wi, Vb.isect.shadingNormal, dtlb);
     if (L.type == kLightEnv) {
         dpb = dpb + epb * env_position_pdf(s) - dot(value, lcb) * L.samplingWeight / (dp * dp);
         env_sample_direction_adj(s, r0, r1, dtlb, lcb * (L.samplingWeight / dp), dpb, r0b, r1b);
@@ -1538,29 +1561,8 @@ DEV void direct_adj(const SceneView &s, const PathRec &r, int tri, const TState<
 
 // ConnectVertex (AD): camera vertex V, light vertex W.
 template <class T>
-DEV TV3<T> connect_fwd(const SceneView &s, int ctri, int ltri, const TState<T> &V, const TState<T> &W) {
-    TV3<T> dtl = W.isect.position - V.isect.position;
-    const T distSq = dot(dtl, dtl);
-    const T dist = sqrt(distSq);
-    dtl = dtl * (1.0f / dist);
-    TBsdf<T> cb, lb;
-    ad_evaluate(bsdf_of_tri(s, ctri), V.wi, V.isect.shadingNormal, dtl, cb);
-    ad_evaluate(bsdf_of_tri(s, ltri), W.wi, W.isect.shadingNormal, -dtl, lb, true);
-    const TV3<T> lgtF = lb.contrib * ad_snc(W.wi, W.isect, -dtl);
-    const T G = 1.0f / distSq;
-    const T camA = cb.pdf * lb.cosWo * G;
-    const T lgtA = lb.pdf * cb.cosWo * G;
-    const T wLight = tmis(camA) * (W.prev + W.cur * tmis(lb.revPdf));
-    const T wCamera = tmis(lgtA) * (V.prev + V.cur * tmis(cb.revPdf));
-    const T misWeight = 1.0f / (wLight + 1.0f + wCamera);
-    TV3<T> tp = cmul(W.throughput, V.throughput);
-    tp = cmul(tp, cb.contrib);
-    return cmul(tp, lgtF) * (G * misWeight);
-}
-
-template <class T>
 DEV void connect_adj(const SceneView &s, int ctri, int ltri, const TState<T> &V, const TState<T> &W,
-                     const TV3<T> &contribb, TState<T> &Vb, TState<T> &Wb) {
+                     TState<T> &Vb, TState<T> &Wb) {
     const Bsdf &bc = bsdf_of_tri(s, ctri), &bl = bsdf_of_tri(s, ltri);
     const TV3<T> dtl0 = W.isect.position - V.isect.position;
     const T distSq = dot(dtl0, dtl0);
@@ -1583,6 +1585,7 @@ DEV void connect_adj(const SceneView &s, int ctri, int ltri, const TState<T> &V,
     const TV3<T> t2 = cmul(t1, cb.contrib);
     const TV3<T> t3 = cmul(t2, lgtF);
     // reverse
+    const TV3<T> contribb = logf_seed(t3 * (G * mis));
     const TV3<T> t3b = contribb * (G * mis);
     const T gmb = dot(t3, contribb);
     T Gb = gmb * mis;
@@ -1613,9 +1616,9 @@ DEV void connect_adj(const SceneView &s, int ctri, int ltri, const TState<T> &V,
     const T snlb = dot(lb.contrib, lgtFb);
     TV3<T> mdb = tzero<T>();
     snc_adj(W.wi, W.isect, -dtl, snlb, Wb.wi, Wb.isect.shadingNormal, mdb);
-    evaluate_adj(bl, W.wi, W.isect.shadingNormal, -dtl, lbb, true, Wb.wi, Wb.isect.shadingNormal, mdb);
+    evaluate_adj(bl, W.wi, W.isect.shadingNormal, -dtl, FixedOb<T>{lbb}, true, Wb.wi, Wb.isect.shadingNormal, mdb);
     TV3<T> dtlb = -mdb;
-    evaluate_adj(bc, V.wi, V.isect.shadingNormal, dtl, cbb, false, Vb.wi, Vb.isect.shadingNormal, dtlb);
+    evaluate_adj(bc, V.wi, V.isect.shadingNormal, dtl, FixedOb<T>{cbb}, false, Vb.wi, Vb.isect.shadingNormal, dtlb);
     TV3<T> dtl0b = dtlb * idist;
     const T idistb = dot(dtl0, dtlb);
     distSqb = distSqb - idistb * idist * idist * (0.5f / dist);
@@ -1640,7 +1643,6 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
     Carry<T> ck[kMaxLen];
     Carry<T> C;
     TState<T> lpFinal, V;
-    TV3<T> contrib = tzero<T>();
     const bool envLight = l > 1 && s.lights[r.lgtLight].type == kLightEnv;
     int k = 0;
     // ---- forward
@@ -1654,10 +1656,9 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
             hit_fwd(s, r.tri[d], kind, C, V);
             if (d == nl - 1) {
                 lpFinal = V;
-                if (c == 1) contrib = connect_camera_fwd(s, r.tri[d], V);
                 break;
             }
-            step_fwd<T, true>(s, r, d, -1, u[k], u[k + 1], V, C);
+            step_fwd(s, r, d, -1, true, u[k], u[k + 1], V, C);
             k += 2;
         }
     }
@@ -1671,31 +1672,20 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
             const int vi = nl + d;
             const int tri = r.tri[vi];
             ck[vi] = C;
-            if (d == nc - 1 && l == 0 && tri < 0) {
-                contrib = env_exit_fwd(s, C);
-                break;
-            }
-            const bool areaEnd = d == nc - 1 && l == 0;
-            hit_fwd(s, tri, areaEnd ? kHitAreaLight : kHitGeneric, C, V);
-            if (d == nc - 1) {
-                if (l == 0) contrib = area_hit_fwd(s, tri, V, C.dir);
-                else if (l == 1) contrib = direct_fwd(s, r, tri, V, u[k], u[k + 1]);
-                else contrib = connect_fwd(s, tri, r.tri[nl - 1], V, lpFinal);
-                break;
-            }
+            // the last vertex and its connection: in the backward sweep, which
+            // evaluates the contribution (and with it log f's seed) there
+            if (d == nc - 1) break;
+            hit_fwd(s, tri, kHitGeneric, C, V);
             if (l == 0 && d == nc - 2 && s.opt.useLightCoordinateSampling) {
                 const int lastTri = r.tri[nl + nc - 1];
                 const int li = lastTri >= 0 ? area_light_of_tri(s, lastTri) : -1;
                 if (li >= 0 && s.lights[li].type == kLightArea) lcsTri = lastTri;
             }
-            step_fwd<T, false>(s, r, vi, d == nc - 2 ? lcsTri : -1, u[k], u[k + 1], V, C);
+            step_fwd(s, r, vi, d == nc - 2 ? lcsTri : -1, false, u[k], u[k + 1], V, C);
             k += 2;
         }
     }
-    // ---- backward: f = log(lum(contrib))
-    const T lum = tlum(contrib);
-    TV3<T> contribb = tzero<T>();
-    tlum_adj(1.0f / lum, contribb);
+    // ---- backward: f = log(lum(contrib)), seeded in the final connection's adjoint
     TState<T> lpb;
     state_zero(lpb);
     if (c > 1) {
@@ -1705,7 +1695,7 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
             const int d = nc - 1, vi = nl + d, tri = r.tri[vi];
             const Carry<T> &Cv = ck[vi];
             if (l == 0 && tri < 0) {
-                env_exit_adj(s, Cv, contribb, Cb);
+                env_exit_adj(s, Cv, Cb);
             } else {
                 const int kind = l == 0 ? kHitAreaLight : kHitGeneric;
                 hit_fwd(s, tri, kind, Cv, V);
@@ -1713,13 +1703,13 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
                 state_zero(Vb);
                 if (l == 0) {
                     TV3<T> dirb = tzero<T>();
-                    area_hit_adj(s, tri, V, Cv.dir, contribb, Vb, dirb);
+                    area_hit_adj(s, tri, V, Cv.dir, Vb, dirb);
                     Cb.dir = Cb.dir + dirb;
                 } else if (l == 1) {
                     const int kd = kc0 + 2 + 2 * d;
-                    direct_adj(s, r, tri, V, u[kd], u[kd + 1], contribb, Vb, ub[kd], ub[kd + 1]);
+                    direct_adj(s, r, tri, V, u[kd], u[kd + 1], Vb, ub[kd], ub[kd + 1]);
                 } else {
-                    connect_adj(s, tri, r.tri[nl - 1], V, lpFinal, contribb, Vb, lpb);
+                    connect_adj(s, tri, r.tri[nl - 1], V, lpFinal, Vb, lpb);
                 }
                 hit_adj(s, tri, kind, Cv, V, Vb, Cb);
             }
@@ -1731,13 +1721,13 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
             hit_fwd(s, tri, kHitGeneric, ck[vi], V);
             TState<T> Vb;
             state_zero(Vb);
-            step_adj<T, false>(s, r, vi, d == nc - 2 ? lcsTri : -1, u[kd], u[kd + 1], V, Cb, Vb, ub[kd], ub[kd + 1]);
+            step_adj(s, r, vi, d == nc - 2 ? lcsTri : -1, false, u[kd], u[kd + 1], V, Cb, Vb, ub[kd], ub[kd + 1]);
             Cb.zero();
             hit_adj(s, tri, kHitGeneric, ck[vi], V, Vb, Cb);
         }
         camera_adj(s, u[kc0], u[kc0 + 1], Cb, ub[kc0], ub[kc0 + 1]);
     } else if (l > 1) {
-        connect_camera_adj(s, r.tri[nl - 1], lpFinal, contribb, lpb);
+        connect_camera_adj(s, r.tri[nl - 1], lpFinal, lpb);
     }
     if (l > 1) {
         Carry<T> Cb;
@@ -1754,7 +1744,7 @@ DEV void adj_row(const SceneView &s, const PathRec &r, int dim, int row, float *
             hit_fwd(s, r.tri[d], kind, ck[d], V);
             TState<T> Vb;
             state_zero(Vb);
-            step_adj<T, true>(s, r, d, -1, u[kd], u[kd + 1], V, Cb, Vb, ub[kd], ub[kd + 1]);
+            step_adj(s, r, d, -1, true, u[kd], u[kd + 1], V, Cb, Vb, ub[kd], ub[kd + 1]);
             Cb.zero();
             hit_adj(s, r.tri[d], kind, ck[d], V, Vb, Cb);
         }
