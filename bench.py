@@ -483,9 +483,10 @@ def cpu_baseline_sample(sd, seconds: float = 15.0):
 
 
 def schedule_times(sd, device, seed, shape, iterations=8):
-    """ms per iteration of the three chain-loop schedules (they take identical
-    steps): staged at the tuned shape, wavefront rounds, and the persistent
-    cooperative kernel (a quarter and half of the SMs as team workers)."""
+    """ms per iteration of the three chain-loop schedules (they take the same
+    steps; the persistent one with hyper-dual derivatives throughout): staged at
+    the tuned shape, wavefront rounds, and the persistent cooperative kernel (a
+    quarter and half of the SMs as team workers)."""
     from drmlt.integrator import Renderer
     base = dict(autotune=0, stage_lanes=shape["chains_per_warp"], stage2_lanes=shape["stage2_chains_per_warp"],
                 deriv_warps=shape["derivative_warps"], head_chains=shape["head_chains"], head_lanes=shape["head_lanes"],

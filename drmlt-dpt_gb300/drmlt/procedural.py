@@ -280,14 +280,15 @@ def main(argv=None):
     ap.add_argument("--team-sms", type=int, default=0, help="persistent schedule: SMs of the team workers")
     ap.add_argument("--rays", default="", choices=["", "primary", "bounce", "shadow"])
     ap.add_argument("--adjoint-min-dim", type=int, default=0,
-                    help="derivatives by the reverse-mode adjoint from this path dimension on (0: none)")
+                    help="derivatives by the reverse-mode adjoint from this path dimension on "
+                         "(0: library default, -1: hyper-dual for every path)")
     ap.add_argument("--head-chains", type=int, default=0, help="two-tier stage 1: chains of the head tier")
     ap.add_argument("--head-lanes", type=int, default=0, help="two-tier stage 1: chains per warp of the head tier")
     a = ap.parse_args(argv)
     sd = globals()[a.scene]()
     r = Renderer(sd, seed=77, use_graph=a.graph, stage_lanes=a.lanes, stage2_lanes=a.lanes2, deriv_warps=a.warps,
                  wavefront=a.wavefront, persistent=a.persistent, team_sms=a.team_sms,
-                 adjoint_min_dim=a.adjoint_min_dim if a.adjoint_min_dim > 0 else -1,
+                 adjoint_min_dim=a.adjoint_min_dim,
                  head_chains=a.head_chains, head_lanes=a.head_lanes)
     r.prepass()
     r.run(a.iterations)

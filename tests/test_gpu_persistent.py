@@ -40,11 +40,14 @@ def _scene(cfg, dr_type, root):
 def test_persistent_takes_the_staged_steps(built_lib, scene_root, cfg, dr_type):
     """Two persistent runs (4 + 7 iterations) against staged launches of the same
     11 iterations, on scenes with Phong and rough-dielectric BSDFs, the
-    environment light, Green's y* and depth-12 paths (cfg4s)."""
+    environment light, Green's y* and depth-12 paths (cfg4s). The persistent
+    schedule takes hyper-dual derivatives for every path, so the staged run
+    does too (adjoint_min_dim=-1: the adjoint rounds differently)."""
     from drmlt.integrator import Renderer
     sd = _scene(cfg, dr_type, scene_root)
     out = []
-    for kw in (dict(persistent=1), dict(persistent=1, team_sms=3, stage_lanes=32), dict(persistent=0)):
+    for kw in (dict(persistent=1), dict(persistent=1, team_sms=3, stage_lanes=32),
+               dict(persistent=0, adjoint_min_dim=-1)):
         with Renderer(sd, num_chains=4096, **kw) as r:
             r.prepass()
             assert r.run(4) == 4 * 4096
@@ -66,7 +69,7 @@ def test_persistent_extra_samples_and_run_end(built_lib, scene_root):
     from drmlt.integrator import Renderer
     sd = dscene.load_scene(scenegen.config1(os.path.join(scene_root, "persist_extra"), spp=1))
     out = []
-    for kw in (dict(persistent=1), dict(persistent=0)):
+    for kw in (dict(persistent=1), dict(persistent=0, adjoint_min_dim=-1)):
         with Renderer(sd, num_chains=5041, **kw) as r:
             assert r.total_iterations() == 14
             r.prepass()

@@ -140,8 +140,8 @@ def test_tuning_parameters_do_not_change_the_chains(built_lib, scene_root):
 
 def test_adjoint_derivatives_in_the_chain_loop(built_lib, scene_root):
     """The chain loop with every H2MC derivative by the reverse-mode adjoint
-    (adjoint_min_dim=1), by hyper-dual forward mode alone (-1, the default) and
-    mixed (the adjoint from dimension 10 on). The two methods give the same
+    (adjoint_min_dim=1), by hyper-dual forward mode alone (-1, the default)
+    and mixed (the adjoint from dimension 10 on). The two methods give the same
     derivatives up to FP32 rounding, so the chains' H2MC acceptance and the
     images agree statistically: acceptance ratios within 0.01, and the runs'
     images as close to each other as two runs of one method with other
