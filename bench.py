@@ -22,8 +22,10 @@ Keys of the JSON line (ours):
                    timed separately (setup_s) and given with it as
                    value_with_setup
   time_to_relmse   seconds (direct pass, prepass, autotuning, chain loop) until
-  (_plain)         relMSE <= 0.01 against a long render, for the batched form
-                   and for the plain per-stage-launch drop-in
+  (_plain,         relMSE <= 0.01 against a long render, for the batched form
+   _adjoint)       (hyper-dual derivatives), the plain per-stage-launch drop-in
+                   and the batched form with the reverse-mode adjoint taking
+                   the derivatives of paths of dimension 10 and up
   roofline         the slowest chain-loop stage against the HBM peak
   cpu_baseline     the oracle's CPU chain loop (all host cores, the oracle's
                    own BVH) on a bounded sample of the same scene, with its
@@ -321,7 +323,7 @@ def run_ours(args, world, rank, local):
 
     out = None
     if rank == 0:
-        relmse = relmse_plain = None
+        relmse = relmse_plain = relmse_adjoint = None
         if not args.no_relmse:
             _, ref_spp, budget = WORKLOADS[args.workload]
             ref_spp = args.ref_spp or ref_spp
@@ -329,6 +331,9 @@ def run_ours(args, world, rank, local):
             spp = args.relmse_spp or budget
             relmse = time_to_relmse(sd, local, ref, ref_spp, spp=spp)
             relmse_plain = time_to_relmse(sd, local, ref, ref_spp, spp=spp, plain=True)
+            # the batched form with the reverse-mode adjoint taking the H2MC
+            # derivatives of paths of dimension 10 and up (drmlt_options.adjoint_min_dim)
+            relmse_adjoint = time_to_relmse(sd, local, ref, ref_spp, spp=spp, extra=dict(adjoint_min_dim=10))
         cpu = None if args.no_cpu else cpu_baseline_sample(sd, seconds=15.0)
         schedules = None if args.no_schedules else schedule_times(sd, local, seed + 2, shape)
         gb = (3 * SLOT_B + 3 * GAUSS_B + SCRATCH_B) * N / 1e9
@@ -350,6 +355,7 @@ def run_ours(args, world, rank, local):
             "rays": rays,
             "time_to_relmse": relmse,
             "time_to_relmse_plain": relmse_plain,
+            "time_to_relmse_adjoint": relmse_adjoint,
             "schedule_ms_per_iteration": schedules,
             "clocks": clk.summary(),
             "gpu_launches": launches,
@@ -411,7 +417,7 @@ def render_reference(sd, device, spp):
     return img
 
 
-def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False):
+def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False, extra=None):
     """Seconds of GPU rendering until the image is within relMSE `target` of a
     long render (`ref`, ref_spp samples per pixel, other random streams) of the
     same scene: the direct-lighting pass, the prepass (and the autotuner's
@@ -420,10 +426,10 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False)
     relMSE is within 1.5x of the target, so the crossing is resolved to ~3%).
     Partial images scale the indirect film by total / done iterations.
     plain=True runs the plain per-stage-launch configuration (PLAIN) without
-    autotuning."""
+    autotuning; `extra` adds drmlt_options to the batched form."""
     from drmlt.integrator import Renderer
 
-    kw = dict(PLAIN) if plain else {}
+    kw = dict(PLAIN) if plain else dict(extra or {})
     if spp:
         kw["spp"] = spp
     r = Renderer(sd, device=device, seed=0x5EED1234, **kw)
