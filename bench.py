@@ -456,8 +456,9 @@ def time_to_relmse(sd, device, ref, ref_spp, target=0.01, spp=None, plain=False,
             hit = setup_s + run_s
             break
         step = max(8, done // 4) if e > 1.5 * target else max(8, done // 32)
+    shape = r.launch_shape()
     r.close()
-    return {"value": hit, "unit": "s", "target_relmse": target, "reference": "%d spp GPU render, direct pass at %d spp" % (ref_spp, 64 * max(1, sd.options.directSpp)),
+    return {"value": hit, "unit": "s", "target_relmse": target, "launch_shape": shape, "reference": "%d spp GPU render, direct pass at %d spp" % (ref_spp, 64 * max(1, sd.options.directSpp)),
             "setup_s": setup_s, "iterations": done, "spp_equivalent": done * sd.options.numChains /
             (sd.width * sd.height), "mutations_per_s": done * sd.options.numChains / max(run_s, 1e-9),
             "checkpoints": checkpoints}

@@ -12,9 +12,8 @@ struct PathRec;
 // adjMinDim that selects hyper-dual forward mode for every path, which is
 // also the chain loop's default (drmlt_options.adjoint_min_dim = 0): with the
 // adjoint from dimension 10 on, config 4's derivative stages take 0.46 / 0.56
-// instead of 0.50 / 0.64 ms per iteration, but whole renders measured slower
-// (bench 4.01 against 3.96 ms per step, 4.31 against 4.00 ms per iteration
-// in the time-to-relMSE loop).
+// instead of 0.50 / 0.64 ms per iteration, but the iteration as a whole ties
+// (4.02 against 4.00 ms in a time-to-relMSE loop).
 constexpr int kNoAdjoint = 1 << 20;
 constexpr int kDefaultAdjMinDim = kNoAdjoint;
 
