@@ -25,7 +25,8 @@ struct Slot {
 
 enum : int {
     kActive = 1, kAccept1 = 2, kLarge = 4, kSecond = 8, kAniso = 16, kZValid = 32, kAccept2 = 64,
-    kSingle = 128  // integrator=h2mc: the anisotropic proposal is the only stage
+    kSingle = 128,  // integrator=h2mc: the anisotropic proposal is the only stage
+    kLens = 256     // integrator=h2mc: a lens-mutation candidate (k_lens)
 };
 
 struct Scratch {
@@ -51,6 +52,12 @@ enum : int {
     kStatLarge = 0, kStatLargeAcc, kStatStage1, kStatStage1Acc, kStatIso, kStatIsoAcc, kStatH2mc,
     kStatH2mcAcc, kStatMutations, kStatGauss, kStatGaussFallback, kNumStats
 };
+// Counters outside the per-thread StatAcc (added with single atomics where the
+// rare event happens): integrator=h2mc's lens mutations and their acceptances.
+enum : int { kStatLens = kNumStats, kStatLensAcc, kNumStatsAll };
+
+// Work-list lengths per chain group: [0] listX, [1] listZ, [2] listS, [3] listA, [4] listL.
+constexpr int kNumCounters = 8;
 
 struct ChainView {
     Slot *slots;        // N x 3
@@ -61,9 +68,10 @@ struct ChainView {
     int *listZ;         // chains needing a Gaussian at the second proposal
     int *listS;         // chains taking a second stage this iteration
     int *listA;         // chains taking the anisotropic (H2MC) second stage
+    int *listL;         // integrator=h2mc: chains drawn for the lens mutation
     int *order;         // stage-1 processing order (chains grouped by work class)
     int *hist;          // kPlanBins counters of the work classes
-    int *counters;      // [0] = |listX|, [1] = |listZ|, [2] = |listS|, [3] = |listA|
+    int *counters;      // [0] = |listX|, [1] = |listZ|, [2] = |listS|, [3] = |listA|, [4] = |listL|
     float *grad;        // N x kMaxDim (indexed by list position)
     float *hess;        // N x kMaxDim^2
     unsigned long long *stats;
@@ -90,6 +98,8 @@ struct RunParams {
     int drType;          // 0 green, 1 mira
     int integrator;      // 0 drmlt, 1 h2mc, 2 mcmc
     float uniformMix;
+    float lensProb;      // integrator=h2mc: lensPerturbProb
+    float lensSigma;     // integrator=h2mc: lensPerturbStdDev
     int accMap;
     int maxDerv;
     int gaussDim;        // largest path dimension (2 max_depth): sizes the Gaussian scratch

@@ -189,6 +189,8 @@ struct Renderer {
         p.drType = opt.dr_type;
         p.integrator = opt.integrator;
         p.uniformMix = opt.uniform_mixing_prob;
+        p.lensProb = opt.integrator == DRMLT_INTEGRATOR_H2MC ? opt.lens_perturb_prob : 0.0f;
+        p.lensSigma = opt.lens_perturb_stddev;
         p.accMap = opt.acceptance_map;
         p.maxDerv = opt.max_derivative_depth;
         p.gaussDim = std::min(2 * opt.max_depth, kMaxDim);
@@ -236,7 +238,8 @@ struct Renderer {
         p.d.listZ += p.c0;
         p.d.listS += p.c0;
         p.d.listA += p.c0;
-        p.d.counters += 4 * g;
+        p.d.listL += p.c0;
+        p.d.counters += kNumCounters * g;
         p.d.hist += size_t(kPlanBins) * g;
         p.d.order += p.c0;
         p.iterp = dIters + g;
@@ -495,6 +498,7 @@ struct Renderer {
         if ((rc = alloc(&cv.listZ, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listS, size_t(N)))) return rc;
         if ((rc = alloc(&cv.listA, size_t(N)))) return rc;
+        if ((rc = alloc(&cv.listL, size_t(N)))) return rc;
         graphIters = opt.graph_iters > 0 ? std::min(opt.graph_iters, 8) : 1;
         G = opt.chain_groups > 0 ? std::min(opt.chain_groups, 16) : 2;
         G = std::min(G, N);
@@ -519,19 +523,19 @@ struct Renderer {
 
         if ((rc = alloc(&waveCount, size_t(3) * kWaveCountStride * G))) return rc;
         CK(cudaMemset(waveCount, 0, size_t(3) * kWaveCountStride * G * sizeof(int)));
-        if ((rc = alloc(&cv.counters, 4 * size_t(G)))) return rc;
+        if ((rc = alloc(&cv.counters, kNumCounters * size_t(G)))) return rc;
         if ((rc = alloc(&cv.hist, size_t(kPlanBins) * G))) return rc;
         if ((rc = alloc(&dIters, size_t(G)))) return rc;
         if ((rc = alloc(&cv.order, size_t(N)))) return rc;
         if ((rc = alloc(&cv.grad, size_t(N) * kMaxDim))) return rc;
         if ((rc = alloc(&cv.hess, size_t(N) * kMaxDim * kMaxDim))) return rc;
-        if ((rc = alloc(&cv.stats, kNumStats))) return rc;
+        if ((rc = alloc(&cv.stats, kNumStatsAll))) return rc;
         if ((rc = alloc(&cv.film, size_t(W) * H))) return rc;
         if ((rc = alloc(&cv.direct, size_t(W) * H))) return rc;
-        CK(cudaMemset(cv.stats, 0, kNumStats * sizeof(unsigned long long)));
+        CK(cudaMemset(cv.stats, 0, kNumStatsAll * sizeof(unsigned long long)));
         CK(cudaMemset(cv.film, 0, size_t(W) * H * sizeof(float4)));
         CK(cudaMemset(cv.direct, 0, size_t(W) * H * sizeof(float4)));
-        CK(cudaMemset(cv.counters, 0, 4 * size_t(G) * sizeof(int)));
+        CK(cudaMemset(cv.counters, 0, kNumCounters * size_t(G) * sizeof(int)));
         // sample split of delayed.cpp:205-210, including its extra-sample rule
         const long long totalSamples = (long long)opt.spp * W * H;
         samplesPerChain = totalSamples / N;
@@ -684,15 +688,22 @@ struct Renderer {
         const size_t gsm = gauss_smem_bytes(p.gaussDim);
         const bool ystar = p.drType == 0 && p.integrator == 0;
         switch (k) {
-            case 0:
+            case 0: {
                 k_reset_counters<<<1, 128, 0, s>>>(p.d.counters, p.d.hist,
                                                   waveCount + size_t(3) * kWaveCountStride * g,
                                                   p.wave ? 3 * kWaveCountStride : 0);
                 k_plan<<<nb, kStageBlock, 0, s>>>(p);
                 k_scatter<<<std::min((p.N + kScatterBlock - 1) / kScatterBlock, 64), kScatterBlock, 0, s>>>(p);
-                if (p.wave) return 3 + launch_wave<1>(p, g, s);
+                const int nLens = p.lensProb > 0.0f ? 1 : 0;
+                if (p.wave) {
+                    const int n = 3 + launch_wave<1>(p, g, s);
+                    if (nLens) k_lens<<<(p.N + kLensBlock - 1) / kLensBlock, kLensBlock, 0, s>>>(p);
+                    return n + nLens;
+                }
                 k_stage1<<<nbS1, kStageBlock, 0, s>>>(p);
-                return 4;
+                if (nLens) k_lens<<<(p.N + kLensBlock - 1) / kLensBlock, kLensBlock, 0, s>>>(p);
+                return 4 + nLens;
+            }
             case 1: launch_derivs(p, 0, nbWarp, nbAdj, s); return nDerivs;
             case 2:
                 k_gauss<<<nbG, 32 * kGaussTeamWarps, gsm, s>>>(p, 0);
@@ -1095,6 +1106,8 @@ void drmlt_default_options(drmlt_options *o) {
     o->graph_iters = 0;
     o->wavefront = -1;
     o->adjoint_min_dim = 0;
+    o->lens_perturb_prob = 0.3f;
+    o->lens_perturb_stddev = 0.01f;
 }
 
 const char *drmlt_last_error(void) { return g_error.c_str(); }
@@ -1199,7 +1212,7 @@ int drmlt_get_partial_film(void *handle, float *rgb) {
 int drmlt_get_stats(void *handle, drmlt_stats *st) {
     if (!handle || !st) return fail(DRMLT_E_ARG, "null argument");
     Renderer *r = static_cast<Renderer *>(handle);
-    unsigned long long h[kNumStats];
+    unsigned long long h[kNumStatsAll];
     CK(cudaMemcpy(h, r->cv.stats, sizeof(h), cudaMemcpyDeviceToHost));
     st->large_step = h[kStatLarge];
     st->large_step_accepted = h[kStatLargeAcc];
@@ -1212,6 +1225,8 @@ int drmlt_get_stats(void *handle, drmlt_stats *st) {
     st->mutations = h[kStatMutations];
     st->gaussians = h[kStatGauss];
     st->gaussians_fp64_fallback = h[kStatGaussFallback];
+    st->lens = h[kStatLens];
+    st->lens_accepted = h[kStatLensAcc];
     return DRMLT_OK;
 }
 

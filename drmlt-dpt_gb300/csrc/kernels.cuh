@@ -14,6 +14,7 @@
 #pragma once
 #include "chain.cuh"
 #include "derivs.h"
+#include "lens.cuh"
 
 namespace drmlt {
 
@@ -136,8 +137,18 @@ DEV int stage1_begin(const RunParams &p, int i, int iter, Rng &rng, float *off, 
     }
     if (p.integrator == 1 && !(rng.uniform() < p.uniformMix)) {
         // H2MCIntegrator (src/integrators/h2mc.cpp:200-240): H2MCSmallStep::Mutate
-        // (h2mc.cpp:448-606) without its lens branch, as the single stage,
-        // run by the second-stage kernels
+        // (h2mc.cpp:448-606) as the single stage. Its lens branch (taken for a
+        // lens score > 0 with probability lensPerturbProb) draws the coin here
+        // and leaves the score test to k_lens, which sends a chain with a zero
+        // score on to the H2MC step; the H2MC step runs in the second-stage kernels.
+        if (p.lensProb > 0.0f && rng.uniform() < p.lensProb) {
+            flags |= kSecond | kSingle | kLens;
+            if (p.lists) p.d.listL[atomicAdd(&p.d.counters[4], 1)] = i;
+            sc.flags = flags;
+            sc.a1 = 0.0f;
+            sc.a2 = 0.0f;
+            return kTraceNone;
+        }
         flags |= kSecond | kAniso | kSingle;
         acc.c[kStatH2mc]++;
         if (p.lists) {
@@ -415,6 +426,69 @@ static __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
     stage2_end(p, i, st, m.e);
 }
 
+// ------------------------------------------------------------- lens mutation
+// integrator=h2mc's lens branch (H2MCSmallStep::Mutate, h2mc.cpp:466-532) for
+// the chains stage 1 drew for it (listL), one chain per thread, between stage
+// 1 and the derivatives at x: the current state's lens score -- zero sends the
+// chain to the H2MC step instead (its list entries are made here) -- its lens
+// Gaussian, the offset (GenerateSample: two normals of the chain's stage-2
+// stream, which the chain does not otherwise use this iteration), the screen
+// position (x.screen + offset) mod 1, PerturbLensBidir into the second slot,
+// the proposal's lens Gaussian, and the unclamped acceptance
+// exp(log N_z(-o) - log N_x(o)) lens(z) / lens(x) that k_finish clamps and draws.
+constexpr int kLensBlock = 64;
+static __global__ void __launch_bounds__(kLensBlock) k_lens(RunParams p) {
+    const int iter = *p.iterp;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.d.counters[4]) return;
+    const int i = p.d.listL[t];
+    Scratch &sc = p.d.scr[i];
+    const Slot &cur = slot_of(p.d, i, 0);
+    Slot &S = slot_of(p.d, i, 2);
+    Emit e;
+    float lsx;
+    LensAnchor ax;
+    V3 lensPos;
+    // the walk's copy of the path goes to the second slot, which the proposal overwrites
+    const bool okx = lens_walk<false>(p.s, cur.rec, cur.screen[0], cur.screen[1], V3(0.0f, 0.0f, 0.0f), S.rec, e,
+                                      lsx, ax, lensPos);
+    if (!(okx && lsx > 0.0f)) {
+        sc.flags = (sc.flags & ~kLens) | kAniso;
+        atomicAdd(p.d.stats + kStatH2mc, 1ull);
+        p.d.listS[atomicAdd(&p.d.counters[2], 1)] = i;
+        if (!cur.gaussInit) p.d.listX[atomicAdd(&p.d.counters[0], 1)] = i;
+        p.d.listA[atomicAdd(&p.d.counters[3], 1)] = i;
+        return;
+    }
+    atomicAdd(p.d.stats + kStatLens, 1ull);
+    const H2mcParam prm(p.lensSigma);
+    LensGauss gx;
+    lens_gaussian_of(p.s, cur.rec, ax, cur.screen[0], cur.screen[1], lsx, cur.ss, p.maxDerv, prm, gx);
+    Rng rng(p.seed, (unsigned long long)i, (unsigned long long)iter * 4ull + 1ull);
+    const double z0 = double(rng.normal()), z1 = double(rng.normal());
+    const double w0 = z0 / ::sqrt(gx.p[0]), w1 = z1 / ::sqrt(gx.p[1]);
+    float off[2];
+    for (int r = 0; r < 2; r++) off[r] = float(gx.mean[r] + gx.V[r * 2] * w0 + gx.V[r * 2 + 1] * w1);
+    const float sx = mod1(cur.screen[0] + off[0]), sy = mod1(cur.screen[1] + off[1]);
+    float lsz;
+    LensAnchor az;
+    V3 lensPosZ;
+    const bool okz = lens_walk<true>(p.s, cur.rec, sx, sy, lensPos, S.rec, e, lsz, az, lensPosZ);
+    float a2 = 0.0f;
+    S.gaussInit = 0;
+    if (okz) {
+        sc.flags |= kZValid;
+        set_contrib(S, e, p.b);
+        LensGauss gz;
+        lens_gaussian_of(p.s, S.rec, az, e.screen[0], e.screen[1], lsz, e.ss, p.maxDerv, prm, gz);
+        const double px = lens_logpdf(gz, off, -1.0), py = lens_logpdf(gx, off, 1.0);
+        a2 = float(::exp(px - py)) * lsz / lsx;
+    } else {
+        S.hasSplat = 0;
+    }
+    sc.a2 = a2;
+}
+
 // Green's reverse path y* = z + (x - y) and its first-stage acceptance from z
 // (SmallStep::Trace, mutation.cpp:210-238), over the second-stage list only.
 // Prologue: false (aStar = 0 written) when z holds no valid state.
@@ -539,7 +613,10 @@ DEV void finish_chain(const RunParams &p, int i, int iter, StatAcc &acc, Pending
                                       p.sigma1, draw);
             if (draw) accept2 = flip_coin(a2, rng.uniform());
         }
-        if (accept2) acc.c[aniso ? kStatH2mcAcc : kStatIsoAcc]++;
+        if (accept2) {
+            if (flags & kLens) atomicAdd(p.d.stats + kStatLensAcc, 1ull);
+            else acc.c[aniso ? kStatH2mcAcc : kStatIsoAcc]++;
+        }
     }
     // weighted splats (delayed.cpp:547-561)
     const float w1 = a1;
@@ -600,7 +677,7 @@ static __global__ void k_set_iters(int *iters, int n, int value) {
 // A chain group's list counters, work-class histogram and (nWave > 0) the
 // queue counters of its wavefront stage passes, at the start of an iteration.
 static __global__ void k_reset_counters(int *counters, int *hist, int *waveCount, int nWave) {
-    if (threadIdx.x < 4) counters[threadIdx.x] = 0;
+    if (threadIdx.x < kNumCounters) counters[threadIdx.x] = 0;
     for (int k = threadIdx.x; k < kPlanBins; k += blockDim.x) hist[k] = 0;
     for (int k = threadIdx.x; k < nWave; k += blockDim.x) waveCount[k] = 0;
 }

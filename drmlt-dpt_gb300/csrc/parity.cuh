@@ -41,6 +41,71 @@ __global__ void k_perturb_paths(SceneView s, const PathRec *in, const float *off
     ct[i] = c;
 }
 
+__global__ void k_lens_eval(SceneView s, const PathRec *paths, const float *screen, const float *ss, int n,
+                            float sigma, int maxDerv, float *score, float *pos, float *logf, float *grad, float *hess,
+                            double *gauss) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PathRec tmp;
+    Emit e;
+    LensAnchor a;
+    V3 lp;
+    float ls = 0.0f;
+    const PathRec &r = paths[i];
+    const float sx = screen[2 * i], sy = screen[2 * i + 1];
+    if (!lens_walk<false>(s, r, sx, sy, V3(0.0f, 0.0f, 0.0f), tmp, e, ls, a, lp)) ls = 0.0f;
+    score[i] = ls;
+    pos[3 * i] = lp.x;
+    pos[3 * i + 1] = lp.y;
+    pos[3 * i + 2] = lp.z;
+    float g[2] = {0.0f, 0.0f}, h[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    float f = 0.0f;
+    const bool have = lens_func_exists(r.c, r.l, maxDerv);
+    if (have && ls > 1e-15f) {
+        lens_derivs(s, a, sx, sy, ls, g, h);
+        f = lens_logf<float>(s, a, sx, sy);
+    }
+    logf[i] = f;
+    for (int k = 0; k < 2; k++) grad[2 * i + k] = g[k];
+    for (int k = 0; k < 4; k++) hess[4 * i + k] = h[k];
+    LensGauss G;
+    const H2mcParam prm(sigma);
+    if (have) lens_gaussian(prm, ss[i], g, h, G); else lens_gauss_isotropic(double(prm.sigma), G);
+    double *o = gauss + 7 * size_t(i);
+    o[0] = G.mean[0];
+    o[1] = G.mean[1];
+    for (int r2 = 0; r2 < 2; r2++)
+        for (int c2 = 0; c2 < 2; c2++)
+            o[2 + r2 * 2 + c2] = G.V[r2 * 2] * G.p[0] * G.V[c2 * 2] + G.V[r2 * 2 + 1] * G.p[1] * G.V[c2 * 2 + 1];
+    o[6] = G.logDet;
+}
+
+__global__ void k_lens_perturb(SceneView s, const PathRec *in, const float *screen, const float *lensPos, int n,
+                               PathRec *out, drmlt_contrib *ct, float *score) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Emit e;
+    LensAnchor a;
+    V3 lp;
+    float ls = 0.0f;
+    const V3 pos(lensPos[3 * i], lensPos[3 * i + 1], lensPos[3 * i + 2]);
+    const bool ok = lens_walk<true>(s, in[i], screen[2 * i], screen[2 * i + 1], pos, out[i], e, ls, a, lp);
+    drmlt_contrib c;
+    std::memset(&c, 0, sizeof(c));
+    if (ok) {
+        c.screen[0] = e.screen[0];
+        c.screen[1] = e.screen[1];
+        c.rgb[0] = e.rgb.x;
+        c.rgb[1] = e.rgb.y;
+        c.rgb[2] = e.rgb.z;
+        c.ls = e.ls;
+        c.ss = e.ss;
+        c.valid = 1;
+    }
+    ct[i] = c;
+    score[i] = ok ? ls : 0.0f;
+}
+
 struct SinkList {
     int *tech;
     drmlt_contrib *ct;
@@ -279,6 +344,55 @@ int drmlt_perturb(void *handle, const drmlt_path *in, const float *offset, int n
     CK(cudaDeviceSynchronize());
     if ((rc = dout.get(reinterpret_cast<PathRec *>(out), n))) return rc;
     return dc.get(contrib, n);
+}
+
+int drmlt_lens_eval(void *handle, const drmlt_path *paths, const float *screen, const float *ss, int n,
+                    float lens_sigma, int max_derivative_depth, float *lens_score, float *lens_pos, float *logf,
+                    float *grad, float *hess, double *gauss) {
+    if (!handle || n < 0 ||
+        (n && (!paths || !screen || !ss || !lens_score || !lens_pos || !logf || !grad || !hess || !gauss)))
+        return fail(DRMLT_E_ARG, "bad argument");
+    if (!(lens_sigma > 0.0f)) return fail(DRMLT_E_ARG, "lens_sigma must be positive");
+    if (n == 0) return DRMLT_OK;
+    int rc = check_paths(paths, n);
+    if (rc) return rc;
+    Renderer *r = static_cast<Renderer *>(handle);
+    DevBuf<PathRec> dp;
+    DevBuf<float> dsc, dss, dls, dpos, dlf, dg, dh;
+    DevBuf<double> dga;
+    if ((rc = dp.put(reinterpret_cast<const PathRec *>(paths), n)) || (rc = dsc.put(screen, size_t(n) * 2)) ||
+        (rc = dss.put(ss, n)) || (rc = dls.alloc(n)) || (rc = dpos.alloc(size_t(n) * 3)) || (rc = dlf.alloc(n)) ||
+        (rc = dg.alloc(size_t(n) * 2)) || (rc = dh.alloc(size_t(n) * 4)) || (rc = dga.alloc(size_t(n) * 7)))
+        return rc;
+    k_lens_eval<<<(n + 63) / 64, 64>>>(r->sv, dp.p, dsc.p, dss.p, n, lens_sigma, max_derivative_depth, dls.p, dpos.p,
+                                       dlf.p, dg.p, dh.p, dga.p);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if ((rc = dls.get(lens_score, n)) || (rc = dpos.get(lens_pos, size_t(n) * 3)) || (rc = dlf.get(logf, n)) ||
+        (rc = dg.get(grad, size_t(n) * 2)) || (rc = dh.get(hess, size_t(n) * 4)))
+        return rc;
+    return dga.get(gauss, size_t(n) * 7);
+}
+
+int drmlt_lens_perturb(void *handle, const drmlt_path *in, const float *screen_new, const float *lens_pos, int n,
+                       drmlt_path *out, drmlt_contrib *contrib, float *lens_score) {
+    if (!handle || n < 0 || (n && (!in || !screen_new || !lens_pos || !out || !contrib || !lens_score)))
+        return fail(DRMLT_E_ARG, "bad argument");
+    if (n == 0) return DRMLT_OK;
+    int rc = check_paths(in, n);
+    if (rc) return rc;
+    Renderer *r = static_cast<Renderer *>(handle);
+    DevBuf<PathRec> di, dout;
+    DevBuf<float> dsc, dlp, dls;
+    DevBuf<drmlt_contrib> dc;
+    if ((rc = di.put(reinterpret_cast<const PathRec *>(in), n)) || (rc = dsc.put(screen_new, size_t(n) * 2)) ||
+        (rc = dlp.put(lens_pos, size_t(n) * 3)) || (rc = dout.alloc(n)) || (rc = dc.alloc(n)) || (rc = dls.alloc(n)))
+        return rc;
+    k_lens_perturb<<<(n + 63) / 64, 64>>>(r->sv, di.p, dsc.p, dlp.p, n, dout.p, dc.p, dls.p);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if ((rc = dout.get(reinterpret_cast<PathRec *>(out), n)) || (rc = dc.get(contrib, n))) return rc;
+    return dls.get(lens_score, n);
 }
 
 int drmlt_replay(void *handle, int mode, const float *tapes, const int32_t *tape_len, int stride, int n,

@@ -10,7 +10,8 @@
 // second-component-first, because the reference's compiler evaluates those
 // constructor arguments right to left; a replayed stream then reproduces the
 // reference's paths. Lens-mutation quantities (lensContrib / lensScore) are not
-// computed: the DR integrator never reads them.
+// tracked here: the DR integrator never reads them; integrator=h2mc's lens
+// mutation takes them by a walk of its own (lens.cuh).
 #pragma once
 #include "bsdf_light.cuh"
 
@@ -25,12 +26,18 @@ struct PathRec {
     int c, l;
     int lgtLight, lgtPrim;
     int dlLight, dlPrim;
-    unsigned useAbs;
+    unsigned useAbs;  // bit v: vertex v's useAbsoluteParam; bit 31: kLensFormBit (lens.cuh)
     float u[kMaxDim];
     int tri[kMaxVerts];
     float disc[kMaxVerts];
     float rr[kMaxVerts];
 };
+
+// PathRec::useAbs bit 31, above the per-vertex bits: the path was made by
+// integrator=h2mc's lens mutation (PerturbLensBidir), whose lens score of a
+// light path connected to the camera carries a shading-normal factor of its
+// own (lens.cuh). The other samplers clear it.
+constexpr unsigned kLensFormBit = 1u << 31;
 
 struct Contrib {
     float screen[2];
@@ -852,6 +859,7 @@ DEV_SHARED int perturb_step(const SceneView &s, const PathRec &in, const float *
         switch (m.pc) {
             case kPStart: {
                 out = in;
+                out.useAbs &= ~kLensFormBit;
                 m.k = 0;
                 zero_state(m.lp);
                 m.lastLgtTri = -1;

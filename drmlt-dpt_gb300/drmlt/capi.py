@@ -64,14 +64,15 @@ class Options(C.Structure):
                 ("smem_carveout", C.c_int32), ("autotune", C.c_int32), ("stage2_lanes", C.c_int32),
                 ("graph_iters", C.c_int32), ("wavefront", C.c_int32), ("head_chains", C.c_int32),
                 ("head_lanes", C.c_int32), ("persistent", C.c_int32),
-                ("team_sms", C.c_int32), ("wait_limit", C.c_int32), ("adjoint_min_dim", C.c_int32)]
+                ("team_sms", C.c_int32), ("wait_limit", C.c_int32), ("adjoint_min_dim", C.c_int32),
+                ("lens_perturb_prob", C.c_float), ("lens_perturb_stddev", C.c_float)]
 
 
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "large_step", "large_step_accepted", "stage1", "stage1_accepted", "stage2_iso",
         "stage2_iso_accepted", "stage2_h2mc", "stage2_h2mc_accepted", "mutations", "gaussians",
-        "gaussians_fp64_fallback")]
+        "gaussians_fp64_fallback", "lens", "lens_accepted")]
 
 
 class Path(C.Structure):
@@ -130,6 +131,10 @@ _SIGS = {
     "drmlt_path_grad_hess": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "drmlt_path_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "drmlt_perturb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "drmlt_lens_eval": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_int,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "drmlt_lens_perturb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]),
     "drmlt_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "drmlt_dr_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -10,7 +10,6 @@ from __future__ import annotations
 
 import os
 import time
-import warnings
 
 import ctypes as C
 
@@ -31,10 +30,9 @@ def make_options(sd: SceneData, *, seed: int = 0x1234ABCD, device: int = 0,
         raise ValueError("Unknown integrator %r" % d.integrator)
     o.integrator = _INTEGRATORS[d.integrator]
     # mcmc's SmallStep never proposes a lens mutation (mutation.cpp:126-166); only
-    # H2MCSmallStep does (h2mc.cpp:466-532)
-    if d.integrator == "h2mc" and d.lensPerturbProb > 0:
-        warnings.warn("the lens mutation of integrator=h2mc (h2mc.cpp:466-532) is not implemented; "
-                      "lensperturbprob=%g is treated as 0" % d.lensPerturbProb)
+    # H2MCSmallStep does (h2mc.cpp:466-532): the options are read for integrator=h2mc
+    o.lens_perturb_prob = d.lensPerturbProb
+    o.lens_perturb_stddev = d.lensPerturbStdDev
     o.dr_type = capi.DR_MIRA if d.type == "mira" else capi.DR_GREEN
     o.aniso_perturb_prob = d.anisoPerturbProb
     o.aniso_perturb_stddev = d.anisoperturbstddev
@@ -227,6 +225,43 @@ class Renderer:
                                              capi.ptr(ct)))
         return out, ct
 
+    def lens_eval(self, paths: np.ndarray, screen: np.ndarray, ss: np.ndarray, lens_sigma: float = 0.01,
+                  max_derivative_depth: int = 9):
+        """integrator=h2mc's lens quantities of each path (drmlt_lens_eval): lens
+        score, lens vertex position, lens-mode log f, its gradient and Hessian
+        w.r.t. the screen position, and the 2-D Gaussian (mean, inverse
+        covariance, log det)."""
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        screen = np.ascontiguousarray(screen, np.float32).reshape(n, 2)
+        ss = np.ascontiguousarray(ss, np.float32).reshape(n)
+        score = np.zeros(n, np.float32)
+        pos = np.zeros((n, 3), np.float32)
+        logf = np.zeros(n, np.float32)
+        g = np.zeros((n, 2), np.float32)
+        h = np.zeros((n, 4), np.float32)
+        gauss = np.zeros((n, 7), np.float64)
+        capi.check(capi.lib().drmlt_lens_eval(self.handle, capi.ptr(paths), capi.ptr(screen), capi.ptr(ss), n,
+                                               float(lens_sigma), int(max_derivative_depth), capi.ptr(score),
+                                               capi.ptr(pos), capi.ptr(logf), capi.ptr(g), capi.ptr(h),
+                                               capi.ptr(gauss)))
+        return dict(score=score, pos=pos, logf=logf, grad=g, hess=h, mean=gauss[:, :2], inv_cov=gauss[:, 2:6],
+                    log_det=gauss[:, 6])
+
+    def lens_perturb(self, paths: np.ndarray, screen_new: np.ndarray, lens_pos: np.ndarray):
+        """PerturbLensBidir of each path (drmlt_lens_perturb): perturbed paths,
+        contributions and lens scores."""
+        paths = np.ascontiguousarray(paths, capi.PATH_DTYPE)
+        n = len(paths)
+        scr = np.ascontiguousarray(screen_new, np.float32).reshape(n, 2)
+        lp = np.ascontiguousarray(lens_pos, np.float32).reshape(n, 3)
+        out = np.zeros(n, capi.PATH_DTYPE)
+        ct = np.zeros(n, capi.CONTRIB_DTYPE)
+        score = np.zeros(n, np.float32)
+        capi.check(capi.lib().drmlt_lens_perturb(self.handle, capi.ptr(paths), capi.ptr(scr), capi.ptr(lp), n,
+                                                  capi.ptr(out), capi.ptr(ct), capi.ptr(score)))
+        return out, ct, score
+
     def replay(self, mode: int, tapes: list, cam_len=None, lgt_len=None, max_contribs: int = 64):
         n = len(tapes)
         stride = max(1, max(len(t) for t in tapes))
@@ -389,7 +424,7 @@ class DRIntegrator(Integrator):
 
 
 class H2MCIntegrator(Integrator):
-    """H2MC (src/integrators/h2mc.cpp) without its lens mutation."""
+    """H2MC (src/integrators/h2mc.cpp), with its lens mutation."""
 
 
 class MCMCIntegrator(Integrator):

@@ -82,12 +82,14 @@ void dump(const drmlt_dropin::GpuDRIntegrator &gi, const std::string &path) {
                  "\"large_step_prob\":%.9g,\"roughness_threshold\":%.9g,\"discrete_stddev\":%.9g,"
                  "\"uniform_mixing_prob\":%.9g,\"num_chains\":%d,\"num_init_samples\":%d,\"spp\":%d,"
                  "\"direct_spp\":%d,\"min_depth\":%d,\"max_depth\":%d,\"seed_offset\":%d,"
-                 "\"use_light_coordinate_sampling\":%d,\"max_derivative_depth\":%d}}\n",
+                 "\"use_light_coordinate_sampling\":%d,\"max_derivative_depth\":%d,"
+                 "\"lens_perturb_prob\":%.9g,\"lens_perturb_stddev\":%.9g}}\n",
                  o.integrator, o.dr_type, double(o.aniso_perturb_prob), double(o.aniso_perturb_stddev),
                  o.acceptance_map, double(o.perturb_stddev), double(o.large_step_prob),
                  double(o.roughness_threshold), double(o.discrete_stddev), double(o.uniform_mixing_prob),
                  o.num_chains, o.num_init_samples, o.spp, o.direct_spp, o.min_depth, o.max_depth, o.seed_offset,
-                 o.use_light_coordinate_sampling, o.max_derivative_depth);
+                 o.use_light_coordinate_sampling, o.max_derivative_depth, double(o.lens_perturb_prob),
+                 double(o.lens_perturb_stddev));
     std::fclose(f);
 }
 

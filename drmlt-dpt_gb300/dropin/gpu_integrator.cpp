@@ -172,9 +172,6 @@ drmlt_options BuildOptions(const DptOptions &o, int maxDervDepth, uint64_t seed)
     else if (o.integrator == "h2mc") r.integrator = DRMLT_INTEGRATOR_H2MC;
     else if (o.integrator == "mcmc") r.integrator = DRMLT_INTEGRATOR_MCMC;
     else throw std::runtime_error("GPU integrator: unknown integrator " + o.integrator);
-    if (o.integrator == "h2mc" && o.lensPerturbProb > Float(0.0))
-        std::cerr << "GPU integrator: the lens mutation of integrator=h2mc is not implemented; lensperturbprob="
-                  << o.lensPerturbProb << " is treated as 0" << std::endl;
     // an unknown DR type is green (delayed.cpp:352-362)
     r.dr_type = o.type == "mira" ? DRMLT_DR_MIRA : DRMLT_DR_GREEN;
     r.aniso_perturb_prob = float(o.anisoPerturbProb);
@@ -193,6 +190,8 @@ drmlt_options BuildOptions(const DptOptions &o, int maxDervDepth, uint64_t seed)
     r.max_depth = o.maxDepth;
     r.seed_offset = o.seedOffset;
     r.use_light_coordinate_sampling = o.useLightCoordinateSampling ? 1 : 0;
+    r.lens_perturb_prob = float(o.lensPerturbProb);
+    r.lens_perturb_stddev = float(o.lensPerturbStdDev);
     r.max_derivative_depth = maxDervDepth;
     r.seed = seed + uint64_t(int64_t(o.seedOffset));
     return r;

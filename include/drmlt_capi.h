@@ -167,12 +167,18 @@ typedef struct drmlt_options {
                                      switch of method mid-render would change later accept
                                      decisions). The persistent schedule takes hyper-dual
                                      derivatives for every path. */
+    float lens_perturb_prob;      /* lensperturbprob: integrator=h2mc's lens mutation (default 0.3) */
+    float lens_perturb_stddev;    /* lensperturbstddev: its isotropic sigma (default 0.01). The
+                                     reference's parser also writes the XML anisoperturbstddev
+                                     here (src/parsescene.cpp:553-554); a front end that mirrors
+                                     it passes that value. */
 } drmlt_options;
 
 /* DR statistics counters (delayed.cpp:287-329, raw, unswapped labels), plus
  * two counters of this implementation: anisotropic Gaussians computed, and how
  * many of them needed the FP64 Jacobi fallback (eigenvalue clusters the
- * FP32-then-refined eigensolver could not certify). */
+ * FP32-then-refined eigensolver could not certify); for integrator=h2mc the
+ * lens mutations and their acceptances (h2mc.cpp:139-149, lensStep). */
 typedef struct drmlt_stats {
     uint64_t large_step, large_step_accepted;
     uint64_t stage1, stage1_accepted;
@@ -180,6 +186,7 @@ typedef struct drmlt_stats {
     uint64_t stage2_h2mc, stage2_h2mc_accepted;
     uint64_t mutations;
     uint64_t gaussians, gaussians_fp64_fallback;
+    uint64_t lens, lens_accepted;
 } drmlt_stats;
 
 /* A technique path (one Markov state): SubpathContrib camDepth c / lightDepth l,
@@ -316,6 +323,33 @@ int drmlt_path_adjoint(void *handle, const drmlt_path *paths, const float *u, in
  * offsets (DRMLT_MAX_DIM stride) -> perturbed paths and contributions. */
 int drmlt_perturb(void *handle, const drmlt_path *in, const float *offset, int n, drmlt_path *out,
                   drmlt_contrib *contrib);
+
+/* integrator=h2mc's lens mutation, per path (H2MCSmallStep::Mutate's lens
+ * branch, src/integrators/h2mc.cpp:466-532).
+ * drmlt_lens_eval: for technique paths with their contributions' screen
+ * positions (screen, 2 per path) and ss scores, the lens score
+ * (SubpathContrib::lensScore, as the sampler that made the path computes it),
+ * the lens vertex position (Path::lensVertexPos, 3 per path), and the lens-mode
+ * path function (RegisterPathFuncBidir with PathFuncMode::Lens,
+ * src/path.cpp:2987-3175): log f (logf), its gradient (grad, 2) and Hessian
+ * (hess, 2 x 2 row-major) w.r.t. the screen position -- zeros where the lens
+ * score is <= 1e-15 or the reference has no lens function for the technique
+ * (c + l <= 3 or c + l - 1 > max_derivative_depth), logf 0 there -- and the
+ * 2-D Gaussian ComputeGaussian (h2mc.cpp:607-640) builds from them with
+ * sigma lens_sigma: gauss = mean[2], inv_cov[4], log_det (7 doubles per path).
+ * It replaces the lens-function lookup of the chad library
+ * (lensFuncMap / lensDervFuncMap, src/path.h:158-159). */
+int drmlt_lens_eval(void *handle, const drmlt_path *paths, const float *screen, const float *ss, int n,
+                    float lens_sigma, int max_derivative_depth, float *lens_score, float *lens_pos, float *logf,
+                    float *grad, float *hess, double *gauss);
+
+/* PerturbLensBidir (src/path.cpp:1913-2078): each path moved to screen
+ * position screen_new (2 per path) with its first camera vertex aimed at
+ * lens_pos (3 per path) -> the perturbed path, its contribution and its lens
+ * score. The output paths carry bit 31 of use_abs (made by the lens
+ * mutation: a later lens score of the path takes that sampler's form). */
+int drmlt_lens_perturb(void *handle, const drmlt_path *in, const float *screen_new, const float *lens_pos, int n,
+                       drmlt_path *out, drmlt_contrib *contrib, float *lens_score);
 
 /* Replays recorded uniform streams through GeneratePathBidir (mode 0,
  * src/path.cpp:978-1121), GenerateSubpath (mode 1, camLength/lgtLength per

@@ -9,6 +9,7 @@
 //   GetPathPos / Serialize src/path.cpp:2303-2439
 //   chad static path function + derivative (generated pathlibbidir.so)
 //   PH2MCSmallStep::ComputeGaussian src/integrators/delayed/drsmallstep.cpp:219-266
+//   PerturbLensBidir + chad lens-mode functions, ComputeGaussian (h2mc.cpp:607-640)
 // and writes JSON lines. Every random number a sampler consumed is recorded
 // (the reference draws them with std::uniform_real_distribution from a
 // pcg32_k64_fast stream), so a replay of the same stream must reproduce the
@@ -16,7 +17,7 @@
 // the continuous offsets move the path.
 //
 // usage: ref_harness <scene.xml> <libdir> <maxDervDepth> <out.jsonl> <mode> <seed0> <count> [extra]
-//   mode = camera | bidir | subpath | direct | tech | accept | mesh
+//   mode = camera | bidir | subpath | direct | tech | accept | lens | mesh
 //   (mesh: every shape's triangles as loaded by ParseObj / LoadSerialized,
 //    src/parseobj.cpp:148-264, src/loadserialized.cpp:236-317)
 #include "parsescene.h"
@@ -28,6 +29,7 @@
 #include "camera.h"
 #include "gaussian.h"
 #include "integrators/delayed/drsmallstep.h"
+#include "integrators/h2mc.h"
 #include "mutation.h"
 #include "distribution.h"
 #include "texturesystem.h"
@@ -123,6 +125,8 @@ void DumpContribs(const std::vector<SubpathContrib> &cs) {
         F(c.ssScore);
         fprintf(g_out, ",\"mis\":");
         F(c.misWeight);
+        fprintf(g_out, ",\"lens\":");
+        F(c.lensScore);
         fputc('}', g_out);
     }
     fputc(']', g_out);
@@ -332,6 +336,133 @@ void ModeTech(uint64_t seed0, int count, int nPerturb, const PathFuncLib &lib, i
                 Arr(GetPathPos(y), dim);
                 fprintf(g_out, ",\"path\":");
                 DumpPath(y);
+                fprintf(g_out, ",\"contribs\":");
+                DumpContribs(ycs);
+                fputc('}', g_out);
+            }
+            fprintf(g_out, "]}\n");
+            written++;
+        }
+    }
+}
+
+// The lens mutation of H2MCSmallStep::Mutate (src/integrators/h2mc.cpp:466-532)
+// on technique paths x (bootstrap samples, as in ModeTech): x's lens score
+// (SubpathContrib::lensScore from the sampler), its lens vertex position, the
+// chad lens-mode log f and its gradient / Hessian with respect to the screen
+// position (lensFuncMap / lensDervFuncMap, called as initLensGaussian calls
+// them), the 2-D Gaussian the integrator's ComputeGaussian (h2mc.cpp:607-640)
+// builds from them with lensPerturbStdDev, and PerturbLensBidir
+// (src/path.cpp:1913-2078) at screen positions x.screen + offset (mod 1).
+// Techniques with a zero lens score are kept one in four (no perturbation).
+void ModeLens(uint64_t seed0, int count, int nPerturb, const PathFuncLib &lib, int maxDervDepth) {
+    const int maxDepth = g_scene->options->maxDepth;
+    const int minDepth = std::max(g_scene->options->minDepth, 3);
+    AlignedStdVector sceneParams(GetSceneSerializedSize());
+    Serialize(g_scene, &sceneParams[0]);
+    SerializedSubpath ssub;
+    ssub.primary.resize(GetPrimaryParamSize(maxDervDepth, maxDervDepth));
+    ssub.vertParams.resize(GetVertParamSize(maxDervDepth, maxDervDepth));
+    const H2MCIntegrator::H2MCParam lensParam(g_scene->options->lensPerturbStdDev);
+    const Float sigmas[3] = {lensParam.sigma, Float(0.003), Float(0.03)};
+    int written = 0, zeros = 0;
+    for (int s = 0; written < count && s < 100 * count; s++) {
+        RNG rng(seed0 + s);
+        Path full;
+        std::vector<SubpathContrib> contribs;
+        GeneratePathBidir(g_scene, Vector2i(-1, -1), minDepth, maxDepth, full, contribs, rng);
+        for (const SubpathContrib &c : contribs) {
+            if (written >= count) break;
+            if (!(c.lensScore > Float(0.0)) && (zeros++ % 4) != 0) continue;
+            Path path = full;
+            path.Initialize(c.camDepth, c.lightDepth);
+            const int dim = GetDimension(path);
+            fprintf(g_out, "{\"mode\":\"lens\",\"seed\":%llu,\"dim\":%d,\"path\":", (unsigned long long)(seed0 + s),
+                    dim);
+            DumpPath(path);
+            fprintf(g_out, ",\"contrib\":");
+            DumpContribs({c});
+            fprintf(g_out, ",\"pos\":");
+            Arr(GetPathPos(path), dim);
+            fprintf(g_out, ",\"lensPos\":");
+            Arr(path.lensVertexPos, 3);
+            AlignedStdVector grad(2, Float(0.0)), hess(4, Float(0.0));
+            auto dit = lib.lensDervFuncMap.find({c.camDepth, c.lightDepth});
+            auto fit = lib.lensFuncMap.find({c.camDepth, c.lightDepth});
+            const bool haveDerv = dit != lib.lensDervFuncMap.end();
+            Float logf = Float(0.0);
+            bool scrubbed = false;
+            if (haveDerv && c.lensScore > Float(1e-15)) {
+                Serialize(g_scene, path, ssub);
+                dit->second(&c.screenPos[0], &ssub.primary[0], &sceneParams[0], &ssub.vertParams[0], &grad[0],
+                            &hess[0]);
+                if (fit != lib.lensFuncMap.end())
+                    fit->second(&c.screenPos[0], &ssub.primary[0], &sceneParams[0], &ssub.vertParams[0], &logf);
+                if (!IsFinite(grad) || !IsFinite(hess)) {
+                    scrubbed = true;
+                    std::fill(grad.begin(), grad.end(), Float(0.0));
+                    std::fill(hess.begin(), hess.end(), Float(0.0));
+                }
+            }
+            // Central differences of chad's lens gradient (h = 1e-4 in the screen
+            // position): a consistency check of chad's own lens Hessian.
+            std::vector<double> fdH(4, 0.0);
+            if (haveDerv && c.lensScore > Float(1e-15)) {
+                AlignedStdVector g2(2), h2(4);
+                for (int j = 0; j < 2; j++) {
+                    for (int sgn = -1; sgn <= 1; sgn += 2) {
+                        Vector2 sp = c.screenPos;
+                        sp[j] += Float(sgn) * Float(1e-4);
+                        dit->second(&sp[0], &ssub.primary[0], &sceneParams[0], &ssub.vertParams[0], &g2[0], &h2[0]);
+                        for (int i = 0; i < 2; i++) fdH[i * 2 + j] += double(sgn) * double(g2[i]) / 2e-4;
+                    }
+                }
+            }
+            fprintf(g_out, ",\"haveDerv\":%d,\"scrubbed\":%d,\"logf\":", int(haveDerv), int(scrubbed));
+            F(logf);
+            fprintf(g_out, ",\"grad\":");
+            Arr(grad, 2);
+            fprintf(g_out, ",\"hess\":");
+            Arr(hess, 4);
+            fprintf(g_out, ",\"fdHess\":");
+            Arr(fdH, 4);
+            Gaussian g;
+            if (haveDerv) {
+                ComputeGaussian(lensParam, c.ssScore, grad, hess, g);
+            } else {
+                IsotropicGaussian(2, lensParam.sigma, g);
+            }
+            fprintf(g_out, ",\"gauss\":{\"mean\":");
+            Arr(g.mean, 2);
+            fprintf(g_out, ",\"invCov\":");
+            Arr(g.invCov.data(), 4);
+            fprintf(g_out, ",\"logDet\":");
+            F(g.logDet);
+            fprintf(g_out, "},\"perturb\":[");
+            for (int p = 0; c.lensScore > Float(0.0) && p < nPerturb; p++) {
+                RNG prng(9191u * (seed0 + s) + 37u * written + p);
+                std::normal_distribution<Float> nd(Float(0.0), sigmas[p % 3]);
+                Vector offset(2);
+                offset[0] = nd(prng);
+                offset[1] = nd(prng);
+                Vector2 screen(Modulo(c.screenPos[0] + offset[0], Float(1.0)),
+                               Modulo(c.screenPos[1] + offset[1], Float(1.0)));
+                Path y = path;
+                std::vector<SubpathContrib> ycs;
+                PerturbLensBidir(g_scene, screen, y, ycs);
+                if (p) fputc(',', g_out);
+                fprintf(g_out, "{\"offset\":");
+                Arr(offset, 2);
+                fprintf(g_out, ",\"screen\":");
+                Arr(screen, 2);
+                fprintf(g_out, ",\"logpdf\":");
+                F(GaussianLogPdf(offset, g));
+                fprintf(g_out, ",\"ypos\":");
+                Arr(GetPathPos(y), dim);
+                fprintf(g_out, ",\"path\":");
+                DumpPath(y);
+                fprintf(g_out, ",\"lensPos\":");
+                Arr(y.lensVertexPos, 3);
                 fprintf(g_out, ",\"contribs\":");
                 DumpContribs(ycs);
                 fputc('}', g_out);
@@ -610,6 +741,10 @@ int main(int argc, char **argv) {
         if (chdir(libdir.c_str()) != 0) return 3;
         std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);
         ModeTech(seed0, count, extra, *lib, maxDervDepth);
+    } else if (mode == "lens") {
+        if (chdir(libdir.c_str()) != 0) return 3;
+        std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);
+        ModeLens(seed0, count, extra, *lib, maxDervDepth);
     } else if (mode == "accept") {
         if (chdir(libdir.c_str()) != 0) return 3;
         std::shared_ptr<const PathFuncLib> lib = BuildPathFuncLibrary(true, maxDervDepth, true);

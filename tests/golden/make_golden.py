@@ -15,6 +15,10 @@ synthetic Cornell-box scenes of drmlt/scenegen.py and writes gzipped JSON lines:
                           on a recorded stream, SmallStep::Mutate (both sigmas),
                           PH2MCSmallStep::Mutate, SmallStep::Trace (Green's y*), with
                           their offsets, and Green / Mira second-stage acceptances
+  <cfg>_lens.jsonl.gz     the lens mutation of integrator=h2mc on technique paths:
+                          lens scores, chad lens-mode log f / gradient / Hessian
+                          w.r.t. the screen position, the 2-D Gaussian and
+                          PerturbLensBidir results
   cfg3d_tech.jsonl.gz     technique paths of config 3 at max depth 10 with the FP64
                           chad library's log f, gradient and Hessian
   <cfg>_render*.json.gz   a full `dpt -d` render of the scene (the reference's
@@ -27,6 +31,8 @@ usage (in a container that has the reference at /root/reference):
   python tests/golden/make_golden.py [--render] [cfg1] [cfg2]   (--render: only the renders)
   python tests/golden/make_golden.py --mesh                     (only cfgM_mesh)
   python tests/golden/make_golden.py --accept [cfg1] ...        (only the acceptance fixtures)
+  python tests/golden/make_golden.py --lens [cfg1] ...          (only the lens-mutation fixtures)
+  python tests/golden/make_golden.py --render-only cfg1 render_h2mc_lens   (named renders only)
   python tests/golden/make_golden.py --double                    (cfg3d_tech: FP64 chad, depth 10)
 """
 from __future__ import annotations
@@ -60,10 +66,11 @@ CONFIGS = {
 }
 
 # full renders: (output suffix, scene writer with the render's spp, derivative depth)
-NO_LENS = {"lensperturbprob": "0"}  # the lens mutation of h2mc / mcmc is not part of this build
+NO_LENS = {"lensperturbprob": "0"}  # h2mc / mcmc without the lens mutation (render_h2mc_lens has it)
 RENDERS = {
     "cfg1": [("render", lambda d: scenegen.config1(d, spp=16), 5),
              ("render_h2mc", lambda d: scenegen.config1(d, spp=16, integrator="h2mc", extra=NO_LENS), 5),
+             ("render_h2mc_lens", lambda d: scenegen.config1(d, spp=16, integrator="h2mc"), 5),
              ("render_mcmc", lambda d: scenegen.config1(d, spp=16, integrator="mcmc", extra=NO_LENS), 5),
              ("render_accmap", lambda d: scenegen.config1(d, spp=16, acceptance_map=True), 5)],
     "cfg3": [("render", lambda d: scenegen.config3(d, spp=16), 5)],
@@ -97,10 +104,12 @@ def _stats(log: str) -> dict:
     return dict(large=vals[0], small=vals[1], lens=vals[2])
 
 
-def render(cfg: str, blocks: int = 16):
+def render(cfg: str, blocks: int = 16, only=None):
     import numpy as np
     subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
     for name, writer, depth in RENDERS[cfg]:
+        if only and name not in only:
+            continue
         tmp = tempfile.mkdtemp()
         try:
             xml = writer(os.path.join(tmp, "scene"))
@@ -168,6 +177,33 @@ def accept(cfg: str):
         shutil.rmtree(tmp)
 
 
+LENS_COUNT = 120
+LENS_PERTURB = 4
+
+
+def lens(cfg: str):
+    """<cfg>_lens.jsonl.gz: the lens mutation of integrator=h2mc on technique
+    paths -- lens scores, chad lens-mode derivatives, the 2-D Gaussian and
+    PerturbLensBidir results (ref_harness mode lens)."""
+    writer, depth, _ = CONFIGS[cfg]
+    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle", "ref"), "-j8"], stdout=subprocess.DEVNULL)
+    libdir = os.path.join(REF_DIR, "lib_d%d" % depth)
+    os.makedirs(libdir, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    try:
+        xml = writer(os.path.join(tmp, "scene"))
+        out = os.path.join(tmp, "lens.jsonl")
+        subprocess.check_call([HARNESS, xml, libdir, str(depth), out, "lens", "21", str(LENS_COUNT), str(LENS_PERTURB)],
+                              stdout=subprocess.DEVNULL)
+        dst = os.path.join(HERE, "%s_lens.jsonl.gz" % cfg)
+        with open(out, "rb") as f, open(dst, "wb") as raw:
+            with gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as g:
+                shutil.copyfileobj(f, g)
+        print(dst, os.path.getsize(dst))
+    finally:
+        shutil.rmtree(tmp)
+
+
 DEEP_COUNT = 240
 
 
@@ -220,9 +256,17 @@ if __name__ == "__main__":
     if "--double" in args:
         double_tech()
         sys.exit(0)
+    if "--lens" in args:
+        for c in [a for a in args if not a.startswith("--")] or ["cfg1", "cfg3", "cfgL", "cfgE"]:
+            lens(c)
+        sys.exit(0)
     if "--accept" in args:
         for c in [a for a in args if not a.startswith("--")] or list(CONFIGS):
             accept(c)
+        sys.exit(0)
+    if "--render-only" in args:  # --render-only cfg name ...: single renders
+        rest = [a for a in args if not a.startswith("--")]
+        render(rest[0], only=set(rest[1:]))
         sys.exit(0)
     only_render = "--render" in args
     for c in [a for a in args if not a.startswith("--")] or ["cfg1"]:

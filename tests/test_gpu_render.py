@@ -36,7 +36,8 @@ pytestmark = pytest.mark.gpu
 RENDERS = [("cfg1", "render", "green"), ("cfg2", "render_mira", "mira"), ("cfg2", "render_green", "green"),
            ("cfg1", "render_accmap", "green"), ("cfg3", "render", "green"), ("cfgL", "render", "green"),
            ("cfgE", "render", "green")]
-SINGLE_STAGE = [("cfg1", "render_h2mc", "h2mc"), ("cfg1", "render_mcmc", "mcmc")]
+SINGLE_STAGE = [("cfg1", "render_h2mc", "h2mc"), ("cfg1", "render_mcmc", "mcmc"),
+                ("cfg1", "render_h2mc_lens", "h2mc")]
 
 
 def _fixture(cfg, name):
@@ -52,6 +53,8 @@ def _scene(cfg, dr_type, root, name="render"):
     d = os.path.join(root, "%s_%s_%s" % (cfg, dr_type, name))
     if name == "render_accmap":
         return scenegen.config1(d, spp=16, acceptance_map=True)
+    if name == "render_h2mc_lens":
+        return scenegen.config1(d, spp=16, integrator="h2mc")
     if dr_type in ("h2mc", "mcmc"):
         return scenegen.config1(d, spp=16, integrator=dr_type, extra={"lensperturbprob": "0"})
     if cfg == "cfg1":
@@ -261,8 +264,9 @@ def test_autotuner_keeps_the_chains(built_lib, scene_root):
 def test_single_stage_integrators_match_reference(built_lib, scene_root, cfg, name, integrator):
     """integrator=h2mc (H2MC small step with uniform mixing, h2mc.cpp:200-240,
     448-606) and integrator=mcmc (mcmc.cpp) against `dpt -d` renders of the
-    same scene, with lensperturbprob = 0 (the lens mutation is not part of this
-    build). Small-step ratio within 0.012, large step 0.006, image as above."""
+    same scene, h2mc with lensperturbprob = 0 and with the default 0.3 (the
+    lens mutation, h2mc.cpp:466-532). Small-step ratio within 0.012, large
+    step 0.006, lens 0.015, image as above."""
     from drmlt import scene as dscene
     from drmlt.integrator import Renderer
     ref = _fixture(cfg, name)
@@ -276,6 +280,12 @@ def test_single_stage_integrators_match_reference(built_lib, scene_root, cfg, na
     small = (st["stage1_accepted"] + st["stage2_h2mc_accepted"]) / (st["stage1"] + st["stage2_h2mc"])
     assert abs(large - ref["stats"]["large"][0]) <= 0.006, (large, ref["stats"]["large"])
     assert abs(small - ref["stats"]["small"][0]) <= 0.012, (small, ref["stats"]["small"])
+    if name == "render_h2mc_lens":
+        assert st["lens"] > 1000 and abs(st["lens"] - ref["stats"]["lens"][1]) < 0.1 * ref["stats"]["lens"][1]
+        lens = st["lens_accepted"] / st["lens"]
+        assert abs(lens - ref["stats"]["lens"][0]) <= 0.015, (lens, ref["stats"]["lens"])
+    else:
+        assert st["lens"] == 0
     np.testing.assert_allclose(img.mean(axis=(0, 1)), ref["mean"], rtol=0.02)
     rb = np.array(ref["blocks"]).reshape(8, 2, 8, 2, 3).mean(axis=(1, 3))
     H, W, _ = img.shape
