@@ -265,7 +265,8 @@ def main(argv=None):
     """Renders a few chain-loop iterations of a procedural scene (and optionally
     one ray-benchmark pass) -- a small driver for profiling runs:
     python -m drmlt.procedural config4 --iterations 4 --lanes 16 --warps 2 --graph 1
-    (--wavefront 1 or --persistent 1 --team-sms T select the other schedules)"""
+    (--wavefront 1 or --persistent 1 --team-sms T select the other schedules;
+    --integrator h2mc [--lens-prob P] the h2mc integrator with its lens mutation)"""
     import argparse
     from .integrator import Renderer
     ap = argparse.ArgumentParser()
@@ -284,15 +285,22 @@ def main(argv=None):
                          "(0: library default, -1: hyper-dual for every path)")
     ap.add_argument("--head-chains", type=int, default=0, help="two-tier stage 1: chains of the head tier")
     ap.add_argument("--head-lanes", type=int, default=0, help="two-tier stage 1: chains per warp of the head tier")
+    ap.add_argument("--integrator", default="drmlt", choices=["drmlt", "h2mc", "mcmc"])
+    ap.add_argument("--lens-prob", type=float, default=0.3, help="integrator=h2mc: lensperturbprob")
     a = ap.parse_args(argv)
     sd = globals()[a.scene]()
+    sd.options.integrator = a.integrator
+    sd.options.lensPerturbProb = a.lens_prob
     r = Renderer(sd, seed=77, use_graph=a.graph, stage_lanes=a.lanes, stage2_lanes=a.lanes2, deriv_warps=a.warps,
                  wavefront=a.wavefront, persistent=a.persistent, team_sms=a.team_sms,
                  adjoint_min_dim=a.adjoint_min_dim,
                  head_chains=a.head_chains, head_lanes=a.head_lanes)
     r.prepass()
     r.run(a.iterations)
-    out = {"mutations": r.stats()["mutations"], "run_ms": r.last_run_ms()}
+    st = r.stats()
+    out = {"mutations": st["mutations"], "run_ms": r.last_run_ms()}
+    if a.integrator == "h2mc":
+        out["lens"] = [st["lens"], st["lens_accepted"]]
     if a.rays:
         out["rays"] = r.ray_benchmark(a.rays, 1 << 21, 1)
     r.close()
