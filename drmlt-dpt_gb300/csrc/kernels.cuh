@@ -436,7 +436,14 @@ static __global__ void __launch_bounds__(kStageBlock) k_stage2(RunParams p) {
 // position (x.screen + offset) mod 1, PerturbLensBidir into the second slot,
 // the proposal's lens Gaussian, and the unclamped acceptance
 // exp(log N_z(-o) - log N_x(o)) lens(z) / lens(x) that k_finish clamps and draws.
-constexpr int kLensBlock = 64;
+// One chain per thread, one warp per block, so that the list's warps spread
+// over every SM: the kernel is large (two path walks, six hyper-dual path
+// evaluations, two Gaussians) and bound by instruction fetch once several of
+// its warps share an SM. Config 4, h2mc, per launch (ncu, serialised): 32
+// chains on each warp of 64-thread blocks 1.13-1.35 ms (the list's blocks on
+// ~86 SMs), 4 chains per warp 1.66-1.79 ms (8 warps per SM, 30 cycles of
+// instruction-fetch stall per issued instruction).
+constexpr int kLensBlock = 32;
 static __global__ void __launch_bounds__(kLensBlock) k_lens(RunParams p) {
     const int iter = *p.iterp;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
