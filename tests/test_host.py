@@ -43,7 +43,8 @@ def _declared_symbols():
 def test_header_declares_entry_points():
     names = _declared_symbols()
     for n in ("drmlt_create", "drmlt_prepass", "drmlt_run", "drmlt_get_film", "drmlt_path_grad_hess",
-              "drmlt_path_eval", "drmlt_path_adjoint", "drmlt_compute_gaussian", "drmlt_compute_gaussian_noalloc"):
+              "drmlt_path_eval", "drmlt_path_adjoint", "drmlt_compute_gaussian", "drmlt_compute_gaussian_noalloc",
+              "drmlt_lens_eval", "drmlt_lens_perturb"):
         assert n in names
 
 
@@ -60,6 +61,8 @@ def test_default_options_and_error_path_without_device(built_lib):
     fails with DRMLT_E_CUDA and a readable message (no silent CPU path)."""
     o = built_lib.default_options()
     assert o.large_step_prob == pytest.approx(0.3) and o.perturb_stddev == pytest.approx(0.01)
+    # lensPerturbProb / lensPerturbStdDev defaults (src/dptoptions.h:20-21)
+    assert o.lens_perturb_prob == pytest.approx(0.3) and o.lens_perturb_stddev == pytest.approx(0.01)
     try:
         import torch
         has_gpu = torch.cuda.is_available()
