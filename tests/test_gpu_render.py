@@ -231,6 +231,29 @@ def test_wavefront_takes_the_per_lane_steps(built_lib, scene_root, cfg, dr_type)
     np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-4, atol=1e-6)
 
 
+def test_lens_mutation_takes_the_same_steps_in_every_schedule(built_lib, scene_root):
+    """integrator=h2mc with its lens mutation: the lens kernel runs after stage 1
+    in the per-lane and the wavefront schedules, with and without graphs, for
+    other chain-group counts and chains per warp; the chains take the same steps
+    (integer counters identical, film equal up to the order of the splat
+    additions), and a chain whose lens score is zero takes the H2MC step."""
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    sd = dscene.load_scene(_scene("cfg1", "h2mc", scene_root, "render_h2mc_lens"))
+    assert sd.options.lensPerturbProb > 0
+    out = []
+    for kw in (dict(), dict(wavefront=1), dict(use_graph=0, chain_groups=3), dict(stage_lanes=4, stage2_lanes=8)):
+        with Renderer(sd, num_chains=4096, **kw) as r:
+            r.prepass()
+            r.run(12)
+            out.append((r.stats(), r.film().astype(np.float64)))
+    st0 = out[0][0]
+    assert st0["lens"] > 1000 and 0 < st0["lens_accepted"] < st0["lens"] and st0["stage2_h2mc"] > 1000
+    for st, film in out[1:]:
+        assert st == st0
+        np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
+
+
 def test_autotuner_keeps_the_chains(built_lib, scene_root):
     """drmlt_autotune runs real iterations under each candidate launch shape and
     settles on one of them; the render is the one an untuned render gives
