@@ -161,6 +161,9 @@ struct Renderer {
         return rc;
     }
     ~Renderer() {
+        if (hStats) cudaFreeHost(hStats);
+        for (cudaEvent_t e : statsEv)
+            if (e) cudaEventDestroy(e);
         if (graph) cudaGraphExecDestroy(graph);
         if (forkEv) cudaEventDestroy(forkEv);
         if (midEv) cudaEventDestroy(midEv);
@@ -891,6 +894,56 @@ struct Renderer {
         }
         k_set_iters<<<1, 32, 0, stream>>>(dIters, G, int(iterDone));
         CK(cudaEventRecord(ev0, stream));
+        if (int rc = enqueue(end, mutations)) return rc;
+        CK(cudaEventRecord(ev1, stream));
+        CK(cudaGetLastError());
+        CK(cudaEventSynchronize(ev1));
+        CK(cudaEventElapsedTime(&lastRunMs, ev0, ev1));
+        iterDone = end;
+        if (done) *done = mutations;
+        return DRMLT_OK;
+    }
+
+    // Pipelined stepping (drmlt_run_async / drmlt_wait_stats): the iterations
+    // and a copy of the statistics counters into pinned slot `slot`, enqueued
+    // on the handle's stream without a host wait. The persistent schedule
+    // (one cooperative launch that the host waits on) is not offered here.
+    unsigned long long *hStats = nullptr;  // 2 pinned slots of kNumStatsAll counters
+    cudaEvent_t statsEv[2] = {nullptr, nullptr};
+    int run_async(long long iterations, int slot, long long *done) {
+        if (!prepassDone) return fail(DRMLT_E_STATE, "run before prepass");
+        if (slot < 0 || slot > 1) return fail(DRMLT_E_ARG, "slot must be 0 or 1");
+        if (persistent_schedule()) return fail(DRMLT_E_STATE, "the persistent schedule has no pipelined run");
+        if (!hStats) {
+            CK(cudaMallocHost(&hStats, 2 * kNumStatsAll * sizeof(unsigned long long)));
+            for (int k = 0; k < 2; k++) CK(cudaEventCreateWithFlags(&statsEv[k], cudaEventDisableTiming));
+        }
+        const long long end = std::min(iterDone + iterations, total_iterations());
+        long long mutations = 0;
+        if (opt.use_graph && !graph) {
+            if (int rc = build_graph()) return rc;
+        }
+        k_set_iters<<<1, 32, 0, stream>>>(dIters, G, int(iterDone));
+        if (int rc = enqueue(end, mutations)) return rc;
+        CK(cudaMemcpyAsync(hStats + slot * kNumStatsAll, cv.stats, kNumStatsAll * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, stream));
+        CK(cudaEventRecord(statsEv[slot], stream));
+        CK(cudaGetLastError());
+        iterDone = end;
+        if (done) *done = mutations;
+        return DRMLT_OK;
+    }
+    int wait_stats(int slot, unsigned long long *h) {
+        if (slot < 0 || slot > 1 || !hStats) return fail(DRMLT_E_STATE, "no pipelined run in this slot");
+        CK(cudaEventSynchronize(statsEv[slot]));
+        std::memcpy(h, hStats + slot * kNumStatsAll, kNumStatsAll * sizeof(unsigned long long));
+        return DRMLT_OK;
+    }
+
+    // The chain-loop launches from iteration iterDone up to `end` on the
+    // handle's stream (graph replays, then per-stage launches on the group
+    // streams for iterations short of a whole graph), joined back into it.
+    int enqueue(long long end, long long &mutations) {
         long long it = iterDone;
         if (graph) {
             for (; it + graphIters <= end; it += graphIters) {
@@ -912,12 +965,6 @@ struct Renderer {
                 CK(cudaStreamWaitEvent(stream, gevents[g], 0));
             }
         }
-        CK(cudaEventRecord(ev1, stream));
-        CK(cudaGetLastError());
-        CK(cudaEventSynchronize(ev1));
-        CK(cudaEventElapsedTime(&lastRunMs, ev0, ev1));
-        iterDone = end;
-        if (done) *done = mutations;
         return DRMLT_OK;
     }
 
@@ -1147,6 +1194,14 @@ int drmlt_run(void *handle, int64_t iterations, int64_t *done) {
     return rc;
 }
 
+int drmlt_run_async(void *handle, int64_t iterations, int slot, int64_t *done) {
+    if (!handle) return fail(DRMLT_E_ARG, "null handle");
+    long long d = 0;
+    const int rc = static_cast<Renderer *>(handle)->run_async(iterations, slot, &d);
+    if (done) *done = d;
+    return rc;
+}
+
 int drmlt_render(void *handle) {
     if (!handle) return fail(DRMLT_E_ARG, "null handle");
     Renderer *r = static_cast<Renderer *>(handle);
@@ -1209,11 +1264,7 @@ int drmlt_get_partial_film(void *handle, float *rgb) {
     return static_cast<Renderer *>(handle)->partial_film(rgb);
 }
 
-int drmlt_get_stats(void *handle, drmlt_stats *st) {
-    if (!handle || !st) return fail(DRMLT_E_ARG, "null argument");
-    Renderer *r = static_cast<Renderer *>(handle);
-    unsigned long long h[kNumStatsAll];
-    CK(cudaMemcpy(h, r->cv.stats, sizeof(h), cudaMemcpyDeviceToHost));
+static void stats_from_counters(const unsigned long long *h, drmlt_stats *st) {
     st->large_step = h[kStatLarge];
     st->large_step_accepted = h[kStatLargeAcc];
     st->stage1 = h[kStatStage1];
@@ -1227,6 +1278,22 @@ int drmlt_get_stats(void *handle, drmlt_stats *st) {
     st->gaussians_fp64_fallback = h[kStatGaussFallback];
     st->lens = h[kStatLens];
     st->lens_accepted = h[kStatLensAcc];
+}
+
+int drmlt_get_stats(void *handle, drmlt_stats *st) {
+    if (!handle || !st) return fail(DRMLT_E_ARG, "null argument");
+    Renderer *r = static_cast<Renderer *>(handle);
+    unsigned long long h[kNumStatsAll];
+    CK(cudaMemcpy(h, r->cv.stats, sizeof(h), cudaMemcpyDeviceToHost));
+    stats_from_counters(h, st);
+    return DRMLT_OK;
+}
+
+int drmlt_wait_stats(void *handle, int slot, drmlt_stats *st) {
+    if (!handle || !st) return fail(DRMLT_E_ARG, "null argument");
+    unsigned long long h[kNumStatsAll];
+    if (int rc = static_cast<Renderer *>(handle)->wait_stats(slot, h)) return rc;
+    stats_from_counters(h, st);
     return DRMLT_OK;
 }
 

@@ -110,6 +110,8 @@ _SIGS = {
     "drmlt_prepass": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "drmlt_direct": (C.c_int, [C.c_void_p]),
     "drmlt_run": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "drmlt_run_async": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_int64)]),
+    "drmlt_wait_stats": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "drmlt_render": (C.c_int, [C.c_void_p]),
     "drmlt_get_film": (C.c_int, [C.c_void_p, C.c_void_p]),
     "drmlt_get_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),

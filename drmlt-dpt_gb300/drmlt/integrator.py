@@ -101,6 +101,19 @@ class Renderer:
         capi.check(capi.lib().drmlt_run(self.handle, int(iterations), C.byref(done)))
         return done.value
 
+    def run_async(self, iterations: int, slot: int) -> int:
+        """drmlt_run_async: enqueues the iterations and a copy of the statistics
+        into pinned slot `slot` (0 or 1) without waiting; returns the mutations."""
+        done = C.c_int64()
+        capi.check(capi.lib().drmlt_run_async(self.handle, int(iterations), int(slot), C.byref(done)))
+        return done.value
+
+    def wait_stats(self, slot: int) -> dict:
+        """drmlt_wait_stats: the statistics copied by the run_async call on `slot`."""
+        s = capi.Stats()
+        capi.check(capi.lib().drmlt_wait_stats(self.handle, int(slot), C.byref(s)))
+        return {k: getattr(s, k) for k, _ in capi.Stats._fields_}
+
     def render(self):
         capi.check(capi.lib().drmlt_render(self.handle))
 

@@ -235,6 +235,17 @@ int drmlt_direct(void *handle);
  * Returns the number of mutations done in *done (may be NULL). */
 int drmlt_run(void *handle, int64_t iterations, int64_t *done);
 
+/* Pipelined stepping for a host that reads every step's statistics without
+ * idling the GPU between steps: drmlt_run_async enqueues `iterations`
+ * iterations as drmlt_run does (not timed: drmlt_last_run_ms is not updated)
+ * and then a copy of the statistics counters into pinned slot `slot` (0 or
+ * 1), and returns without waiting; drmlt_wait_stats waits for the copy in
+ * `slot` and returns those statistics. A host keeps one step in flight:
+ * drmlt_run_async(step k, slot k % 2), then drmlt_wait_stats of step k - 1.
+ * Not for the persistent schedule (DRMLT_E_STATE). */
+int drmlt_run_async(void *handle, int64_t iterations, int slot, int64_t *done);
+int drmlt_wait_stats(void *handle, int slot, drmlt_stats *st);
+
 /* Integrator::Render (delayed.cpp:181-686): prepass + direct + all iterations. */
 int drmlt_render(void *handle);
 

@@ -254,6 +254,30 @@ def test_lens_mutation_takes_the_same_steps_in_every_schedule(built_lib, scene_r
         np.testing.assert_allclose(film, out[0][1], rtol=1e-4, atol=1e-6)
 
 
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_pipelined_steps_match_synchronous_steps(built_lib, scene_root, use_graph):
+    """drmlt_run_async with drmlt_wait_stats one step behind (the GPU never
+    waits for the host between steps) against drmlt_run + drmlt_get_stats: the
+    same statistics after every step and the same film."""
+    from drmlt import scene as dscene
+    from drmlt.integrator import Renderer
+    sd = dscene.load_scene(_scene("cfg2", "mira", scene_root))
+    with Renderer(sd, num_chains=4096, use_graph=use_graph) as a, \
+            Renderer(sd, num_chains=4096, use_graph=use_graph) as b:
+        a.prepass()
+        b.prepass()
+        sa, sb = [], []
+        n = 7
+        for k in range(n):
+            assert a.run(1) == b.run_async(1, k % 2)
+            sa.append(a.stats())
+            if k > 0:
+                sb.append(b.wait_stats((k - 1) % 2))
+        sb.append(b.wait_stats((n - 1) % 2))
+        assert sa == sb
+        np.testing.assert_allclose(b.film(), a.film(), rtol=1e-4, atol=1e-6)
+
+
 def test_autotuner_keeps_the_chains(built_lib, scene_root):
     """drmlt_autotune runs real iterations under each candidate launch shape and
     settles on one of them; the render is the one an untuned render gives
