@@ -674,6 +674,18 @@ static __global__ void __launch_bounds__(kStageBlock) k_finish(RunParams p) {
     flush_stats(acc, p.d.stats);
 }
 
+// MergeBuffer (src/image.h:76-93, delayed.cpp:681-685): direct * 1/directSpp +
+// indirect * 1/spp per channel, rounded after every operation as the host
+// loop it replaces did.
+static __global__ void k_merge_film(const float4 *ind, const float4 *dir, float dw, float iw, size_t n, float *rgb) {
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 d = dir[i], v = ind[i];
+    rgb[3 * i + 0] = __fadd_rn(__fmul_rn(dw, d.x), __fmul_rn(iw, v.x));
+    rgb[3 * i + 1] = __fadd_rn(__fmul_rn(dw, d.y), __fmul_rn(iw, v.y));
+    rgb[3 * i + 2] = __fadd_rn(__fmul_rn(dw, d.z), __fmul_rn(iw, v.z));
+}
+
 // One chain group's iteration counter, advanced after each of its iterations
 // on the group's stream (so a captured iteration replays as the next one).
 static __global__ void k_advance_iter(int *iterp) { *iterp += 1; }
