@@ -139,3 +139,52 @@ def test_lens_perturbation_vs_reference(renderers, cfg):
         bad += 0 if good else 1
     assert nvalid > len(refs) // 2
     assert bad <= max(1, len(refs) // 50), "%d / %d lens perturbations differ" % (bad, len(refs))
+
+
+IDENTITY_DEPTH = {"cfg3": 5, "cfgE": 5, "cfg4s": 12}
+IDENTITY_STEPS = {"cfg3": 4096, "cfgE": 4096, "cfg4s": 1 << 16}
+
+
+@pytest.mark.parametrize("cfg", ["cfg3", "cfgE", "cfg4s"])
+def test_lens_perturbation_to_the_own_screen_position_is_the_identity(renderers, cfg):
+    """A property that holds at any size, on random valid paths up to depth 12
+    (the miniature config 4): PerturbLensBidir of a state with a positive lens
+    score to its own screen position, aimed at its own lens vertex, gives the
+    state back as PerturbPathBidir with zero offsets re-traces it (both
+    evaluate the BSDF at the absolute-parameter vertices; the sampler that made
+    the state sampled them, whose pdfs can differ) -- the same hit triangles
+    and, for c >= 2, the same contribution (1e-3: the first camera vertex's
+    direction is recomputed toward the lens vertex) and lens score. For c = 1
+    the contribution differs by design: PerturbLensLastVertex multiplies the
+    throughput by its shading-normal factor with wi and wo swapped
+    (src/path.cpp:1862-1866), which differs from BSDFSampling's on
+    smooth-shaded vertices."""
+    r = renderers(cfg)
+    rng = np.random.default_rng(23)
+    n = IDENTITY_STEPS[cfg]
+    L = rng.integers(3, IDENTITY_DEPTH[cfg] + 1, n)
+    cam = np.array([rng.integers(1, x + 2) for x in L], np.int32)
+    lgt = (L + 1 - cam).astype(np.int32)
+    tapes = rng.random((n, 64 if IDENTITY_DEPTH[cfg] <= 8 else 128), dtype=np.float32)
+    tapes = np.minimum(tapes, np.float32(1.0 - 2 ** -24))
+    cnt, _, ct, pth, _ = r.replay(1, list(tapes), cam, lgt)
+    keep = np.nonzero(cnt == 1)[0]
+    paths, contrib = pth[keep], ct[keep, 0]
+    screen = np.ascontiguousarray(contrib["screen"], np.float32)
+    ev = r.lens_eval(paths, screen, contrib["ss"], lens_sigma=0.01, max_derivative_depth=IDENTITY_DEPTH[cfg])
+    sel = np.nonzero(ev["score"] > 0)[0]
+    assert len(sel) > 50
+    p0, c0 = r.perturb(paths[sel], np.zeros((len(sel), 24), np.float32))
+    out, c2, s2 = r.lens_perturb(paths[sel], screen[sel], ev["pos"][sel])
+    bad = 0
+    for j, i in enumerate(sel):
+        c, l = int(paths[i]["c"]), int(paths[i]["l"])
+        nv = (l - 1 if l > 1 else 0) + c - 1
+        good = bool(c2[j]["valid"]) and bool(c0[j]["valid"])
+        good = good and np.array_equal(out[j]["tri"][:nv], p0[j]["tri"][:nv])
+        if c >= 2:
+            good = good and rel_err(c2[j]["ls"], c0[j]["ls"], 1e-20) < 1e-3
+            good = good and np.allclose(c2[j]["rgb"], c0[j]["rgb"], rtol=1e-3, atol=1e-12)
+            good = good and rel_err(s2[j], ev["score"][i], 1e-20) < 1e-3
+        bad += 0 if good else 1
+    assert bad <= max(2, len(sel) // 100), "%d / %d identity lens perturbations differ" % (bad, len(sel))
